@@ -1,0 +1,133 @@
+/*
+ * mps_gb300 — C ABI of the GB300 (sm_103a) MPS time-step engine.
+ *
+ * The engine replaces the body of the reference's MPS class
+ * (iori3150/MPS src/mps.hpp:22-71, src/mps.cpp:96-130) behind plain C
+ * functions: host pointers and sizes in, status codes out, no C++ types.
+ * The particle state lives on the GPU in structure-of-arrays form, sorted
+ * by neighbour cell; it is copied in at create/upload and out at
+ * download.  One engine drives one GPU (the device current at create) and
+ * is single-threaded, like the reference's caller.
+ *
+ * Particle type codes follow ParticleType (src/particle.hpp:5):
+ * Ghost -1, Fluid 0, Wall 1, DummyWall 2.  Boundary codes follow
+ * BoundaryCondition (src/particle.hpp:20): Ignored 0, Surface 1, Inner 2.
+ * Particle ids are array indices (src/mps.cpp:192,290 rely on the same).
+ *
+ * Every function returns MPS_OK (0) or an MPS_ERR_* code;
+ * mps_last_error() returns the message of the last failure.
+ */
+#ifndef MPS_GB300_H
+#define MPS_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MPS_OK = 0,
+    MPS_ERR_ARG = 1,         /* invalid argument (null pointer, bad size, bad setting) */
+    MPS_ERR_CUDA = 2,        /* a CUDA call failed; the engine should be destroyed */
+    MPS_ERR_CAPACITY = 3,    /* a particle had more neighbours than the engine's list capacity */
+    MPS_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up (kernel returned early) */
+    MPS_ERR_NO_DEVICE = 5    /* no CUDA device, or not an sm_103 part */
+};
+
+enum { MPS_PRECISION_FP64 = 0, MPS_PRECISION_MIXED = 1 };
+
+/* Settings::load's values (src/settings.hpp:35-86) in absolute units:
+ * radii and the collision distance are ratio * particle distance. */
+typedef struct {
+    int32_t dim;
+    int32_t quasi_compressibility_on;
+    int32_t higher_order_on;
+    int32_t pad0;
+    double particle_distance;
+    double dt;
+    double domain_min[3];
+    double domain_max[3];
+    double density;
+    double kinematic_viscosity;
+    double gravity[3];
+    double re_pressure;
+    double re_viscosity;
+    double re_surface;
+    double surface_threshold;
+    double compressibility;
+    double higher_order_gamma;
+    double relaxation;
+    double collision_distance;
+    double restitution;
+    double cfl;
+} mps_params;
+
+/* What one step reports (the reference returns only the Courant number,
+ * src/mps.cpp:129, and counts debug events in MPS::debugLogCount). */
+typedef struct {
+    double courant;                 /* max |v| dt / l0 over fluid (src/mps.cpp:547-571) */
+    double cg_relative_residual;    /* ||b - A x|| / ||b|| of the returned pressure */
+    int64_t cg_iterations;          /* Krylov iterations (inner ones for MIXED) */
+    int32_t refinements;            /* FP64 residual recomputations (MIXED), else 0 */
+    int32_t debug_log_count;        /* cumulative, as MPS::debugLogCount */
+    int32_t n_collision_candidates; /* pairs the collision pass tested (dist < cd) */
+    int32_t n_new_ghosts;           /* particles that left the domain this step */
+    int32_t n_unconnected;          /* Inner particles without a Dirichlet path */
+    int32_t n_inner;
+    int32_t n_surface;
+    int32_t status;                 /* MPS_OK or the MPS_ERR_* of a device-side failure */
+    float ms_step;                  /* device time of the whole step */
+    float ms_solve;                 /* device time of the pressure solve */
+} mps_step_stats;
+
+typedef struct mps_engine mps_engine;
+
+/* MPS::MPS + MPS::loadInitialState (src/mps.cpp:18-36, 96-109): copies the
+ * initial condition to the GPU and computes the initial number density.
+ * pos/vel are n*3 doubles (x,y,z per particle), type n ints. */
+int mps_create(const mps_params* prm, int32_t n, const double* pos, const double* vel,
+               const int32_t* type, mps_engine** out);
+int mps_destroy(mps_engine* e);
+
+/* Pressure solver: MPS_PRECISION_FP64 is the reference's Jacobi-CG in FP64
+ * (tolerance default machine epsilon, iteration cap default 2n, as Eigen's
+ * defaults, src/mps.cpp:452-460).  MPS_PRECISION_MIXED runs FP32 Krylov
+ * iterations with FP64 dot products inside FP64 iterative refinement until
+ * ||b - A x|| <= tol ||b|| (default tol 1e-10).  tol <= 0 / max_iter <= 0
+ * keep the defaults. */
+int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_iter);
+
+/* MPS::stepForward (src/mps.cpp:111-130). */
+int mps_step(mps_engine* e, int32_t is_time_to_export, mps_step_stats* stats);
+
+/* n_steps consecutive non-export steps; stats of the last step. */
+int mps_run(mps_engine* e, int32_t n_steps, mps_step_stats* stats);
+
+/* Particle state in id order (host pointers; any may be NULL). */
+int mps_download(mps_engine* e, double* pos, double* vel, double* pressure,
+                 double* min_pressure, double* ndr, int32_t* type, int32_t* bc,
+                 int32_t* dirichlet);
+
+/* Replace positions, velocities and types (same n) — the host-owned state
+ * of the reference's std::vector<Particle>.  Any pointer may be NULL to keep
+ * that field. */
+int mps_upload(mps_engine* e, const double* pos, const double* vel, const int32_t* type);
+
+int32_t mps_particle_count(const mps_engine* e);
+
+/* Parity/debug views of the last step, in id order. */
+/* Neighbour lists of the last neighbour build (src/mps.cpp:585-619) as CSR;
+ * call with ids == NULL to get the total in *total. */
+int mps_neighbors(mps_engine* e, int64_t* offsets, int32_t* ids, double* dist, int64_t* total);
+/* Source term and PPE matrix (CSR, ascending columns, Dirichlet fix applied). */
+int mps_system(mps_engine* e, double* source, int64_t* row_ptr, int32_t* col, double* val,
+               int64_t* nnz);
+/* Collision candidate pairs (i, j, stale distance) in processing order. */
+int mps_collisions(mps_engine* e, int32_t* pi, int32_t* pj, double* dist, int32_t* count);
+
+const char* mps_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPS_GB300_H */

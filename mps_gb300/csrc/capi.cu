@@ -1,0 +1,652 @@
+// C ABI of the engine (include/mps_gb300.h): device memory, the per-step
+// kernel sequence of MPS::stepForward (src/mps.cpp:111-130), and the
+// host<->device views in particle-id order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/mps_gb300.h"
+#include "engine.cuh"
+
+using namespace mpsg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CU(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t err_ = (call);                                                        \
+        if (err_ != cudaSuccess)                                                          \
+            return fail(MPS_ERR_CUDA, std::string(#call " failed: ") + cudaGetErrorString(err_)); \
+    } while (0)
+
+// RefValues::RefValues, src/mps.cpp:132-163 (host, same operation order).
+void ref_values(int dim, double l0, double re, double* n0o, double* lamo) {
+    double n0 = 0.0, lam = 0.0;
+    int zb = dim == 2 ? 0 : -4, ze = dim == 2 ? 1 : 5;
+    for (int ix = -4; ix < 5; ix++)
+        for (int iy = -4; iy < 5; iy++)
+            for (int iz = zb; iz < ze; iz++) {
+                if (ix == 0 && iy == 0 && iz == 0) continue;
+                double x = l0 * (double)ix, y = l0 * (double)iy, z = l0 * (double)iz;
+                double dist = std::sqrt((x * x + y * y) + z * z);
+                double w = dist < re ? (re / dist) - 1.0 : 0.0;
+                n0 += w;
+                lam += (dist * dist) * w;
+            }
+    lam /= n0;
+    *n0o = n0;
+    *lamo = lam;
+}
+
+// Smallest t with sqrt_rn(t) >= re, so that sqrt_rn(d2) < re <=> d2 < t.
+double sq_threshold(double re) {
+    if (!(re > 0.0)) return 0.0;
+    double t = re * re;
+    while (t > 0.0 && std::sqrt(t) >= re) t = std::nextafter(t, 0.0);
+    while (std::sqrt(t) < re) t = std::nextafter(t, std::numeric_limits<double>::infinity());
+    return t;
+}
+
+int lattice_count(int dim, double ratio) {
+    int r = (int)std::ceil(ratio) + 1, cnt = 0;
+    for (int ix = -r; ix <= r; ix++)
+        for (int iy = -r; iy <= r; iy++)
+            for (int iz = (dim == 2 ? 0 : -r); iz <= (dim == 2 ? 0 : r); iz++) {
+                double d = std::sqrt((double)(ix * ix + iy * iy + iz * iz));
+                if ((ix || iy || iz) && d < ratio) cnt++;
+            }
+    return cnt;
+}
+
+__global__ void k_from_host_order(int n, const int32_t* __restrict__ id, const double* __restrict__ src,
+                                  int comps, int comp, double* __restrict__ dst) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = src[(size_t)id[k] * comps + comp];
+}
+__global__ void k_type_from_host_order(int n, const int32_t* __restrict__ id,
+                                       const int32_t* __restrict__ src, int8_t* __restrict__ dst) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = (int8_t)src[id[k]];
+}
+__global__ void k_to_host_order(int n, const int32_t* __restrict__ id, const double* __restrict__ src,
+                                int comps, int comp, double* __restrict__ dst) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[(size_t)id[k] * comps + comp] = src[k];
+}
+__global__ void k_fill_host_order(int n, const int32_t* __restrict__ id, double v, int comps,
+                                  int comp, double* __restrict__ dst) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[(size_t)id[k] * comps + comp] = v;
+}
+__global__ void k_i8_to_host_order(int n, const int32_t* __restrict__ id, const int8_t* __restrict__ src,
+                                   int32_t* __restrict__ dst) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[id[k]] = src[k];
+}
+__global__ void k_iota(int n, int32_t* a) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) a[k] = k;
+}
+
+}  // namespace
+
+struct mps_engine {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    mps_params P{};
+    Consts c{};
+    int n = 0, n_pad = 0;
+    StateBuf buf[2]{};
+    int cur = 0;
+    SortScratch sc{};
+    NbList nb{};
+    Ppe A{};
+    Krylov kv{};
+    int32_t *cand_cnt = nullptr, *cand_base = nullptr;
+    CollPair* pairs = nullptr;
+    int32_t pair_cap = 0;
+    int32_t* parent = nullptr;
+    int8_t* has_surface = nullptr;
+    double *ax = nullptr, *ay = nullptr, *az = nullptr;
+    double* stage = nullptr;  // 3 n doubles for host transfers
+    int32_t* stage_i = nullptr;
+    DevStats* ds = nullptr;
+    DevStats* hs = nullptr;  // pinned
+    int precision = MPS_PRECISION_FP64;
+    double tol = std::numeric_limits<double>::epsilon();
+    int64_t max_iter = 0;
+    int32_t debug_log_count = 0;
+    cudaEvent_t ev[4]{};
+    std::vector<void*> allocs;
+
+    template <typename T>
+    cudaError_t alloc(T** p, size_t count) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) {
+            allocs.push_back(q);
+            *p = (T*)q;
+        }
+        return e;
+    }
+    StateBuf& S() { return buf[cur]; }
+    void swap() { cur ^= 1; }
+};
+
+namespace {
+
+int alloc_state(mps_engine* e, StateBuf& s) {
+    size_t n = e->n_pad;
+    CU(e->alloc(&s.x, n));
+    CU(e->alloc(&s.y, n));
+    CU(e->alloc(&s.z, n));
+    CU(e->alloc(&s.vx, n));
+    CU(e->alloc(&s.vy, n));
+    CU(e->alloc(&s.vz, n));
+    CU(e->alloc(&s.p, n));
+    CU(e->alloc(&s.minp, n));
+    CU(e->alloc(&s.ndr, n));
+    CU(e->alloc(&s.nd_last, n));
+    CU(e->alloc(&s.id, n));
+    CU(e->alloc(&s.type, n));
+    CU(e->alloc(&s.bc, n));
+    CU(e->alloc(&s.dir, n));
+    return MPS_OK;
+}
+
+int check_status(mps_engine* e) {
+    int32_t s = e->hs->status;
+    if (s & ST_TIMEOUT) return fail(MPS_ERR_TIMEOUT, "a bounded device-side wait gave up");
+    if (s & ST_CAPACITY)
+        return fail(MPS_ERR_CAPACITY, "neighbour or collision list capacity exceeded (max neighbours " +
+                                          std::to_string(e->hs->max_neighbors) + ", capacity " +
+                                          std::to_string(e->c.K) + ")");
+    return MPS_OK;
+}
+
+// One MPS::stepForward.  Launches only; the caller synchronises.
+void enqueue_step(mps_engine* e, bool do_export) {
+    Consts& c = e->c;
+    cudaStream_t st = e->st;
+    const int mixed = e->precision == MPS_PRECISION_MIXED;
+    // setNeighbors + calcGravity + calcViscosity + moveParticles
+    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, st);
+    e->swap();
+    launch_explicit(c, e->S(), e->buf[e->cur ^ 1], e->sc, mixed, e->ds, st);
+    e->swap();
+    // setNeighbors + collision
+    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, st);
+    e->swap();
+    launch_collision(c, e->S(), e->sc, e->cand_cnt, e->cand_base, nullptr, e->pairs, e->pair_cap,
+                     e->sc.scan_tmp, e->ds, st);
+    // setNeighbors + calcPressure
+    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, st);
+    e->swap();
+    launch_build_list(c, e->S(), e->sc, e->nb, e->ds, st);
+    launch_bc_source(c, e->S(), e->nb, e->A, e->ds, st);
+    launch_assemble(c, e->S(), e->nb, e->A, st);
+    launch_dirichlet(c, e->S(), e->nb, e->A, e->parent, e->has_surface, e->ds, st);
+    cudaEventRecord(e->ev[2], st);
+    int64_t mi = e->max_iter > 0 ? e->max_iter : 2 * (int64_t)c.n;
+    if (mixed)
+        launch_solve_mixed(c, e->A, e->kv, e->tol, mi, e->ds, st);
+    else
+        launch_solve_fp64(c, e->A, e->kv, e->tol, mi, e->ds, st);
+    cudaEventRecord(e->ev[3], st);
+    // removeNegativePressure, setMinimumPressure, calcPressureGradient,
+    // moveParticlesWithPressureGradient, getCourantNumber
+    launch_pressure_post(c, e->S(), e->nb, e->kv.x, e->ax, e->ay, e->az, mixed, e->ds, st);
+    if (do_export || c.ho_on) {  // setNumberDensity
+        launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, st);
+        e->swap();
+        launch_build_list(c, e->S(), e->sc, e->nb, e->ds, st);
+        launch_number_density(c, e->S(), e->nb, st);
+    }
+}
+
+void fill_stats(mps_engine* e, mps_step_stats* out) {
+    DevStats& h = *e->hs;
+    double cour = 0.0;
+    unsigned long long b = h.courant_bits;
+    std::memcpy(&cour, &b, sizeof cour);
+    e->debug_log_count += h.n_new_ghosts + h.n_unconnected;
+    if (cour > e->P.cfl) e->debug_log_count++;  // src/mps.cpp:559-565
+    if (!out) return;
+    out->courant = cour;
+    out->cg_relative_residual = h.cg_rel_residual;
+    out->cg_iterations = h.cg_iterations;
+    out->refinements = h.refinements;
+    out->debug_log_count = e->debug_log_count;
+    out->n_collision_candidates = h.n_cand;
+    out->n_new_ghosts = h.n_new_ghosts;
+    out->n_unconnected = h.n_unconnected;
+    out->n_inner = h.n_inner;
+    out->n_surface = h.n_surface;
+    out->status = h.status;
+    float ms = 0.f, ms2 = 0.f;
+    cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]);
+    cudaEventElapsedTime(&ms2, e->ev[2], e->ev[3]);
+    out->ms_step = ms;
+    out->ms_solve = ms2;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mps_last_error(void) { return g_last_error.c_str(); }
+
+int32_t mps_particle_count(const mps_engine* e) { return e ? e->n : 0; }
+
+int mps_create(const mps_params* prm, int32_t n, const double* pos, const double* vel,
+               const int32_t* type, mps_engine** out) {
+    if (!prm || !pos || !vel || !type || !out || n <= 0)
+        return fail(MPS_ERR_ARG, "mps_create: null pointer or non-positive particle count");
+    *out = nullptr;
+    const mps_params& P = *prm;
+    if (!(P.particle_distance > 0) || !(P.dt > 0) || !(P.density > 0) || (P.dim != 2 && P.dim != 3))
+        return fail(MPS_ERR_ARG, "mps_create: invalid dim, particle distance, dt or density");
+    if (!(P.re_pressure > 0) || !(P.re_viscosity > 0) || !(P.re_surface > 0))
+        return fail(MPS_ERR_ARG, "mps_create: effective radii must be positive");
+    for (int32_t i = 0; i < n; i++)
+        if (type[i] < -1 || type[i] > 2)
+            return fail(MPS_ERR_ARG, "mps_create: particle type outside {-1,0,1,2}");
+    int dev = 0, ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(MPS_ERR_NO_DEVICE, "no CUDA device");
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    CU(cudaGetDeviceProperties(&prop, dev));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(MPS_ERR_NO_DEVICE, "this build targets sm_103 (GB300); device is sm_" +
+                                           std::to_string(prop.major) + std::to_string(prop.minor));
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) return fail(MPS_ERR_NO_DEVICE, "device lacks cooperative launch");
+
+    mps_engine* e = new mps_engine();
+    e->device = dev;
+    e->P = P;
+    e->n = n;
+    e->n_pad = (n + 31) & ~31;
+    Consts& c = e->c;
+    c.n = n;
+    c.dim = P.dim;
+    c.qc_on = P.quasi_compressibility_on != 0;
+    c.ho_on = P.higher_order_on != 0;
+    c.l0 = P.particle_distance;
+    c.dt = P.dt;
+    for (int d = 0; d < 3; d++) {
+        c.dmin[d] = P.domain_min[d];
+        c.dmax[d] = P.domain_max[d];
+        c.g[d] = P.gravity[d];
+    }
+    c.rho = P.density;
+    c.re_p = P.re_pressure;
+    c.re_v = P.re_viscosity;
+    c.re_s = P.re_surface;
+    c.re_max = std::max({P.re_pressure, P.re_viscosity, P.re_surface});  // src/settings.cpp:138
+    c.cd = P.collision_distance;
+    c.len = c.re_max;
+    // Bucket::Bucket, src/bucket.cpp:10-22
+    c.numX = (int)((P.domain_max[0] - P.domain_min[0]) / c.len) + 3;
+    c.numY = (int)((P.domain_max[1] - P.domain_min[1]) / c.len) + 3;
+    c.numZ = (int)((P.domain_max[2] - P.domain_min[2]) / c.len) + 3;
+    bool planar = P.gravity[2] == 0.0;
+    for (int32_t i = 0; i < n && planar; i++)
+        planar = pos[3 * i + 2] == pos[2] && vel[3 * i + 2] == 0.0;
+    c.planar = planar;
+    c.z0 = pos[2];
+    double nk = planar ? (double)c.numX * c.numY : (double)c.numX * c.numY * c.numZ;
+    if (nk > 1.5e9) {
+        delete e;
+        return fail(MPS_ERR_ARG, "mps_create: bucket grid too large for the domain and radius");
+    }
+    c.nkeys = (int32_t)nk;
+    c.t_p = sq_threshold(c.re_p);
+    c.t_v = sq_threshold(c.re_v);
+    c.t_s = sq_threshold(c.re_s);
+    c.t_max = sq_threshold(c.re_max);
+    c.t_cd = sq_threshold(c.cd);
+    ref_values(P.dim, c.l0, c.re_p, &c.n0_p, &c.lam_p);
+    ref_values(P.dim, c.l0, c.re_v, &c.n0_v, &c.lam_v);
+    ref_values(P.dim, c.l0, c.re_s, &c.n0_s, &c.lam_s);
+    const double dimd = (double)P.dim;
+    c.beta_n0s = P.surface_threshold * c.n0_s;
+    c.visc_a = (P.kinematic_viscosity * (2.0 * dimd)) / (c.n0_v * c.lam_v);
+    c.mat_c = 2.0 * dimd / (c.lam_p * c.n0_p);
+    c.qc_term = P.compressibility / (P.dt * P.dt);
+    c.src_g1 = P.relaxation * (1.0 / (P.dt * P.dt));
+    c.ho_g1 = P.higher_order_gamma * (1.0 / (P.dt * P.dt));
+    c.ho_c = 1.0 / (c.n0_p * P.dt);
+    c.grad_scale = dimd / c.n0_p;
+    c.e = P.restitution;
+    c.fre_v = (float)c.re_v;
+    c.fre_p = (float)c.re_p;
+    c.fvisc_a = (float)c.visc_a;
+    c.fgrad_scale = (float)c.grad_scale;
+    int lc = lattice_count(P.dim, c.re_max / c.l0);
+    c.K = std::max(32, ((2 * lc + 8 + 31) / 32) * 32);
+    e->nb.n_pad = e->n_pad;
+
+    int rc = MPS_OK;
+    auto bail = [&](int code) {
+        mps_destroy(e);
+        return code;
+    };
+    cudaError_t ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) return bail(fail(MPS_ERR_CUDA, cudaGetErrorString(ce)));
+    for (auto& ev : e->ev)
+        if (cudaEventCreate(&ev) != cudaSuccess) return bail(fail(MPS_ERR_CUDA, "event create"));
+    if ((rc = alloc_state(e, e->buf[0])) || (rc = alloc_state(e, e->buf[1]))) return bail(rc);
+    const size_t np = e->n_pad, K = c.K;
+    if (e->alloc(&e->sc.key, np) || e->alloc(&e->sc.rank, np) || e->alloc(&e->sc.perm, np) ||
+        e->alloc(&e->sc.skey, np) || e->alloc(&e->sc.cell_count, (size_t)c.nkeys + 2) ||
+        e->alloc(&e->sc.cell_start, (size_t)c.nkeys + 2) ||
+        e->alloc(&e->sc.scan_tmp, scan_tmp_ints(std::max(c.nkeys + 1, n + 1))) ||
+        e->alloc(&e->nb.cnt, np) || e->alloc(&e->nb.slot, np * K) || e->alloc(&e->nb.dist, np * K) ||
+        e->alloc(&e->nb.wp, np * K) || e->alloc(&e->A.src, np) || e->alloc(&e->A.diag, np) ||
+        e->alloc(&e->A.offcnt, np) || e->alloc(&e->A.col, np * K) || e->alloc(&e->A.val, np * K) ||
+        e->alloc(&e->A.slice_w, np / 32 + 1) || e->alloc(&e->A.val32, np * K) ||
+        e->alloc(&e->A.diag32, np) || e->alloc(&e->kv.x, np) || e->alloc(&e->kv.r, np) ||
+        e->alloc(&e->kv.p, np) || e->alloc(&e->kv.q, np) || e->alloc(&e->kv.z, np) ||
+        e->alloc(&e->kv.inv_diag, np) || e->alloc(&e->kv.r32, np) || e->alloc(&e->kv.p32, np) ||
+        e->alloc(&e->kv.q32, np) || e->alloc(&e->kv.z32, np) || e->alloc(&e->kv.x32, np) ||
+        e->alloc(&e->kv.inv_diag32, np) || e->alloc(&e->kv.barrier, 4) ||
+        e->alloc(&e->cand_cnt, np + 1) || e->alloc(&e->cand_base, np + 2) ||
+        e->alloc(&e->parent, np) || e->alloc(&e->has_surface, np) || e->alloc(&e->ax, np) ||
+        e->alloc(&e->ay, np) || e->alloc(&e->az, np) || e->alloc(&e->stage, 3 * np) ||
+        e->alloc(&e->stage_i, np) || e->alloc(&e->ds, 1))
+        return bail(fail(MPS_ERR_CUDA, "cudaMalloc failed (out of device memory?)"));
+    e->pair_cap = (int32_t)std::min<size_t>(4 * np + 1024, (size_t)1 << 30);
+    if (e->alloc(&e->pairs, e->pair_cap)) return bail(fail(MPS_ERR_CUDA, "cudaMalloc pairs"));
+    solver_setup(e->kv, e->n_pad, dev);
+    if (e->alloc(&e->kv.partials, (size_t)e->kv.grid * 8))
+        return bail(fail(MPS_ERR_CUDA, "cudaMalloc partials"));
+    if (cudaMallocHost(&e->hs, sizeof(DevStats)) != cudaSuccess)
+        return bail(fail(MPS_ERR_CUDA, "cudaMallocHost"));
+    // zero-init everything that a kernel may read before writing
+    StateBuf& s = e->buf[0];
+    for (int b = 0; b < 2; b++) {
+        StateBuf& t = e->buf[b];
+        cudaMemsetAsync(t.p, 0, np * 8, e->st);
+        cudaMemsetAsync(t.minp, 0, np * 8, e->st);
+        cudaMemsetAsync(t.ndr, 0, np * 8, e->st);
+        cudaMemsetAsync(t.nd_last, 0, np * 8, e->st);
+        cudaMemsetAsync(t.bc, 0, np, e->st);
+        cudaMemsetAsync(t.dir, 0, np, e->st);
+        cudaMemsetAsync(t.z, 0, np * 8, e->st);
+        cudaMemsetAsync(t.vz, 0, np * 8, e->st);
+    }
+    cudaMemsetAsync(e->kv.x, 0, np * 8, e->st);
+    cudaMemsetAsync(e->nb.cnt, 0, np * 4, e->st);
+    k_iota<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id);
+    // upload the initial condition (identity slot order, ids = indices)
+    for (int comp = 0; comp < 3; comp++) {
+        double* pd[3] = {s.x, s.y, s.z};
+        double* vd[3] = {s.vx, s.vy, s.vz};
+        CU(cudaMemcpyAsync(e->stage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
+        k_from_host_order<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id, e->stage, 3, comp, pd[comp]);
+        CU(cudaMemcpyAsync(e->stage, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
+        k_from_host_order<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id, e->stage, 3, comp, vd[comp]);
+    }
+    CU(cudaMemcpyAsync(e->stage_i, type, sizeof(int32_t) * n, cudaMemcpyHostToDevice, e->st));
+    k_type_from_host_order<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id, e->stage_i, s.type);
+    e->cur = 0;
+    // MPS::loadInitialState's setNumberDensity (src/mps.cpp:106)
+    CU(cudaMemsetAsync(e->ds, 0, sizeof(DevStats), e->st));
+    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->st);
+    e->swap();
+    launch_initial_number_density(c, e->S(), e->sc, e->nb, e->ds, e->st);
+    CU(cudaMemcpyAsync(e->hs, e->ds, sizeof(DevStats), cudaMemcpyDeviceToHost, e->st));
+    CU(cudaStreamSynchronize(e->st));
+    CU(cudaGetLastError());
+    if ((rc = check_status(e))) return bail(rc);
+    *out = e;
+    return MPS_OK;
+}
+
+int mps_destroy(mps_engine* e) {
+    if (!e) return MPS_OK;
+    if (e->st) cudaStreamSynchronize(e->st);
+    for (void* p : e->allocs) cudaFree(p);
+    if (e->hs) cudaFreeHost(e->hs);
+    for (auto& ev : e->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (e->st) cudaStreamDestroy(e->st);
+    delete e;
+    return MPS_OK;
+}
+
+int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_iter) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    if (precision != MPS_PRECISION_FP64 && precision != MPS_PRECISION_MIXED)
+        return fail(MPS_ERR_ARG, "unknown precision");
+    e->precision = precision;
+    e->tol = tol > 0 ? tol
+                     : (precision == MPS_PRECISION_FP64 ? std::numeric_limits<double>::epsilon() : 1e-10);
+    e->max_iter = max_iter > 0 ? max_iter : 0;
+    return MPS_OK;
+}
+
+int mps_run(mps_engine* e, int32_t n_steps, mps_step_stats* stats) {
+    if (!e || n_steps < 0) return fail(MPS_ERR_ARG, "mps_run: bad arguments");
+    for (int32_t s = 0; s < n_steps; s++) {
+        CU(cudaMemsetAsync(e->ds, 0, sizeof(DevStats), e->st));
+        CU(cudaEventRecord(e->ev[0], e->st));
+        enqueue_step(e, false);
+        CU(cudaEventRecord(e->ev[1], e->st));
+        CU(cudaMemcpyAsync(e->hs, e->ds, sizeof(DevStats), cudaMemcpyDeviceToHost, e->st));
+        CU(cudaStreamSynchronize(e->st));
+        CU(cudaGetLastError());
+        fill_stats(e, stats);
+        int rc = check_status(e);
+        if (rc) return rc;
+    }
+    return MPS_OK;
+}
+
+int mps_step(mps_engine* e, int32_t is_time_to_export, mps_step_stats* stats) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    CU(cudaMemsetAsync(e->ds, 0, sizeof(DevStats), e->st));
+    CU(cudaEventRecord(e->ev[0], e->st));
+    enqueue_step(e, is_time_to_export != 0);
+    CU(cudaEventRecord(e->ev[1], e->st));
+    CU(cudaMemcpyAsync(e->hs, e->ds, sizeof(DevStats), cudaMemcpyDeviceToHost, e->st));
+    CU(cudaStreamSynchronize(e->st));
+    CU(cudaGetLastError());
+    fill_stats(e, stats);
+    return check_status(e);
+}
+
+int mps_download(mps_engine* e, double* pos, double* vel, double* pressure, double* min_pressure,
+                 double* ndr, int32_t* type, int32_t* bc, int32_t* dirichlet) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    const int n = e->n, T = 256, G = (n + 255) / 256;
+    StateBuf& s = e->S();
+    // planar engines do not store z / v_z: they are the constants z0 / 0
+    auto vec3 = [&](double* host, double* d[3], double zconst) -> int {
+        for (int comp = 0; comp < 3; comp++) {
+            if (comp == 2 && e->c.planar)
+                k_fill_host_order<<<G, T, 0, e->st>>>(n, s.id, zconst, 3, 2, e->stage);
+            else
+                k_to_host_order<<<G, T, 0, e->st>>>(n, s.id, d[comp], 3, comp, e->stage);
+        }
+        CU(cudaMemcpyAsync(host, e->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->st));
+        CU(cudaStreamSynchronize(e->st));
+        return MPS_OK;
+    };
+    int rc;
+    if (pos) {
+        double* d[3] = {s.x, s.y, s.z};
+        if ((rc = vec3(pos, d, e->c.z0))) return rc;
+    }
+    if (vel) {
+        double* d[3] = {s.vx, s.vy, s.vz};
+        if ((rc = vec3(vel, d, 0.0))) return rc;
+    }
+    auto scal = [&](double* host, double* d) -> int {
+        k_to_host_order<<<G, T, 0, e->st>>>(n, s.id, d, 1, 0, e->stage);
+        CU(cudaMemcpyAsync(host, e->stage, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
+        CU(cudaStreamSynchronize(e->st));
+        return MPS_OK;
+    };
+    if (pressure && (rc = scal(pressure, s.p))) return rc;
+    if (min_pressure && (rc = scal(min_pressure, s.minp))) return rc;
+    if (ndr && (rc = scal(ndr, s.ndr))) return rc;
+    auto i8 = [&](int32_t* host, int8_t* d) -> int {
+        k_i8_to_host_order<<<G, T, 0, e->st>>>(n, s.id, d, e->stage_i);
+        CU(cudaMemcpyAsync(host, e->stage_i, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, e->st));
+        CU(cudaStreamSynchronize(e->st));
+        return MPS_OK;
+    };
+    if (type && (rc = i8(type, s.type))) return rc;
+    if (bc && (rc = i8(bc, s.bc))) return rc;
+    if (dirichlet && (rc = i8(dirichlet, s.dir))) return rc;
+    CU(cudaGetLastError());
+    return MPS_OK;
+}
+
+int mps_upload(mps_engine* e, const double* pos, const double* vel, const int32_t* type) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    const int n = e->n, T = 256, G = (n + 255) / 256;
+    StateBuf& s = e->S();
+    if (e->c.planar) {
+        for (int i = 0; i < n; i++)
+            if ((pos && pos[3 * i + 2] != e->c.z0) || (vel && vel[3 * i + 2] != 0.0))
+                return fail(MPS_ERR_ARG, "mps_upload: a planar engine keeps z and v_z constant");
+    }
+    int comps = e->c.planar ? 2 : 3;
+    if (pos) {
+        double* d[3] = {s.x, s.y, s.z};
+        CU(cudaMemcpyAsync(e->stage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
+        for (int comp = 0; comp < comps; comp++)
+            k_from_host_order<<<G, T, 0, e->st>>>(n, s.id, e->stage, 3, comp, d[comp]);
+        CU(cudaStreamSynchronize(e->st));
+    }
+    if (vel) {
+        double* d[3] = {s.vx, s.vy, s.vz};
+        CU(cudaMemcpyAsync(e->stage, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
+        for (int comp = 0; comp < comps; comp++)
+            k_from_host_order<<<G, T, 0, e->st>>>(n, s.id, e->stage, 3, comp, d[comp]);
+        CU(cudaStreamSynchronize(e->st));
+    }
+    if (type) {
+        for (int i = 0; i < n; i++)
+            if (type[i] < -1 || type[i] > 2) return fail(MPS_ERR_ARG, "mps_upload: bad particle type");
+        CU(cudaMemcpyAsync(e->stage_i, type, sizeof(int32_t) * n, cudaMemcpyHostToDevice, e->st));
+        k_type_from_host_order<<<G, T, 0, e->st>>>(n, s.id, e->stage_i, s.type);
+        CU(cudaStreamSynchronize(e->st));
+    }
+    CU(cudaGetLastError());
+    return MPS_OK;
+}
+
+int mps_neighbors(mps_engine* e, int64_t* offsets, int32_t* ids, double* dist, int64_t* total) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    const int n = e->n, np = e->n_pad, K = e->c.K;
+    std::vector<int32_t> cnt(n), id(n), slot((size_t)np * K);
+    std::vector<double> dd((size_t)np * K);
+    CU(cudaStreamSynchronize(e->st));
+    CU(cudaMemcpy(cnt.data(), e->nb.cnt, 4 * n, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(id.data(), e->S().id, 4 * n, cudaMemcpyDeviceToHost));
+    int64_t tot = 0;
+    for (int k = 0; k < n; k++) tot += cnt[k];
+    if (total) *total = tot;
+    if (!ids) return MPS_OK;
+    CU(cudaMemcpy(slot.data(), e->nb.slot, 4 * (size_t)np * K, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(dd.data(), e->nb.dist, 8 * (size_t)np * K, cudaMemcpyDeviceToHost));
+    std::vector<int32_t> slot_of(n);
+    for (int k = 0; k < n; k++) slot_of[id[k]] = k;
+    int64_t o = 0;
+    offsets[0] = 0;
+    for (int i = 0; i < n; i++) {
+        int k = slot_of[i];
+        for (int m = 0; m < cnt[k]; m++) {
+            ids[o] = id[slot[(size_t)m * np + k]];
+            if (dist) dist[o] = dd[(size_t)m * np + k];
+            o++;
+        }
+        offsets[i + 1] = o;
+    }
+    return MPS_OK;
+}
+
+int mps_system(mps_engine* e, double* source, int64_t* row_ptr, int32_t* col, double* val,
+               int64_t* nnz) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    const int n = e->n, np = e->n_pad, K = e->c.K;
+    std::vector<int32_t> id(n), offcnt(n), scol((size_t)np * K);
+    std::vector<int8_t> bc(n);
+    std::vector<double> src(n), diag(n), sval((size_t)np * K);
+    CU(cudaStreamSynchronize(e->st));
+    CU(cudaMemcpy(id.data(), e->S().id, 4 * n, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(bc.data(), e->S().bc, n, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(offcnt.data(), e->A.offcnt, 4 * n, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(src.data(), e->A.src, 8 * n, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(diag.data(), e->A.diag, 8 * n, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(scol.data(), e->A.col, 4 * (size_t)np * K, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(sval.data(), e->A.val, 8 * (size_t)np * K, cudaMemcpyDeviceToHost));
+    std::vector<int32_t> slot_of(n);
+    for (int k = 0; k < n; k++) slot_of[id[k]] = k;
+    int64_t tot = 0;
+    for (int k = 0; k < n; k++)
+        if (bc[k] == BC_INNER) tot += offcnt[k] + 1;
+    if (nnz) *nnz = tot;
+    if (source)
+        for (int i = 0; i < n; i++) source[i] = src[slot_of[i]];
+    if (!row_ptr) return MPS_OK;
+    int64_t o = 0;
+    row_ptr[0] = 0;
+    std::vector<std::pair<int32_t, double>> row;
+    for (int i = 0; i < n; i++) {
+        int k = slot_of[i];
+        if (bc[k] == BC_INNER) {
+            row.clear();
+            row.push_back({i, diag[k]});
+            size_t base = (size_t)(k >> 5) * K * 32 + (k & 31);
+            for (int m = 0; m < offcnt[k]; m++)
+                row.push_back({id[scol[base + (size_t)m * 32]], sval[base + (size_t)m * 32]});
+            std::sort(row.begin(), row.end(), [](auto& a, auto& b) { return a.first < b.first; });
+            for (auto& r : row) {
+                if (col) col[o] = r.first;
+                if (val) val[o] = r.second;
+                o++;
+            }
+        }
+        row_ptr[i + 1] = o;
+    }
+    return MPS_OK;
+}
+
+int mps_collisions(mps_engine* e, int32_t* pi, int32_t* pj, double* dist, int32_t* count) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    CU(cudaStreamSynchronize(e->st));
+    int32_t cnt = std::min(e->hs->n_cand, e->pair_cap);
+    if (count) *count = cnt;
+    if (!pi || cnt == 0) return MPS_OK;
+    std::vector<CollPair> v(cnt);
+    CU(cudaMemcpy(v.data(), e->pairs, sizeof(CollPair) * cnt, cudaMemcpyDeviceToHost));
+    for (int t = 0; t < cnt; t++) {
+        pi[t] = v[t].ii;
+        pj[t] = v[t].ij;
+        if (dist) dist[t] = v[t].dist;
+    }
+    return MPS_OK;
+}
+
+}  // extern "C"

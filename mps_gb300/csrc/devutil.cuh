@@ -1,0 +1,93 @@
+// Device helpers shared by the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "engine.cuh"
+
+namespace mpsg {
+
+// FP64 operations that are never contracted into a fused multiply-add, so
+// that every rounding matches the reference's (x86 builds of it have no FMA).
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
+
+// weight(): src/mps.cpp:9-16
+__device__ __forceinline__ double weight(double dist, double re) {
+    return dist < re ? dsub(ddiv(re, dist), 1.0) : 0.0;
+}
+
+// Cell coordinate int((x - lo) / len) + 1 (src/bucket.cpp:40-42,
+// src/mps.cpp:595-597), clamped to [1, cells - 2] where the reference
+// would index outside its padded grid.
+__device__ __forceinline__ int cell_coord(double x, double lo, double len, int cells) {
+    double q = ddiv(dsub(x, lo), len);
+    if (!(q >= 0.0)) return 1;
+    if (q >= (double)(cells - 2)) return cells - 2;
+    return (int)q + 1;
+}
+
+__device__ __forceinline__ int32_t cell_key(const Consts& c, double x, double y, double z) {
+    int ix = cell_coord(x, c.dmin[0], c.len, c.numX);
+    int iy = cell_coord(y, c.dmin[1], c.len, c.numY);
+    if (c.planar) return ix * c.numY + iy;
+    int iz = cell_coord(z, c.dmin[2], c.len, c.numZ);
+    return (ix * c.numY + iy) * c.numZ + iz;
+}
+
+// Visits the candidate slots of the 3x3(x3) cells around `key` in the
+// reference's order: jx outer, jy, jz inner (src/mps.cpp:599-601), and
+// ascending id inside a cell.  Keys are x-major, so the cells of one jx
+// column (planar) or one (jx, jy) row (3-D) form one contiguous slot range.
+template <bool PLANAR, class F>
+__device__ __forceinline__ void for_each_candidate(const Consts& c, const int32_t* __restrict__ cs,
+                                                   int32_t key, F&& f) {
+    if (PLANAR) {
+        int ix = key / c.numY;
+        int iy = key - ix * c.numY;
+#pragma unroll 1
+        for (int jx = ix - 1; jx <= ix + 1; jx++) {
+            int kk = jx * c.numY + iy - 1;
+            int b = __ldg(cs + kk), e = __ldg(cs + kk + 3);
+#pragma unroll 1
+            for (int j = b; j < e; j++) f(j);
+        }
+    } else {
+        int iz = key % c.numZ;
+        int t = key / c.numZ;
+        int iy = t % c.numY;
+        int ix = t / c.numY;
+#pragma unroll 1
+        for (int jx = ix - 1; jx <= ix + 1; jx++)
+#pragma unroll 1
+            for (int jy = iy - 1; jy <= iy + 1; jy++) {
+                int kk = (jx * c.numY + jy) * c.numZ + iz - 1;
+                int b = __ldg(cs + kk), e = __ldg(cs + kk + 3);
+#pragma unroll 1
+                for (int j = b; j < e; j++) f(j);
+            }
+    }
+}
+
+// Exact squared distance in the reference's order, (dx^2 + dy^2) + dz^2.
+template <bool PLANAR>
+__device__ __forceinline__ double dist2(const StateBuf& s, int i, int j, double xi, double yi,
+                                        double zi) {
+    double dx = dsub(s.x[j], xi), dy = dsub(s.y[j], yi);
+    double r = dadd(dmul(dx, dx), dmul(dy, dy));
+    if (!PLANAR) {
+        double dz = dsub(s.z[j], zi);
+        r = dadd(r, dmul(dz, dz));
+    }
+    return r;
+}
+
+__device__ __forceinline__ void atomic_max_nonneg_double(unsigned long long* a, double v) {
+    atomicMax(a, (unsigned long long)__double_as_longlong(v));
+}
+
+}  // namespace mpsg

@@ -1,0 +1,156 @@
+// Device-side data model and kernel entry points of the MPS engine.
+//
+// Layout in HBM: every per-particle field is a separate array ("slots"),
+// kept sorted by neighbour-cell key so that the 3x3(x3) cell sweep of a
+// particle reads a few contiguous slot ranges.  Each neighbour build
+// re-sorts the state into the second of two buffers (StateBuf) and swaps.
+// The particle id (its index in the reference's std::vector<Particle>)
+// travels with the slot.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace mpsg {
+
+enum : int8_t { T_GHOST = -1, T_FLUID = 0, T_WALL = 1, T_DUMMY = 2 };
+enum : int8_t { BC_IGNORED = 0, BC_SURFACE = 1, BC_INNER = 2 };
+
+// Status bits raised on the device, reported through mps_step_stats.status.
+enum : int32_t {
+    ST_CAPACITY = 1,  // neighbour list overflow
+    ST_TIMEOUT = 2,   // a bounded wait gave up
+};
+
+// Constants of one scene, computed on the host with the reference's
+// operation order (src/settings.cpp:43-56, src/mps.cpp:132-163 and the
+// per-routine constant expressions).
+struct Consts {
+    int32_t dim;
+    int32_t planar;   // z and v_z never change: sweep 3 cell columns, skip z arithmetic
+    int32_t qc_on, ho_on;
+    int32_t numX, numY, numZ, nkeys;
+    int32_t K;        // neighbour-list capacity per particle
+    int32_t n;        // particles
+    double l0, dt;
+    double dmin[3], dmax[3];
+    double z0;        // the constant z of a planar scene
+    double rho, g[3];
+    double len;       // bucket edge = re_max
+    double re_p, re_v, re_s, re_max, cd;
+    // squared-distance thresholds: sqrt_rn(d2) < re  <=>  d2 < t_*
+    double t_p, t_v, t_s, t_max, t_cd;
+    double n0_p, n0_v, n0_s, lam_p, lam_v, lam_s;
+    double beta_n0s;    // beta * n0 (src/mps.cpp:271)
+    double visc_a;      // nu * (2 dim) / (n0 lambda)           src/mps.cpp:182
+    double mat_c;       // 2 D / (lambda n0)                     src/mps.cpp:343
+    double qc_term;     // alpha / (dt dt)                       src/mps.cpp:354
+    double src_g1;      // gamma * (1 / (dt dt))                 src/mps.cpp:313
+    double ho_g1;       // gamma_ho * (1 / (dt dt))              src/mps.cpp:291
+    double ho_c;        // 1 / (n0 dt)                           src/mps.cpp:304
+    double grad_scale;  // dim / n0                              src/mps.cpp:530
+    double e;           // restitution
+    float fre_v, fre_p, fvisc_a, fgrad_scale;  // FP32 copies for the mixed path
+};
+
+struct StateBuf {
+    double *x, *y, *z, *vx, *vy, *vz;
+    double *p, *minp, *ndr, *nd_last;
+    int32_t* id;
+    int8_t *type, *bc, *dir;
+};
+
+// Per-step device counters (one struct in device memory, copied out once per step).
+struct DevStats {
+    unsigned long long courant_bits;  // max of non-negative doubles via integer max
+    int32_t status;
+    int32_t n_new_ghosts;
+    int32_t n_unconnected;
+    int32_t n_cand;
+    int32_t n_cand_particles;
+    int32_t n_inner;
+    int32_t n_surface;
+    int32_t max_neighbors;
+    int64_t cg_iterations;
+    int32_t refinements;
+    int32_t pad;
+    double cg_rel_residual;
+};
+
+struct CollPair {
+    int32_t si, sj;  // slots
+    int32_t ii, ij;  // particle ids
+    double dist;     // distance at detection (the reference's stale neighbour distance)
+};
+
+// ----------------------------------------------------------------- sort.cu
+struct SortScratch {
+    int32_t *key, *rank, *perm, *skey;  // per slot
+    int32_t *cell_count, *cell_start;   // nkeys + 2
+    int32_t *scan_tmp;                  // block sums
+};
+void launch_rebuild(const Consts& c, const StateBuf& in, const StateBuf& out, SortScratch& s,
+                    cudaStream_t st);
+// exclusive scan of n int32 (in-place allowed); out has n+1 entries (total last)
+void launch_exclusive_scan(const int32_t* in, int32_t* out, int32_t n, int32_t* tmp,
+                           cudaStream_t st);
+size_t scan_tmp_ints(int32_t n);
+
+// --------------------------------------------------------------- sweeps.cu
+struct NbList {
+    int32_t* cnt;    // per slot
+    int32_t* slot;   // K x n_pad, column-major (entry m of slot k at m * n_pad + k)
+    double* dist;
+    double* wp;      // weight(dist, re_p)
+    int32_t n_pad;
+};
+
+struct Ppe {
+    double* src;      // per slot
+    double* diag;     // per slot (0 for rows that are not Inner)
+    int32_t* offcnt;  // per slot
+    int32_t* col;     // SELL-32, width K: ((slot/32)*K + m)*32 + slot%32
+    double* val;
+    int32_t* slice_w; // max offcnt of each 32-slot slice
+    float* val32;     // FP32 copy of val (mixed path)
+    float* diag32;
+};
+
+void launch_initial_number_density(const Consts& c, const StateBuf& s, const SortScratch& sc,
+                                   const NbList& nb, DevStats* ds, cudaStream_t st);
+void launch_explicit(const Consts& c, const StateBuf& in, const StateBuf& out,
+                     const SortScratch& sc, int mixed, DevStats* ds, cudaStream_t st);
+void launch_collision(const Consts& c, const StateBuf& s, const SortScratch& sc,
+                      int32_t* cand_cnt, int32_t* cand_base, int32_t* order, CollPair* pairs,
+                      int32_t pair_cap, int32_t* scan_tmp, DevStats* ds, cudaStream_t st);
+void launch_build_list(const Consts& c, const StateBuf& s, const SortScratch& sc,
+                       const NbList& nb, DevStats* ds, cudaStream_t st);
+void launch_bc_source(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
+                      DevStats* ds, cudaStream_t st);
+void launch_assemble(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
+                     cudaStream_t st);
+void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
+                      int32_t* parent, int8_t* has_surface, DevStats* ds, cudaStream_t st);
+void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb,
+                          const double* x, double* ax, double* ay, double* az, int mixed,
+                          DevStats* ds, cudaStream_t st);
+void launch_number_density(const Consts& c, const StateBuf& s, const NbList& nb,
+                           cudaStream_t st);
+
+// --------------------------------------------------------------- solver.cu
+struct Krylov {
+    double *x, *r, *p, *q, *z, *inv_diag;
+    float *r32, *p32, *q32, *z32, *x32, *inv_diag32;
+    double* partials;  // per block, several slots
+    unsigned int* barrier;  // grid barrier counter + generation
+    int32_t grid;      // cooperative grid size
+    int32_t block;
+};
+void solver_setup(Krylov& k, int32_t n_pad, int device);
+// Solves A x = b; returns through DevStats (iterations, residual, status).
+void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double tol,
+                       int64_t max_iter, DevStats* ds, cudaStream_t st);
+void launch_solve_mixed(const Consts& c, const Ppe& A, const Krylov& k, double tol,
+                        int64_t max_iter, DevStats* ds, cudaStream_t st);
+
+}  // namespace mpsg

@@ -1,0 +1,659 @@
+// Particle-interaction kernels of the MPS step (src/mps.cpp:165-667).
+//
+// Every kernel works on the cell-sorted slots of the current StateBuf; the
+// neighbour sweep visits candidates in the reference's order so that the
+// FP64 sums (viscosity, number densities, matrix diagonal, gradient) round
+// exactly like the reference's.  Roofline of this family: FP64 issue on
+// GB300 (~0.5 T DFMA/s, ~52 G div or sqrt/s per GPU) for the exact sweeps,
+// HBM for the list-driven ones.
+#include "devutil.cuh"
+#include "engine.cuh"
+
+namespace mpsg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int blocks_for(int n, int t = kThreads) { return (n + t - 1) / t; }
+
+__device__ __forceinline__ void raise_status(DevStats* ds, int32_t bit) { atomicOr(&ds->status, bit); }
+
+__device__ __forceinline__ bool outside_domain(const Consts& c, double x, double y, double z) {
+    // MPS::checkBoundaryViolation: src/mps.cpp:643-667
+    return x < c.dmin[0] || c.dmax[0] < x || y < c.dmin[1] || c.dmax[1] < y || z < c.dmin[2] ||
+           c.dmax[2] < z;
+}
+
+// Number density at re_p over a particle's current neighbours (d < re_max),
+// in sweep order: the value a later setNumberDensity reads from the stale
+// list of a particle that has just become a ghost (src/mps.cpp:590-593).
+template <bool PLANAR>
+__device__ double sweep_number_density_p(const Consts& c, const StateBuf& s, const int32_t* cs,
+                                         int32_t key, int k) {
+    double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
+    double nd = 0.0;
+    for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
+        if (j == k) return;
+        double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
+        if (d2 < c.t_max && d2 < c.t_p) nd = dadd(nd, weight(dsqrt(d2), c.re_p));
+    });
+    return nd;
+}
+
+// ---------------------------------------------------------------------------
+// calcGravity + calcViscosity + moveParticles (+ checkBoundaryViolation),
+// src/mps.cpp:165-215 and 643-667, fused with the first neighbour sweep.
+// Reads `in`, writes the moved state to `out` (same slot order).
+template <bool PLANAR, bool MIXED>
+__global__ void __launch_bounds__(kThreads) k_explicit(Consts c, StateBuf in, StateBuf out,
+                                                       const int32_t* __restrict__ skey,
+                                                       const int32_t* __restrict__ cs,
+                                                       DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n) return;
+    int8_t t = in.type[k];
+    double x = in.x[k], y = in.y[k], vx = in.vx[k], vy = in.vy[k];
+    double z = PLANAR ? c.z0 : in.z[k], vz = PLANAR ? 0.0 : in.vz[k];
+    double nd_last = in.nd_last[k];
+    if (t == T_FLUID) {
+        const int32_t key = skey[k];
+        double ax, ay, az;
+        if (!MIXED) {
+            double tx = 0.0, ty = 0.0, tz = 0.0;
+            for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
+                if (j == k) return;
+                double d2 = dist2<PLANAR>(in, k, j, x, y, z);
+                if (d2 < c.t_max && d2 < c.t_v) {
+                    double w = weight(dsqrt(d2), c.re_v);
+                    tx = dadd(tx, dmul(dsub(in.vx[j], vx), w));
+                    ty = dadd(ty, dmul(dsub(in.vy[j], vy), w));
+                    if (!PLANAR) tz = dadd(tz, dmul(dsub(in.vz[j], vz), w));
+                }
+            });
+            ax = dadd(c.g[0], dmul(tx, c.visc_a));
+            ay = dadd(c.g[1], dmul(ty, c.visc_a));
+            az = PLANAR ? 0.0 : dadd(c.g[2], dmul(tz, c.visc_a));
+        } else {
+            // FP32 weights and FP32 accumulation; the neighbour set is the
+            // exact FP64 one.
+            float tx = 0.f, ty = 0.f, tz = 0.f;
+            const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
+            for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
+                if (j == k) return;
+                double d2 = dist2<PLANAR>(in, k, j, x, y, z);
+                if (d2 < c.t_max && d2 < c.t_v) {
+                    float w = c.fre_v * rsqrtf((float)d2) - 1.f;
+                    tx = fmaf((float)in.vx[j] - fvx, w, tx);
+                    ty = fmaf((float)in.vy[j] - fvy, w, ty);
+                    if (!PLANAR) tz = fmaf((float)in.vz[j] - fvz, w, tz);
+                }
+            });
+            ax = c.g[0] + (double)(tx * c.fvisc_a);
+            ay = c.g[1] + (double)(ty * c.fvisc_a);
+            az = PLANAR ? 0.0 : c.g[2] + (double)(tz * c.fvisc_a);
+        }
+        vx = dadd(vx, dmul(ax, c.dt));
+        vy = dadd(vy, dmul(ay, c.dt));
+        double nx = dadd(x, dmul(vx, c.dt));
+        double ny = dadd(y, dmul(vy, c.dt));
+        double nz = z;
+        if (!PLANAR) {
+            vz = dadd(vz, dmul(az, c.dt));
+            nz = dadd(z, dmul(vz, c.dt));
+        }
+        if (outside_domain(c, nx, ny, nz)) {
+            t = T_GHOST;
+            atomicAdd(&ds->n_new_ghosts, 1);
+            nd_last = sweep_number_density_p<PLANAR>(c, in, cs, key, k);
+        }
+        x = nx;
+        y = ny;
+        z = nz;
+    }
+    out.x[k] = x;
+    out.y[k] = y;
+    out.vx[k] = vx;
+    out.vy[k] = vy;
+    if (!PLANAR) {
+        out.z[k] = z;
+        out.vz[k] = vz;
+    }
+    out.type[k] = t;
+    out.nd_last[k] = nd_last;
+    out.p[k] = in.p[k];
+    out.minp[k] = in.minp[k];
+    out.ndr[k] = in.ndr[k];
+    out.id[k] = in.id[k];
+    out.bc[k] = in.bc[k];
+    out.dir[k] = in.dir[k];
+}
+
+// ---------------------------------------------------------------------------
+// MPS::collision (src/mps.cpp:217-250).  The candidate pairs — fluid i,
+// neighbour j with the stale distance < cd, skipping fluid j with id >= id_i
+// — are found in parallel; their effect is order dependent (Gauss-Seidel,
+// in place), so they are then applied by one thread in ascending id_i and
+// sweep order, exactly as the reference's loop does.
+template <bool PLANAR>
+__device__ __forceinline__ int for_each_collision(const Consts& c, const StateBuf& s,
+                                                  const int32_t* cs, int32_t key, int k,
+                                                  CollPair* out) {
+    double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
+    int32_t idi = s.id[k];
+    int m = 0;
+    for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
+        if (j == k) return;
+        double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
+        if (!(d2 < c.t_max && d2 < c.t_cd)) return;
+        if (s.type[j] == T_FLUID && s.id[j] >= idi) return;
+        if (out) out[m] = CollPair{k, j, idi, s.id[j], dsqrt(d2)};
+        m++;
+    });
+    return m;
+}
+
+template <bool PLANAR>
+__global__ void __launch_bounds__(kThreads) k_coll_count(Consts c, StateBuf s,
+                                                         const int32_t* __restrict__ skey,
+                                                         const int32_t* __restrict__ cs,
+                                                         int32_t* __restrict__ cnt_by_id) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n || s.type[k] != T_FLUID) return;
+    int m = for_each_collision<PLANAR>(c, s, cs, skey[k], k, nullptr);
+    if (m) cnt_by_id[s.id[k]] = m;
+}
+
+template <bool PLANAR>
+__global__ void __launch_bounds__(kThreads) k_coll_write(Consts c, StateBuf s,
+                                                         const int32_t* __restrict__ skey,
+                                                         const int32_t* __restrict__ cs,
+                                                         const int32_t* __restrict__ cnt_by_id,
+                                                         const int32_t* __restrict__ base_by_id,
+                                                         CollPair* pairs, int32_t cap,
+                                                         DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n || s.type[k] != T_FLUID) return;
+    int32_t id = s.id[k];
+    if (cnt_by_id[id] == 0) return;
+    int32_t b = base_by_id[id];
+    if (b + cnt_by_id[id] > cap) {
+        raise_status(ds, ST_CAPACITY);
+        return;
+    }
+    for_each_collision<PLANAR>(c, s, cs, skey[k], k, pairs + b);
+}
+
+template <bool PLANAR>
+__global__ void k_coll_apply(Consts c, StateBuf s, const CollPair* __restrict__ pairs,
+                             const int32_t* __restrict__ total_p, int32_t cap, DevStats* ds) {
+    int32_t total = *total_p;
+    ds->n_cand = total;
+    if (total > cap) total = cap;
+    const double inv_rho = ddiv(1.0, c.rho);  // Particle::inverseDensity, src/particle.cpp:19-29
+    for (int32_t t = 0; t < total; t++) {
+        CollPair q = pairs[t];
+        int i = q.si, j = q.sj;
+        double inv_i = inv_rho;  // i is fluid
+        double inv_j = s.type[j] == T_FLUID ? inv_rho : 0.0;
+        double reduced = ddiv(1.0, dadd(inv_i, inv_j));
+        double dx = dsub(s.x[j], s.x[i]), dy = dsub(s.y[j], s.y[i]);
+        double dz = PLANAR ? 0.0 : dsub(s.z[j], s.z[i]);
+        double z2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+        double nx = dx, ny = dy, nz = dz;
+        if (z2 > 0.0) {
+            double r = dsqrt(z2);
+            nx = ddiv(dx, r);
+            ny = ddiv(dy, r);
+            nz = ddiv(dz, r);
+        }
+        double ux = dsub(s.vx[j], s.vx[i]), uy = dsub(s.vy[j], s.vy[i]);
+        double uz = PLANAR ? 0.0 : dsub(s.vz[j], s.vz[i]);
+        double rel = dadd(dadd(dmul(ux, nx), dmul(uy, ny)), dmul(uz, nz));
+        if (rel < 0.0) {
+            double impulse = dmul(dmul(-dadd(1.0, c.e), rel), reduced);
+            double ci = dmul(impulse, inv_i), cj = dmul(impulse, inv_j);
+            s.vx[i] = dsub(s.vx[i], dmul(ci, nx));
+            s.vy[i] = dsub(s.vy[i], dmul(ci, ny));
+            s.vx[j] = dadd(s.vx[j], dmul(cj, nx));
+            s.vy[j] = dadd(s.vy[j], dmul(cj, ny));
+            double pimp = dmul(dsub(c.cd, q.dist), reduced);
+            double pi_ = dmul(pimp, inv_i), pj_ = dmul(pimp, inv_j);
+            s.x[i] = dsub(s.x[i], dmul(pi_, nx));
+            s.y[i] = dsub(s.y[i], dmul(pi_, ny));
+            s.x[j] = dadd(s.x[j], dmul(pj_, nx));
+            s.y[j] = dadd(s.y[j], dmul(pj_, ny));
+            if (!PLANAR) {
+                s.vz[i] = dsub(s.vz[i], dmul(ci, nz));
+                s.vz[j] = dadd(s.vz[j], dmul(cj, nz));
+                s.z[i] = dsub(s.z[i], dmul(pi_, nz));
+                s.z[j] = dadd(s.z[j], dmul(pj_, nz));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// MPS::setNeighbors (src/mps.cpp:585-619): the neighbour list of the build
+// that the pressure part uses, stored column-major (slot, FP64 distance,
+// FP64 weight at re_p), plus the number density at re_p (kept per particle
+// as the value a stale-list read returns once it becomes a ghost).
+template <bool PLANAR>
+__global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
+                                                         const int32_t* __restrict__ skey,
+                                                         const int32_t* __restrict__ cs, NbList nb,
+                                                         DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n) return;
+    if (s.type[k] == T_GHOST) {
+        nb.cnt[k] = 0;
+        return;
+    }
+    double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
+    double nd = 0.0;
+    int m = 0;
+    const int np = nb.n_pad;
+    for_each_candidate<PLANAR>(c, cs, skey[k], [&](int j) {
+        if (j == k) return;
+        double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
+        if (!(d2 < c.t_max)) return;
+        double dist = dsqrt(d2);
+        double w = weight(dist, c.re_p);
+        if (dist < c.re_p) nd = dadd(nd, w);
+        if (m < c.K) {
+            nb.slot[(size_t)m * np + k] = j;
+            nb.dist[(size_t)m * np + k] = dist;
+            nb.wp[(size_t)m * np + k] = w;
+        }
+        m++;
+    });
+    if (m > c.K) raise_status(ds, ST_CAPACITY);
+    atomicMax(&ds->max_neighbors, m);
+    nb.cnt[k] = m < c.K ? m : c.K;
+    s.nd_last[k] = nd;
+}
+
+// setBoundaryCondition + setSourceTerm (classic form), src/mps.cpp:262-320.
+__global__ void __launch_bounds__(kThreads) k_bc_source(Consts c, StateBuf s, NbList nb, Ppe A,
+                                                        DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n) return;
+    int8_t t = s.type[k];
+    int8_t bc;
+    if (t == T_GHOST || t == T_DUMMY) {
+        bc = BC_IGNORED;
+    } else {
+        const int np = nb.n_pad, m = nb.cnt[k];
+        double ns = 0.0;
+        for (int q = 0; q < m; q++) {
+            double dist = nb.dist[(size_t)q * np + k];
+            if (dist < c.re_s) ns = dadd(ns, weight(dist, c.re_s));
+        }
+        bc = ns < c.beta_n0s ? BC_SURFACE : BC_INNER;
+    }
+    s.bc[k] = bc;
+    double b = 0.0;
+    if (bc == BC_INNER && !c.ho_on) b = ddiv(dmul(c.src_g1, dsub(s.nd_last[k], c.n0_p)), c.n0_p);
+    A.src[k] = b;
+    unsigned in_mask = __ballot_sync(__activemask(), bc == BC_INNER);
+    unsigned sf_mask = __ballot_sync(__activemask(), bc == BC_SURFACE);
+    if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) {
+        if (in_mask) atomicAdd(&ds->n_inner, __popc(in_mask));
+        if (sf_mask) atomicAdd(&ds->n_surface, __popc(sf_mask));
+    }
+}
+
+// Higher-order source term (src/mps.cpp:288-306), needs every neighbour's BC.
+template <bool PLANAR>
+__global__ void __launch_bounds__(kThreads) k_source_ho(Consts c, StateBuf s, NbList nb, Ppe A) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n || s.bc[k] != BC_INNER) return;
+    double b = dmul(c.ho_g1, dsub(s.ndr[k], 1.0));
+    const double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
+    const double ui = s.vx[k], vi = s.vy[k], wi = PLANAR ? 0.0 : s.vz[k];
+    const double cre = dmul(c.ho_c, c.re_p);
+    const int np = nb.n_pad, m = nb.cnt[k];
+    for (int q = 0; q < m; q++) {
+        int j = nb.slot[(size_t)q * np + k];
+        if (s.bc[j] == BC_IGNORED) continue;
+        double dist = nb.dist[(size_t)q * np + k];
+        if (!(dist < c.re_p)) continue;
+        double rx = dsub(s.x[j], xi), ry = dsub(s.y[j], yi);
+        double ux = dsub(s.vx[j], ui), uy = dsub(s.vy[j], vi);
+        double dot = dadd(dmul(rx, ux), dmul(ry, uy));
+        if (!PLANAR) dot = dadd(dot, dmul(dsub(s.z[j], zi), dsub(s.vz[j], wi)));
+        b = dsub(b, ddiv(dmul(cre, dot), dmul(dmul(dist, dist), dist)));
+    }
+    A.src[k] = b;
+}
+
+// MPS::setMatrix (src/mps.cpp:322-360): one SELL-32 row per Inner slot.
+__global__ void __launch_bounds__(kThreads) k_assemble(Consts c, StateBuf s, NbList nb, Ppe A) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int off = 0;
+    if (k < c.n) {
+        double diag = 0.0;
+        if (s.bc[k] == BC_INNER) {
+            const int np = nb.n_pad, m = nb.cnt[k];
+            const size_t sbase = (size_t)(k >> 5) * c.K * 32 + (k & 31);
+            for (int q = 0; q < m; q++) {
+                int j = nb.slot[(size_t)q * np + k];
+                int8_t bj = s.bc[j];
+                if (bj == BC_IGNORED) continue;
+                double dist = nb.dist[(size_t)q * np + k];
+                if (!(dist < c.re_p)) continue;
+                double a = ddiv(dmul(c.mat_c, nb.wp[(size_t)q * np + k]), c.rho);
+                diag = dadd(diag, a);
+                if (bj == BC_INNER) {
+                    A.col[sbase + (size_t)off * 32] = j;
+                    A.val[sbase + (size_t)off * 32] = -a;
+                    off++;
+                }
+            }
+            if (c.qc_on) diag = dadd(diag, c.qc_term);
+        }
+        A.diag[k] = diag;
+        A.offcnt[k] = off;
+    }
+    int w = __reduce_max_sync(0xffffffffu, off);
+    if ((threadIdx.x & 31) == 0 && (k >> 5) < (c.n + 31) / 32) A.slice_w[k >> 5] = w;
+}
+
+// ---------------------------------------------------------------------------
+// MPS::ensureDirichletBoundaryConnection (src/mps.cpp:362-415).  The BFS
+// from every Surface particle over edges with dist < re_p marks exactly the
+// connected components that contain a Surface particle, so it is computed as
+// a lock-free union-find over those edges.
+constexpr int kUfLimit = 1 << 22;
+
+__device__ int uf_find(int* par, int x, DevStats* ds) {
+    volatile int* vp = par;
+    for (int it = 0; it < kUfLimit; it++) {
+        int p = vp[x];
+        if (p == x) return x;
+        int gp = vp[p];
+        if (gp != p) vp[x] = gp;  // path halving; any ancestor is a valid parent
+        x = p;
+    }
+    raise_status(ds, ST_TIMEOUT);
+    return x;
+}
+
+__device__ void uf_union(int* par, int a, int b, DevStats* ds) {
+    for (int it = 0; it < kUfLimit; it++) {
+        a = uf_find(par, a, ds);
+        b = uf_find(par, b, ds);
+        if (a == b) return;
+        if (a < b) {
+            int t = a;
+            a = b;
+            b = t;
+        }
+        if (atomicCAS(par + a, a, b) == a) return;
+    }
+    raise_status(ds, ST_TIMEOUT);
+}
+
+__global__ void k_cc_init(int n, int* par) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) par[k] = k;
+}
+
+__global__ void __launch_bounds__(kThreads) k_cc_hook(Consts c, StateBuf s, NbList nb, int* par,
+                                                      DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n || s.type[k] == T_GHOST) return;
+    const int np = nb.n_pad, m = nb.cnt[k];
+    for (int q = 0; q < m; q++) {
+        int j = nb.slot[(size_t)q * np + k];
+        if (j < k && nb.dist[(size_t)q * np + k] < c.re_p) uf_union(par, k, j, ds);
+    }
+}
+
+__global__ void k_cc_mark(Consts c, StateBuf s, int* par, int8_t* has_surface, DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n) return;
+    int r = uf_find(par, k, ds);
+    if (s.bc[k] == BC_SURFACE) has_surface[r] = 1;
+}
+
+__global__ void k_cc_apply(Consts c, StateBuf s, const int* __restrict__ par,
+                           const int8_t* __restrict__ has_surface, Ppe A, DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n) return;
+    int r = k;
+    for (int it = 0; it < kUfLimit && par[r] != r; it++) r = par[r];  // roots are final here
+    int8_t conn = (s.type[k] != T_GHOST && has_surface[r]) ? 1 : 0;
+    s.dir[k] = conn;
+    if (!conn && s.bc[k] == BC_INNER) {
+        A.diag[k] = dmul(A.diag[k], 2.0);
+        atomicAdd(&ds->n_unconnected, 1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// solvePoissonEquation's scatter + removeNegativePressure (src/mps.cpp:466-479)
+__global__ void k_pressure_out(int n, const double* __restrict__ x, double* __restrict__ p) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double v = x[k];
+    p[k] = v < 0.0 ? 0.0 : v;
+}
+
+// MPS::setMinimumPressure (src/mps.cpp:481-503)
+__global__ void __launch_bounds__(kThreads) k_min_pressure(Consts c, StateBuf s, NbList nb) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n || s.bc[k] == BC_IGNORED) return;
+    double mn = s.p[k];
+    const int np = nb.n_pad, m = nb.cnt[k];
+    for (int q = 0; q < m; q++) {
+        int j = nb.slot[(size_t)q * np + k];
+        if (s.type[j] == T_DUMMY) continue;
+        if (nb.dist[(size_t)q * np + k] < c.re_p) {
+            double pj = s.p[j];
+            if (mn > pj) mn = pj;
+        }
+    }
+    s.minp[k] = mn;
+}
+
+// MPS::calcPressureGradient (src/mps.cpp:505-533)
+template <bool PLANAR, bool MIXED>
+__global__ void __launch_bounds__(kThreads) k_gradient(Consts c, StateBuf s, NbList nb, double* ax,
+                                                       double* ay, double* az) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n || s.type[k] != T_FLUID) return;
+    const double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
+    const double pmin = s.minp[k];
+    const int np = nb.n_pad, m = nb.cnt[k];
+    if (!MIXED) {
+        double gx = 0.0, gy = 0.0, gz = 0.0;
+        for (int q = 0; q < m; q++) {
+            int j = nb.slot[(size_t)q * np + k];
+            if (s.type[j] == T_DUMMY) continue;
+            double dist = nb.dist[(size_t)q * np + k];
+            if (!(dist < c.re_p)) continue;
+            double dp = dsub(s.p[j], pmin);
+            double w = nb.wp[(size_t)q * np + k];
+            double d2 = dmul(dist, dist);
+            gx = dadd(gx, ddiv(dmul(dmul(dsub(s.x[j], xi), dp), w), d2));
+            gy = dadd(gy, ddiv(dmul(dmul(dsub(s.y[j], yi), dp), w), d2));
+            if (!PLANAR) gz = dadd(gz, ddiv(dmul(dmul(dsub(s.z[j], zi), dp), w), d2));
+        }
+        gx = dmul(gx, c.grad_scale);
+        gy = dmul(gy, c.grad_scale);
+        ax[k] = ddiv(dmul(-1.0, gx), c.rho);
+        ay[k] = ddiv(dmul(-1.0, gy), c.rho);
+        if (!PLANAR) az[k] = ddiv(dmul(-1.0, dmul(gz, c.grad_scale)), c.rho);
+    } else {
+        float gx = 0.f, gy = 0.f, gz = 0.f;
+        for (int q = 0; q < m; q++) {
+            int j = nb.slot[(size_t)q * np + k];
+            if (s.type[j] == T_DUMMY) continue;
+            double dist = nb.dist[(size_t)q * np + k];
+            if (!(dist < c.re_p)) continue;
+            float fd = (float)dist;
+            float coef = (float)(s.p[j] - pmin) * (c.fre_p / fd - 1.f) / (fd * fd);
+            gx = fmaf((float)(s.x[j] - xi), coef, gx);
+            gy = fmaf((float)(s.y[j] - yi), coef, gy);
+            if (!PLANAR) gz = fmaf((float)(s.z[j] - zi), coef, gz);
+        }
+        const float sc = -c.fgrad_scale / (float)c.rho;
+        ax[k] = (double)(gx * sc);
+        ay[k] = (double)(gy * sc);
+        if (!PLANAR) az[k] = (double)(gz * sc);
+    }
+}
+
+// moveParticlesWithPressureGradient + checkBoundaryViolation + the Courant
+// number (src/mps.cpp:535-571).
+template <bool PLANAR>
+__global__ void __launch_bounds__(kThreads) k_move2(Consts c, StateBuf s, const double* __restrict__ ax,
+                                                    const double* __restrict__ ay,
+                                                    const double* __restrict__ az, DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n || s.type[k] != T_FLUID) return;
+    double a0 = ax[k], a1 = ay[k];
+    double vx = dadd(s.vx[k], dmul(a0, c.dt));
+    double vy = dadd(s.vy[k], dmul(a1, c.dt));
+    double x = dadd(s.x[k], dmul(dmul(a0, c.dt), c.dt));
+    double y = dadd(s.y[k], dmul(dmul(a1, c.dt), c.dt));
+    double vz = 0.0, z = c.z0;
+    if (!PLANAR) {
+        double a2 = az[k];
+        vz = dadd(s.vz[k], dmul(a2, c.dt));
+        z = dadd(s.z[k], dmul(dmul(a2, c.dt), c.dt));
+        s.vz[k] = vz;
+        s.z[k] = z;
+    }
+    s.vx[k] = vx;
+    s.vy[k] = vy;
+    s.x[k] = x;
+    s.y[k] = y;
+    if (outside_domain(c, x, y, z)) {
+        s.type[k] = T_GHOST;
+        atomicAdd(&ds->n_new_ghosts, 1);
+        return;
+    }
+    double sp = dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz));
+    double cour = ddiv(dmul(dsqrt(sp), c.dt), c.l0);
+    atomic_max_nonneg_double(&ds->courant_bits, cour);
+}
+
+// MPS::setNumberDensity's ratio (src/mps.cpp:627-641)
+__global__ void k_number_density(Consts c, StateBuf s) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n) return;
+    s.ndr[k] = s.bc[k] == BC_SURFACE ? 0.0 : ddiv(s.nd_last[k], c.n0_p);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+
+void launch_explicit(const Consts& c, const StateBuf& in, const StateBuf& out,
+                     const SortScratch& sc, int mixed, DevStats* ds, cudaStream_t st) {
+    int nb = blocks_for(c.n);
+    if (c.planar) {
+        if (mixed)
+            k_explicit<true, true><<<nb, kThreads, 0, st>>>(c, in, out, sc.skey, sc.cell_start, ds);
+        else
+            k_explicit<true, false><<<nb, kThreads, 0, st>>>(c, in, out, sc.skey, sc.cell_start, ds);
+    } else {
+        if (mixed)
+            k_explicit<false, true><<<nb, kThreads, 0, st>>>(c, in, out, sc.skey, sc.cell_start, ds);
+        else
+            k_explicit<false, false><<<nb, kThreads, 0, st>>>(c, in, out, sc.skey, sc.cell_start, ds);
+    }
+}
+
+void launch_collision(const Consts& c, const StateBuf& s, const SortScratch& sc,
+                      int32_t* cand_cnt, int32_t* cand_base, int32_t* /*order*/, CollPair* pairs,
+                      int32_t pair_cap, int32_t* scan_tmp, DevStats* ds, cudaStream_t st) {
+    int nb = blocks_for(c.n);
+    cudaMemsetAsync(cand_cnt, 0, sizeof(int32_t) * (c.n + 1), st);
+    if (c.planar)
+        k_coll_count<true><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt);
+    else
+        k_coll_count<false><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt);
+    launch_exclusive_scan(cand_cnt, cand_base, c.n, scan_tmp, st);
+    if (c.planar) {
+        k_coll_write<true><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt,
+                                                    cand_base, pairs, pair_cap, ds);
+        k_coll_apply<true><<<1, 1, 0, st>>>(c, s, pairs, cand_base + c.n, pair_cap, ds);
+    } else {
+        k_coll_write<false><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt,
+                                                     cand_base, pairs, pair_cap, ds);
+        k_coll_apply<false><<<1, 1, 0, st>>>(c, s, pairs, cand_base + c.n, pair_cap, ds);
+    }
+}
+
+void launch_build_list(const Consts& c, const StateBuf& s, const SortScratch& sc,
+                       const NbList& nb, DevStats* ds, cudaStream_t st) {
+    int g = blocks_for(c.n);
+    if (c.planar)
+        k_build_list<true><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, ds);
+    else
+        k_build_list<false><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, ds);
+}
+
+void launch_bc_source(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
+                      DevStats* ds, cudaStream_t st) {
+    int g = blocks_for(c.n);
+    k_bc_source<<<g, kThreads, 0, st>>>(c, s, nb, A, ds);
+    if (c.ho_on) {
+        if (c.planar)
+            k_source_ho<true><<<g, kThreads, 0, st>>>(c, s, nb, A);
+        else
+            k_source_ho<false><<<g, kThreads, 0, st>>>(c, s, nb, A);
+    }
+}
+
+void launch_assemble(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
+                     cudaStream_t st) {
+    k_assemble<<<blocks_for(c.n), kThreads, 0, st>>>(c, s, nb, A);
+}
+
+void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
+                      int32_t* parent, int8_t* has_surface, DevStats* ds, cudaStream_t st) {
+    int g = blocks_for(c.n);
+    cudaMemsetAsync(has_surface, 0, c.n, st);
+    k_cc_init<<<g, kThreads, 0, st>>>(c.n, parent);
+    k_cc_hook<<<g, kThreads, 0, st>>>(c, s, nb, parent, ds);
+    k_cc_mark<<<g, kThreads, 0, st>>>(c, s, parent, has_surface, ds);
+    k_cc_apply<<<g, kThreads, 0, st>>>(c, s, parent, has_surface, A, ds);
+}
+
+void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb, const double* x,
+                          double* ax, double* ay, double* az, int mixed, DevStats* ds,
+                          cudaStream_t st) {
+    int g = blocks_for(c.n);
+    k_pressure_out<<<g, kThreads, 0, st>>>(c.n, x, s.p);
+    k_min_pressure<<<g, kThreads, 0, st>>>(c, s, nb);
+    if (c.planar) {
+        if (mixed)
+            k_gradient<true, true><<<g, kThreads, 0, st>>>(c, s, nb, ax, ay, az);
+        else
+            k_gradient<true, false><<<g, kThreads, 0, st>>>(c, s, nb, ax, ay, az);
+        k_move2<true><<<g, kThreads, 0, st>>>(c, s, ax, ay, az, ds);
+    } else {
+        if (mixed)
+            k_gradient<false, true><<<g, kThreads, 0, st>>>(c, s, nb, ax, ay, az);
+        else
+            k_gradient<false, false><<<g, kThreads, 0, st>>>(c, s, nb, ax, ay, az);
+        k_move2<false><<<g, kThreads, 0, st>>>(c, s, ax, ay, az, ds);
+    }
+}
+
+void launch_number_density(const Consts& c, const StateBuf& s, const NbList& /*nb*/,
+                           cudaStream_t st) {
+    k_number_density<<<blocks_for(c.n), kThreads, 0, st>>>(c, s);
+}
+
+void launch_initial_number_density(const Consts& c, const StateBuf& s, const SortScratch& sc,
+                                   const NbList& nb, DevStats* ds, cudaStream_t st) {
+    launch_build_list(c, s, sc, nb, ds, st);
+    launch_number_density(c, s, nb, st);
+}
+
+}  // namespace mpsg
