@@ -1,0 +1,387 @@
+#!/usr/bin/env python3
+"""Throughput of the MPS time step on one GB300: particle-steps/s.
+
+Default workload: the 1M-particle 2-D dam break (water column 0.5 x 1.0 m,
+l0 = 0.5/707 m so the column is 707 x 1414 = 999,698 fluid particles, tank
+2.0 x 1.2 m with 2 wall and 2 dummy layers, dt = 5e-5 s, the reference's
+physics with radii 3.1/3.1/2.1 l0), synthetic and seeded, solved with the
+mixed-precision PPE solver (FP32 Krylov iterations, FP64 dot products and
+FP64 residual refinement to 1e-10).  The same steps are also timed with the
+plain FP64 solver (the reference's Jacobi-CG at machine-epsilon tolerance).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on stdout (rank 0).  `value` is device-timed throughput of K
+steps with the state resident in HBM (CUDA events on the engine's stream);
+`e2e` is the same steps through the C ABI with the host-owned particle
+arrays copied in (pinned) and the step's results copied out every step.
+`--impl reference` times the CPU oracle (the reference's algorithm restated
+in C++/OpenMP, the reference's own sources need Eigen which is absent) on
+this machine's host cores.  Multi-GPU runs are independent replicas (the
+method has no data-parallel split of one scene); value sums all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "particle-steps/s at 1M particles: mixed-precision vs plain FP64, same GB300"
+UNIT = "particle-steps/s"
+
+
+def workload(name: str):
+    from mps_gb300 import scenes
+
+    if name == "dambreak_1m":   # mixed-precision 1M workload
+        l0 = 0.5 / 707
+        return scenes.dam_break(l0, tank=(2.0, 1.2), column=(0.5, 1.0), dt=5e-5)
+    if name == "dambreak_2m":   # plain FP64 2M workload
+        return scenes.dam_break(5e-4, tank=(2.0, 1.2), column=(0.5, 1.0), dt=5e-5)
+    if name == "dambreak_small":  # the reference's CPU-sized case
+        return scenes.dam_break(0.01, tank=(1.0, 0.6), column=(0.25, 0.5), dt=1e-3)
+    if name.startswith("dambreak_cols"):  # dambreak_cols<k>: k x 2k column, same tank
+        k = int(name[len("dambreak_cols"):])
+        return scenes.dam_break(0.5 / k, tank=(2.0, 1.2), column=(0.5, 1.0), dt=5e-5)
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(tempfile.gettempdir(), f"mps_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- roofline
+def solver_bytes(precision: int, st: dict, n: int) -> float:
+    """Algorithmic bytes of one pressure solve (one solver launch pair).
+
+    Per stored off-diagonal entry and iteration: column index 4 B plus the
+    value (8 B FP64 / 4 B FP32); per row and iteration the vectors touched
+    once each (FP64: 116 B, FP32 inner: 60 B); the gathered neighbour
+    vector entries are counted once, as the row's own entry.  MIXED adds per
+    refinement the FP64 residual (12 B/entry + 36 B/row) and once the FP32
+    copy of the matrix (12 B/entry + 16 B/row)."""
+    nnz = st["nnz_offdiag"]
+    it = st["cg_iterations"]
+    if precision == 0:
+        return it * (12.0 * nnz + 116.0 * n) + (36.0 * n)
+    ref = st["refinements"] + 1
+    return it * (8.0 * nnz + 60.0 * n) + ref * (12.0 * nnz + 36.0 * n) + (12.0 * nnz + 16.0 * n)
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_row_iter(kernel: str):
+    """DRAM bytes per (row x iteration) of the solver kernel from the committed
+    ncu summary, if one exists (profiles/<kernel>_*.txt, line 'dram_bytes_per_row_iter: X')."""
+    d = os.path.join(REPO, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if fn.startswith(kernel) and fn.endswith(".txt"):
+            for line in open(os.path.join(d, fn)):
+                if line.startswith("dram_bytes_per_row_iter:"):
+                    return float(line.split(":")[1])
+    return None
+
+
+# ---------------------------------------------------------------- CPU baseline
+CPU_SAMPLE = "dambreak_cols200"  # 200 x 400 = 80,000 fluid particles, same tank and physics
+
+
+def cpu_sample(steps: int = 3, workload_name: str = CPU_SAMPLE) -> dict:
+    """Times full oracle steps (all phases, CG to machine epsilon solved twice,
+    as the reference) in a child process with OMP_NUM_THREADS = host cores."""
+    cores = os.cpu_count() or 1
+    code = (
+        "import sys, time, json; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+        "import bench\nfrom oracle import Oracle, build\nbuild()\n"
+        "prm, pos, vel, t = bench.workload(%r)\n"
+        "o = Oracle(prm, pos, vel, t)\n"
+        "nf = int((t == 0).sum()); times = []; its = []\n"
+        "for s in range(%d):\n"
+        "    t0 = time.perf_counter(); st = o.step(); times.append(time.perf_counter() - t0)"
+        "; its.append(st['cg_iterations'])\n"
+        "print(json.dumps({'nf': nf, 'times': times, 'its': its}))\n"
+    ) % (REPO, os.path.join(REPO, "oracle"), workload_name, steps)
+    env = dict(os.environ, OMP_NUM_THREADS=str(cores))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                         timeout=1800)
+    if out.returncode != 0:
+        raise RuntimeError(out.stderr[-2000:])
+    d = json.loads(out.stdout.strip().splitlines()[-1])
+    tot = sum(d["times"])
+    return {"value": d["nf"] * len(d["times"]) / tot, "unit": UNIT, "cores": cores,
+            "kind": "port",
+            "sample": (f"{len(d['times'])} full steps of the dam break at l0=0.5/200 m "
+                       f"({d['nf']} fluid particles, same tank, physics and dt) on the CPU oracle, "
+                       f"FP64 CG to machine epsilon solved twice per step as the reference "
+                       f"(CG iterations {d['its']}), {tot:.1f} s; the 1M workload's CPU "
+                       f"throughput would be lower since CG iterations grow with resolution")}
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args, rank: int, world: int, dist):
+    import torch
+
+    from mps_gb300 import FP64, MIXED, Engine
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    prm, pos, vel, types = workload(args.workload)
+    n = len(types)
+    nf = int((types == 0).sum())
+    prec = MIXED if args.precision == "mixed" else FP64
+
+    def timed(eng, k):
+        stream = torch.cuda.ExternalStream(eng.stream_ptr())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        stats = []
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(k):
+            stats.append(eng.step())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        return e0.elapsed_time(e1) / 1e3, stats
+
+    # main: mixed precision, state resident in HBM
+    eng = Engine(prm, pos, vel, types, precision=prec)
+    for _ in range(args.warmup):
+        eng.step()
+    with ClockSampler(dev) as clk:
+        sec, stats = timed(eng, args.steps)
+    clocks = clk.summary()
+    if dist:
+        t = torch.tensor([sec], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        sec = float(t.item())
+    value = world * nf * args.steps / sec
+    warm_state = eng.state()
+
+    # roofline of the dominant kernel (the pressure solve)
+    hbm_peak, peak_kind = measured_peaks()
+    solve_ms = [s["ms_solve"] for s in stats]
+    sb = [solver_bytes(prec, s, n) for s in stats]
+    achieved = sum(sb) / (sum(solve_ms) / 1e3) / 1e9
+    row_iters = sum(s["cg_iterations"] for s in stats) * n / len(stats)
+    tpr = traffic_per_row_iter("cg_mixed" if prec == MIXED else "cg64")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(achieved / hbm_peak, 4),
+                "traffic": (tpr * row_iters) if tpr else None,
+                "kernel": "k_cg_mixed" if prec == MIXED else "k_cg64",
+                "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": sum(sb) / len(sb)}
+
+    # plain FP64 on the same steps (skipped with --no-fp64)
+    fp64 = None
+    if not args.no_fp64 and prec == MIXED:
+        e64 = Engine(prm, pos, vel, types, precision=FP64)
+        for _ in range(args.warmup):
+            e64.step()
+        sec64, st64 = timed(e64, args.steps)
+        if dist:
+            t = torch.tensor([sec64], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            sec64 = float(t.item())
+        fp64 = {"value": world * nf * args.steps / sec64, "ms_per_step": 1e3 * sec64 / args.steps,
+                "cg_iterations_mean": float(np.mean([s["cg_iterations"] for s in st64])),
+                "ms_solve_mean": float(np.mean([s["ms_solve"] for s in st64]))}
+        e64.close()
+
+    # accuracy of the mixed step against FP64 from the same state
+    acc = None
+    if prec == MIXED and not args.no_fp64:
+        ws = warm_state
+        ea = Engine(prm, ws["pos"], ws["vel"], ws["type"], precision=FP64)
+        eb = Engine(prm, ws["pos"], ws["vel"], ws["type"], precision=MIXED)
+        ea.step()
+        eb.step()
+        ra, rb = ea.state(), eb.state()
+        pa = np.linalg.norm(ra["pressure"]) or 1.0
+        acc = {"pressure_rel_l2_vs_fp64": float(np.linalg.norm(rb["pressure"] - ra["pressure"]) / pa),
+               "position_max_abs_diff_m": float(np.max(np.abs(rb["pos"] - ra["pos"]))),
+               "surface_flags_equal": bool(np.array_equal(ra["bc"], rb["bc"]))}
+        ea.close()
+        eb.close()
+
+    # end to end through the C ABI with host buffers, every step
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa
+        hpos, hvel, htype = pin(warm_state["pos"]), pin(warm_state["vel"]), pin(warm_state["type"])
+        hp, hndr, hbc = pin(np.zeros(n)), pin(np.zeros(n)), pin(np.zeros(n, np.int32))
+        eng.upload(hpos, hvel, htype)
+        eng.step()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            eng.upload(hpos, hvel, htype)
+            eng.step()
+            eng.download_into(pos=hpos, vel=hvel, pressure=hp, ndr=hndr, types=htype, bc=hbc)
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([te], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te = float(t.item())
+        e2e = {"value": world * nf * args.e2e_steps / te, "unit": UNIT,
+               "h2d_bytes_per_step": int(hpos.nbytes + hvel.nbytes + htype.nbytes),
+               "d2h_bytes_per_step": int(hpos.nbytes + hvel.nbytes + hp.nbytes + hndr.nbytes
+                                         + htype.nbytes + hbc.nbytes),
+               "steps": args.e2e_steps}
+    eng.close()
+
+    if rank != 0:
+        return None
+    cpu = None
+    if not args.no_cpu:
+        try:
+            cpu = cpu_sample()
+        except Exception as ex:  # reported, not hidden
+            cpu = {"value": None, "error": str(ex)[-300:]}
+    mean = lambda k: float(np.mean([s[k] for s in stats]))  # noqa
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32-krylov/fp64" if prec == MIXED else "f64",
+        "data": "synthetic (seeded lattice dam break, the reference generator's layout)",
+        "config": {"workload": f"{args.workload}: dam break, {nf} fluid / {n} particles, "
+                               f"dt {prm['dt']}, {args.precision} PPE solver",
+                   "particles": n, "fluid_particles": nf, "precision": args.precision,
+                   "cache": "working set > L2 (state + neighbour lists + matrix ~ GBs per step)",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "cg_iterations_mean": mean("cg_iterations"), "refinements_mean": mean("refinements"),
+        "ms_solve_mean": mean("ms_solve"),
+        "roofline": roofline, "fp64": fp64,
+        "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
+        "accuracy": acc, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+    }
+    return line
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return None
+    per = []
+    for _ in range(args.warmup if args.warmup < 1 else 0):
+        pass
+    cpu = cpu_sample(steps=max(1, args.steps // 5) + 1)
+    per.append(cpu["value"])
+    return {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{args.workload} (CPU sample: {CPU_SAMPLE})"},
+            "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dambreak_1m")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+    else:
+        if world > 1:
+            import torch.distributed as dist_mod
+
+            dist_mod.init_process_group("nccl")
+            dist = dist_mod
+        line = run_ours(args, rank, world, dist)
+        if dist:
+            dist.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -78,6 +78,9 @@ typedef struct {
     int32_t status;                 /* MPS_OK or the MPS_ERR_* of a device-side failure */
     float ms_step;                  /* device time of the whole step */
     float ms_solve;                 /* device time of the pressure solve */
+    int32_t kernel_launches;        /* kernels this step launched */
+    int64_t nnz_offdiag;            /* stored off-diagonal PPE entries */
+    int32_t max_neighbors;          /* largest neighbour count of the last build */
 } mps_step_stats;
 
 typedef struct mps_engine mps_engine;
@@ -114,6 +117,10 @@ int mps_download(mps_engine* e, double* pos, double* vel, double* pressure,
 int mps_upload(mps_engine* e, const double* pos, const double* vel, const int32_t* type);
 
 int32_t mps_particle_count(const mps_engine* e);
+
+/* The CUDA stream (cudaStream_t) the engine enqueues its kernels on, for
+ * callers that time or order their own work against the step. */
+void* mps_stream(mps_engine* e);
 
 /* Parity/debug views of the last step, in id order. */
 /* Neighbour lists of the last neighbour build (src/mps.cpp:585-619) as CSR;

@@ -130,6 +130,7 @@ struct mps_engine {
     double tol = std::numeric_limits<double>::epsilon();
     int64_t max_iter = 0;
     int32_t debug_log_count = 0;
+    int32_t step_launches = 0;
     cudaEvent_t ev[4]{};
     std::vector<void*> allocs;
 
@@ -180,6 +181,7 @@ int check_status(mps_engine* e) {
 
 // One MPS::stepForward.  Launches only; the caller synchronises.
 void enqueue_step(mps_engine* e, bool do_export) {
+    g_launches = 0;
     Consts& c = e->c;
     cudaStream_t st = e->st;
     const int mixed = e->precision == MPS_PRECISION_MIXED;
@@ -198,7 +200,7 @@ void enqueue_step(mps_engine* e, bool do_export) {
     e->swap();
     launch_build_list(c, e->S(), e->sc, e->nb, e->ds, st);
     launch_bc_source(c, e->S(), e->nb, e->A, e->ds, st);
-    launch_assemble(c, e->S(), e->nb, e->A, st);
+    launch_assemble(c, e->S(), e->nb, e->A, e->ds, st);
     launch_dirichlet(c, e->S(), e->nb, e->A, e->parent, e->has_surface, e->ds, st);
     cudaEventRecord(e->ev[2], st);
     int64_t mi = e->max_iter > 0 ? e->max_iter : 2 * (int64_t)c.n;
@@ -216,6 +218,7 @@ void enqueue_step(mps_engine* e, bool do_export) {
         launch_build_list(c, e->S(), e->sc, e->nb, e->ds, st);
         launch_number_density(c, e->S(), e->nb, st);
     }
+    e->step_launches = g_launches;
 }
 
 void fill_stats(mps_engine* e, mps_step_stats* out) {
@@ -242,6 +245,9 @@ void fill_stats(mps_engine* e, mps_step_stats* out) {
     cudaEventElapsedTime(&ms2, e->ev[2], e->ev[3]);
     out->ms_step = ms;
     out->ms_solve = ms2;
+    out->kernel_launches = e->step_launches;
+    out->nnz_offdiag = (int64_t)h.nnz_off;
+    out->max_neighbors = h.max_neighbors;
 }
 
 }  // namespace
@@ -251,6 +257,8 @@ extern "C" {
 const char* mps_last_error(void) { return g_last_error.c_str(); }
 
 int32_t mps_particle_count(const mps_engine* e) { return e ? e->n : 0; }
+
+void* mps_stream(mps_engine* e) { return e ? (void*)e->st : nullptr; }
 
 int mps_create(const mps_params* prm, int32_t n, const double* pos, const double* vel,
                const int32_t* type, mps_engine** out) {

@@ -13,6 +13,9 @@
 
 namespace mpsg {
 
+// Kernels enqueued by this host thread (reported per step).
+extern thread_local int32_t g_launches;
+
 enum : int8_t { T_GHOST = -1, T_FLUID = 0, T_WALL = 1, T_DUMMY = 2 };
 enum : int8_t { BC_IGNORED = 0, BC_SURFACE = 1, BC_INNER = 2 };
 
@@ -75,6 +78,7 @@ struct DevStats {
     int32_t refinements;
     int32_t pad;
     double cg_rel_residual;
+    unsigned long long nnz_off;
 };
 
 struct CollPair {
@@ -128,7 +132,7 @@ void launch_build_list(const Consts& c, const StateBuf& s, const SortScratch& sc
 void launch_bc_source(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
                       DevStats* ds, cudaStream_t st);
 void launch_assemble(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
-                     cudaStream_t st);
+                     DevStats* ds, cudaStream_t st);
 void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
                       int32_t* parent, int8_t* has_surface, DevStats* ds, cudaStream_t st);
 void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb,

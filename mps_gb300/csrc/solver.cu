@@ -444,6 +444,7 @@ void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double to
     void* args[] = {&cc, &AA, &kk, &a, &ds};
     cudaMemsetAsync(k.barrier, 0, 2 * sizeof(unsigned int), st);
     cudaLaunchCooperativeKernel((const void*)k_cg64, dim3(k.grid), dim3(kBlock), args, 0, st);
+    ++g_launches;
 }
 
 void launch_solve_mixed(const Consts& c, const Ppe& A, const Krylov& k, double tol,
@@ -454,8 +455,10 @@ void launch_solve_mixed(const Consts& c, const Ppe& A, const Krylov& k, double t
     Krylov kk = k;
     void* args[] = {&cc, &AA, &kk, &a, &ds};
     k_to_fp32<<<(c.n + 31 + 255) / 256, 256, 0, st>>>(A, k, c.n, c.K);
+    ++g_launches;
     cudaMemsetAsync(k.barrier, 0, 2 * sizeof(unsigned int), st);
     cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kBlock), args, 0, st);
+    ++g_launches;
 }
 
 }  // namespace mpsg

@@ -13,6 +13,8 @@
 
 namespace mpsg {
 
+thread_local int32_t g_launches = 0;
+
 namespace {
 
 constexpr int kScanThreads = 256;
@@ -186,8 +188,11 @@ void launch_exclusive_scan(const int32_t* in, int32_t* out, int32_t n, int32_t* 
     int nb = (n + kScanTile - 1) / kScanTile;
     if (nb < 1) nb = 1;
     k_scan_reduce<<<nb, kScanThreads, 0, st>>>(in, n, tmp);
+    ++g_launches;
     k_scan_top<<<1, 1024, 0, st>>>(tmp, nb);
+    ++g_launches;
     k_scan_apply<<<nb, kScanThreads, 0, st>>>(in, n, tmp, out);
+    ++g_launches;
 }
 
 void launch_rebuild(const Consts& c, const StateBuf& in, const StateBuf& out, SortScratch& s,
@@ -196,10 +201,14 @@ void launch_rebuild(const Consts& c, const StateBuf& in, const StateBuf& out, So
     int nb = (c.n + T - 1) / T;
     cudaMemsetAsync(s.cell_count, 0, sizeof(int32_t) * (c.nkeys + 1), st);
     k_keys<<<nb, T, 0, st>>>(c, in, s.key, s.rank, s.cell_count);
+    ++g_launches;
     launch_exclusive_scan(s.cell_count, s.cell_start, c.nkeys + 1, s.scan_tmp, st);
     k_scatter<<<nb, T, 0, st>>>(c.n, s.key, s.rank, s.cell_start, s.perm);
+    ++g_launches;
     k_cellsort<<<(c.nkeys + T - 1) / T, T, 0, st>>>(c.nkeys, s.cell_start, s.perm, in.id);
+    ++g_launches;
     k_gather<<<nb, T, 0, st>>>(c.n, s.perm, s.key, s.skey, in, out, c.planar);
+    ++g_launches;
 }
 
 }  // namespace mpsg

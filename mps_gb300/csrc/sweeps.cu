@@ -328,7 +328,8 @@ __global__ void __launch_bounds__(kThreads) k_source_ho(Consts c, StateBuf s, Nb
 }
 
 // MPS::setMatrix (src/mps.cpp:322-360): one SELL-32 row per Inner slot.
-__global__ void __launch_bounds__(kThreads) k_assemble(Consts c, StateBuf s, NbList nb, Ppe A) {
+__global__ void __launch_bounds__(kThreads) k_assemble(Consts c, StateBuf s, NbList nb, Ppe A,
+                                                       DevStats* ds) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     int off = 0;
     if (k < c.n) {
@@ -356,7 +357,11 @@ __global__ void __launch_bounds__(kThreads) k_assemble(Consts c, StateBuf s, NbL
         A.offcnt[k] = off;
     }
     int w = __reduce_max_sync(0xffffffffu, off);
-    if ((threadIdx.x & 31) == 0 && (k >> 5) < (c.n + 31) / 32) A.slice_w[k >> 5] = w;
+    unsigned tot = __reduce_add_sync(0xffffffffu, (unsigned)off);
+    if ((threadIdx.x & 31) == 0 && (k >> 5) < (c.n + 31) / 32) {
+        A.slice_w[k >> 5] = w;
+        if (tot) atomicAdd(&ds->nnz_off, (unsigned long long)tot);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -555,15 +560,21 @@ void launch_explicit(const Consts& c, const StateBuf& in, const StateBuf& out,
                      const SortScratch& sc, int mixed, DevStats* ds, cudaStream_t st) {
     int nb = blocks_for(c.n);
     if (c.planar) {
-        if (mixed)
+        if (mixed) {
             k_explicit<true, true><<<nb, kThreads, 0, st>>>(c, in, out, sc.skey, sc.cell_start, ds);
-        else
+            ++g_launches;
+        } else {
             k_explicit<true, false><<<nb, kThreads, 0, st>>>(c, in, out, sc.skey, sc.cell_start, ds);
+            ++g_launches;
+        }
     } else {
-        if (mixed)
+        if (mixed) {
             k_explicit<false, true><<<nb, kThreads, 0, st>>>(c, in, out, sc.skey, sc.cell_start, ds);
-        else
+            ++g_launches;
+        } else {
             k_explicit<false, false><<<nb, kThreads, 0, st>>>(c, in, out, sc.skey, sc.cell_start, ds);
+            ++g_launches;
+        }
     }
 }
 
@@ -572,46 +583,61 @@ void launch_collision(const Consts& c, const StateBuf& s, const SortScratch& sc,
                       int32_t pair_cap, int32_t* scan_tmp, DevStats* ds, cudaStream_t st) {
     int nb = blocks_for(c.n);
     cudaMemsetAsync(cand_cnt, 0, sizeof(int32_t) * (c.n + 1), st);
-    if (c.planar)
+    if (c.planar) {
         k_coll_count<true><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt);
-    else
+        ++g_launches;
+    } else {
         k_coll_count<false><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt);
+        ++g_launches;
+    }
     launch_exclusive_scan(cand_cnt, cand_base, c.n, scan_tmp, st);
     if (c.planar) {
         k_coll_write<true><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt,
                                                     cand_base, pairs, pair_cap, ds);
+        ++g_launches;
         k_coll_apply<true><<<1, 1, 0, st>>>(c, s, pairs, cand_base + c.n, pair_cap, ds);
+        ++g_launches;
     } else {
         k_coll_write<false><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt,
                                                      cand_base, pairs, pair_cap, ds);
+        ++g_launches;
         k_coll_apply<false><<<1, 1, 0, st>>>(c, s, pairs, cand_base + c.n, pair_cap, ds);
+        ++g_launches;
     }
 }
 
 void launch_build_list(const Consts& c, const StateBuf& s, const SortScratch& sc,
                        const NbList& nb, DevStats* ds, cudaStream_t st) {
     int g = blocks_for(c.n);
-    if (c.planar)
+    if (c.planar) {
         k_build_list<true><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, ds);
-    else
+        ++g_launches;
+    } else {
         k_build_list<false><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, ds);
+        ++g_launches;
+    }
 }
 
 void launch_bc_source(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
                       DevStats* ds, cudaStream_t st) {
     int g = blocks_for(c.n);
     k_bc_source<<<g, kThreads, 0, st>>>(c, s, nb, A, ds);
+    ++g_launches;
     if (c.ho_on) {
-        if (c.planar)
+        if (c.planar) {
             k_source_ho<true><<<g, kThreads, 0, st>>>(c, s, nb, A);
-        else
+            ++g_launches;
+        } else {
             k_source_ho<false><<<g, kThreads, 0, st>>>(c, s, nb, A);
+            ++g_launches;
+        }
     }
 }
 
 void launch_assemble(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
-                     cudaStream_t st) {
-    k_assemble<<<blocks_for(c.n), kThreads, 0, st>>>(c, s, nb, A);
+                     DevStats* ds, cudaStream_t st) {
+    k_assemble<<<blocks_for(c.n), kThreads, 0, st>>>(c, s, nb, A, ds);
+    ++g_launches;
 }
 
 void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
@@ -619,9 +645,13 @@ void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, cons
     int g = blocks_for(c.n);
     cudaMemsetAsync(has_surface, 0, c.n, st);
     k_cc_init<<<g, kThreads, 0, st>>>(c.n, parent);
+    ++g_launches;
     k_cc_hook<<<g, kThreads, 0, st>>>(c, s, nb, parent, ds);
+    ++g_launches;
     k_cc_mark<<<g, kThreads, 0, st>>>(c, s, parent, has_surface, ds);
+    ++g_launches;
     k_cc_apply<<<g, kThreads, 0, st>>>(c, s, parent, has_surface, A, ds);
+    ++g_launches;
 }
 
 void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb, const double* x,
@@ -629,25 +659,36 @@ void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb, 
                           cudaStream_t st) {
     int g = blocks_for(c.n);
     k_pressure_out<<<g, kThreads, 0, st>>>(c.n, x, s.p);
+    ++g_launches;
     k_min_pressure<<<g, kThreads, 0, st>>>(c, s, nb);
+    ++g_launches;
     if (c.planar) {
-        if (mixed)
+        if (mixed) {
             k_gradient<true, true><<<g, kThreads, 0, st>>>(c, s, nb, ax, ay, az);
-        else
+            ++g_launches;
+        } else {
             k_gradient<true, false><<<g, kThreads, 0, st>>>(c, s, nb, ax, ay, az);
+            ++g_launches;
+        }
         k_move2<true><<<g, kThreads, 0, st>>>(c, s, ax, ay, az, ds);
+        ++g_launches;
     } else {
-        if (mixed)
+        if (mixed) {
             k_gradient<false, true><<<g, kThreads, 0, st>>>(c, s, nb, ax, ay, az);
-        else
+            ++g_launches;
+        } else {
             k_gradient<false, false><<<g, kThreads, 0, st>>>(c, s, nb, ax, ay, az);
+            ++g_launches;
+        }
         k_move2<false><<<g, kThreads, 0, st>>>(c, s, ax, ay, az, ds);
+        ++g_launches;
     }
 }
 
 void launch_number_density(const Consts& c, const StateBuf& s, const NbList& /*nb*/,
                            cudaStream_t st) {
     k_number_density<<<blocks_for(c.n), kThreads, 0, st>>>(c, s);
+    ++g_launches;
 }
 
 void launch_initial_number_density(const Consts& c, const StateBuf& s, const SortScratch& sc,

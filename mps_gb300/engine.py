@@ -59,6 +59,9 @@ class MpsStepStats(C.Structure):
         ("status", C.c_int32),
         ("ms_step", C.c_float),
         ("ms_solve", C.c_float),
+        ("kernel_launches", C.c_int32),
+        ("nnz_offdiag", C.c_int64),
+        ("max_neighbors", C.c_int32),
     ]
 
 
@@ -98,6 +101,8 @@ def load(build_if_missing: bool = False):
     L.mps_upload.argtypes = [vp, vp, vp, vp]
     L.mps_particle_count.argtypes = [vp]
     L.mps_particle_count.restype = C.c_int32
+    L.mps_stream.argtypes = [vp]
+    L.mps_stream.restype = C.c_void_p
     L.mps_neighbors.argtypes = [vp, vp, vp, vp, P(C.c_int64)]
     L.mps_system.argtypes = [vp, vp, vp, vp, vp, P(C.c_int64)]
     L.mps_collisions.argtypes = [vp, vp, vp, vp, P(C.c_int32)]
@@ -158,6 +163,10 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+    def stream_ptr(self) -> int:
+        """cudaStream_t the engine launches on (for events around its work)."""
+        return int(_lib.mps_stream(self.h) or 0)
 
     def set_solver(self, precision=FP64, tol=0.0, max_iter=0):
         _check(_lib.mps_set_solver(self.h, int(precision), float(tol), int(max_iter)))

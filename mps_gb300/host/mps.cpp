@@ -1,0 +1,177 @@
+#include "mps.hpp"
+
+#include <cmath>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <stdexcept>
+
+#include "logger.hpp"
+
+namespace {
+void check(int rc) {
+    if (rc != MPS_OK) throw std::runtime_error(std::string("mps engine: ") + mps_last_error());
+}
+double weight(double dist, double re) { return dist < re ? (re / dist) - 1.0 : 0.0; }
+}  // namespace
+
+// src/mps.cpp:132-163
+RefValues::RefValues(const int& dim, const double& l0, const double& re) {
+    int zb = dim == 2 ? 0 : -4, ze = dim == 2 ? 1 : 5;
+    for (int ix = -4; ix < 5; ix++)
+        for (int iy = -4; iy < 5; iy++)
+            for (int iz = zb; iz < ze; iz++) {
+                if (ix == 0 && iy == 0 && iz == 0) continue;
+                Vec3 r(l0 * (double)ix, l0 * (double)iy, l0 * (double)iz);
+                double dist = r.norm();
+                initialNumberDensity += weight(dist, re);
+                lambda += (dist * dist) * weight(dist, re);
+            }
+    lambda /= initialNumberDensity;
+}
+
+// src/mps.cpp:18-36
+MPS::MPS(const std::filesystem::path& inputYamlPath) {
+    settings.load(inputYamlPath);
+    refValues.pressure = RefValues((int)settings.dim, settings.particleDistance, settings.effectiveRadius.pressure);
+    refValues.viscosity = RefValues((int)settings.dim, settings.particleDistance, settings.effectiveRadius.viscosity);
+    refValues.surfaceDetection =
+        RefValues((int)settings.dim, settings.particleDistance, settings.effectiveRadius.surfaceDetection);
+}
+
+// src/mps.cpp:38-94: the CSV written by Exporter::toCsv; ids must be the row
+// indices (the reference indexes particles by id).
+double MPS::importInitialCondition() {
+    std::ifstream in(settings.inputCsvPath);
+    if (!in.is_open())
+        throw std::runtime_error("Input file does not exist in the specified path: " + settings.inputCsvPath.string());
+    std::string line;
+    std::vector<std::string> rows;
+    while (std::getline(in, line)) {
+        if (!line.empty() && line.back() == '\r') line.pop_back();
+        rows.push_back(line);
+    }
+    if (rows.size() < 3) throw std::runtime_error("particle CSV too short: " + settings.inputCsvPath.string());
+    auto split = [](const std::string& s) {
+        std::vector<std::string> f;
+        std::stringstream ss(s);
+        std::string c;
+        while (std::getline(ss, c, ',')) f.push_back(c);
+        return f;
+    };
+    double t0 = std::stod(split(rows[0]).at(1));
+    auto head = split(rows[2]);
+    std::map<std::string, size_t> col;
+    for (size_t k = 0; k < head.size(); k++) col[head[k]] = k;
+    const char* need[] = {"ID", "Type", "Position.x (m)", "Position.y (m)", "Position.z (m)",
+                          "Velocity.x (m/s)", "Velocity.y (m/s)", "Velocity.z (m/s)"};
+    for (const char* k : need)
+        if (!col.count(k)) throw std::runtime_error(std::string("particle CSV lacks column ") + k);
+    particles.clear();
+    for (size_t r = 3; r < rows.size(); r++) {
+        if (rows[r].empty()) continue;
+        auto f = split(rows[r]);
+        int id = std::stoi(f.at(col["ID"]));
+        if (id != (int)particles.size())
+            throw std::runtime_error("particle ids must equal their row index (row " + std::to_string(r) + ")");
+        int type = std::stoi(f.at(col["Type"]));
+        Vec3 x(std::stod(f.at(col["Position.x (m)"])), std::stod(f.at(col["Position.y (m)"])),
+               std::stod(f.at(col["Position.z (m)"])));
+        Vec3 v(std::stod(f.at(col["Velocity.x (m/s)"])), std::stod(f.at(col["Velocity.y (m/s)"])),
+               std::stod(f.at(col["Velocity.z (m/s)"])));
+        particles.emplace_back(id, static_cast<ParticleType>(type), x, v, settings.density);
+    }
+    return t0;
+}
+
+// src/mps.cpp:96-109: import, upload, initial number density.
+double MPS::loadInitialState() {
+    double t0 = importInitialCondition();
+    mps_params p{};
+    p.dim = (int32_t)settings.dim;
+    p.quasi_compressibility_on = settings.quasiCompressibility.on;
+    p.higher_order_on = settings.higherOrderSourceTerm.on;
+    p.particle_distance = settings.particleDistance;
+    p.dt = settings.dt;
+    p.domain_min[0] = settings.domain.x.min;
+    p.domain_min[1] = settings.domain.y.min;
+    p.domain_min[2] = settings.domain.z.min;
+    p.domain_max[0] = settings.domain.x.max;
+    p.domain_max[1] = settings.domain.y.max;
+    p.domain_max[2] = settings.domain.z.max;
+    p.density = settings.density;
+    p.kinematic_viscosity = settings.kinematicViscosity;
+    for (int i = 0; i < 3; i++) p.gravity[i] = settings.gravity[i];
+    p.re_pressure = settings.effectiveRadius.pressure;
+    p.re_viscosity = settings.effectiveRadius.viscosity;
+    p.re_surface = settings.effectiveRadius.surfaceDetection;
+    p.surface_threshold = settings.thresholdForSurfaceDetection;
+    p.compressibility = settings.quasiCompressibility.compressibility;
+    p.higher_order_gamma = settings.higherOrderSourceTerm.gamma;
+    p.relaxation = settings.relaxationCoefficientForPressure;
+    p.collision_distance = settings.collisionDistance;
+    p.restitution = settings.coefficientOfRestitution;
+    p.cfl = settings.cflCondition;
+    const size_t n = particles.size();
+    std::vector<double> pos(3 * n), vel(3 * n);
+    std::vector<int32_t> type(n);
+    for (size_t i = 0; i < n; i++) {
+        for (int c = 0; c < 3; c++) {
+            pos[3 * i + c] = particles[i].position[c];
+            vel[3 * i + c] = particles[i].velocity[c];
+        }
+        type[i] = (int32_t)particles[i].type;
+    }
+    mps_engine* e = nullptr;
+    check(mps_create(&p, (int32_t)n, pos.data(), vel.data(), type.data(), &e));
+    engine.reset(e);
+    check(mps_set_solver(e, precision, tol, maxIter));
+    syncParticles();
+    return t0;
+}
+
+void MPS::setSolver(int prec, double t, long long mi) {
+    precision = prec;
+    tol = t;
+    maxIter = mi;
+    if (engine) check(mps_set_solver(engine.get(), precision, tol, maxIter));
+}
+
+void MPS::syncParticles() {
+    const size_t n = particles.size();
+    std::vector<double> pos(3 * n), vel(3 * n), p(n), mp(n), ndr(n);
+    std::vector<int32_t> type(n), bc(n), dir(n);
+    check(mps_download(engine.get(), pos.data(), vel.data(), p.data(), mp.data(), ndr.data(), type.data(),
+                       bc.data(), dir.data()));
+    for (size_t i = 0; i < n; i++) {
+        Particle& q = particles[i];
+        for (int c = 0; c < 3; c++) {
+            q.position[c] = pos[3 * i + c];
+            q.velocity[c] = vel[3 * i + c];
+        }
+        q.pressure = p[i];
+        q.minimumPressure = mp[i];
+        q.numberDensityRatio = ndr[i];
+        q.type = static_cast<ParticleType>(type[i]);
+        q.boundaryCondition = static_cast<BoundaryCondition>(bc[i]);
+        q.isDirichletBoundaryConnected = dir[i] != 0;
+    }
+}
+
+// src/mps.cpp:111-130 (the whole step on the GPU); the debug events the
+// reference logs one by one are logged here as counts.
+double MPS::stepForward(const bool isTimeToExport) {
+    if (!engine) throw std::runtime_error("MPS::stepForward before loadInitialState");
+    check(mps_step(engine.get(), isTimeToExport ? 1 : 0, &stats));
+    if (stats.n_new_ghosts > 0)
+        mpslog::debug(std::to_string(stats.n_new_ghosts) + " particle(s) went out of the domain.");
+    if (stats.n_unconnected > 0)
+        mpslog::debug("There is no Dirichlet boundary condition connected to " +
+                      std::to_string(stats.n_unconnected) + " particle(s).");
+    if (stats.courant > settings.cflCondition)
+        mpslog::debug("Courant number is larger than CFL condition. Courant=" + std::to_string(stats.courant));
+    if (stats.courant > 1.0) mpslog::error("Courant number is larger than 1.0. Exiting Simulation.");
+    debugLogCount = stats.debug_log_count;
+    if (isTimeToExport) syncParticles();
+    return stats.courant;
+}

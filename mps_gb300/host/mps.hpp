@@ -1,0 +1,58 @@
+// The reference's MPS class (src/mps.hpp:22-71) with the same public surface:
+// MPS(yaml), loadInitialState(), stepForward(isTimeToExport), and the public
+// members settings, particles and debugLogCount.  The step itself runs on
+// the GPU through the engine's C ABI (include/mps_gb300.h); `particles`
+// mirrors the device state after loadInitialState and after every export
+// step (call syncParticles() to refresh it at any other time).
+#pragma once
+#include <filesystem>
+#include <memory>
+#include <vector>
+
+#include "bucket.hpp"
+#include "mps_gb300.h"
+#include "particle.hpp"
+#include "settings.hpp"
+
+class RefValues {
+public:
+    double initialNumberDensity = 0;
+    double lambda = 0;
+    RefValues() = default;
+    RefValues(const int& dim, const double& particleDistance, const double& effectiveRadius);
+};
+
+class MPS {
+public:
+    Settings settings;
+    std::vector<Particle> particles;
+    int debugLogCount = 0;
+
+    MPS() = default;
+    explicit MPS(const std::filesystem::path& inputYamlPath);
+    MPS(MPS&&) noexcept = default;
+    MPS& operator=(MPS&&) noexcept = default;
+
+    double loadInitialState();  // Initialize particles and return initial time
+    double stepForward(const bool isTimeToExport);
+
+    // Additions of this implementation.
+    void setSolver(int precision, double tol = 0.0, long long maxIter = 0);
+    void syncParticles();
+    const mps_step_stats& lastStepStats() const { return stats; }
+
+private:
+    struct EngineDeleter {
+        void operator()(mps_engine* e) const { mps_destroy(e); }
+    };
+    std::unique_ptr<mps_engine, EngineDeleter> engine;
+    mps_step_stats stats{};
+    int precision = MPS_PRECISION_FP64;
+    double tol = 0.0;
+    long long maxIter = 0;
+    struct {
+        RefValues pressure, viscosity, surfaceDetection;
+    } refValues;
+
+    double importInitialCondition();
+};

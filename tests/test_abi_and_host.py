@@ -1,0 +1,119 @@
+"""CPU-only checks: the C ABI library builds, loads and exports every entry
+point its header declares; the C++ front end reads the reference's settings
+format like the Python reader; scene generation and the CSV format."""
+import ctypes
+import json
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared(header):
+    text = open(os.path.join(REPO, "include", header)).read()
+    return sorted(set(re.findall(r"\b(mps_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def built():
+    from mps_gb300 import build
+
+    so = build.build_engine()
+    exe = build.build_host()
+    return so, exe
+
+
+def test_library_exports_every_declared_symbol(built):
+    so, _ = built
+    lib = ctypes.CDLL(so)
+    names = _declared("mps_gb300.h")
+    assert "mps_create" in names and "mps_step" in names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True).stdout
+    for n in names:
+        assert re.search(rf"\bT {n}\b", out), n
+
+
+def test_create_without_gpu_fails_loudly(built):
+    """No silent CPU path: without a device the engine refuses to start."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from mps_gb300 import Engine, MpsError, scenes
+
+    prm, pos, vel, t = scenes.dam_break(0.05, tank=(0.5, 0.4), column=(0.2, 0.2))
+    with pytest.raises(MpsError):
+        Engine(prm, pos, vel, t)
+
+
+def _yaml(tmp_path, prm):
+    import sys
+
+    sys.path.insert(0, os.path.join(REPO, "tests", "golden"))
+    from make_golden import yaml_text
+
+    p = tmp_path / "settings.yml"
+    p.write_text(yaml_text(prm, "input.csv"))
+    return p
+
+
+@pytest.mark.parametrize("variant", ["dambreak", "higher_order", "three_d"])
+def test_cpp_settings_reader_matches_python(built, tmp_path, variant):
+    from mps_gb300 import scenes
+    from mps_gb300.settings import load_settings
+
+    prm, *_ = scenes.dam_break(0.01)
+    if variant == "higher_order":
+        prm.update(higher_order_on=1, higher_order_gamma=1e-3, quasi_compressibility_on=0)
+    if variant == "three_d":
+        prm.update(dim=3, domain_min=[-0.1, -0.1, -0.2], domain_max=[1.1, 0.7, 0.2])
+    path = _yaml(tmp_path, prm)
+    _, exe = built
+    out = subprocess.run([exe, "-s", str(path), "--check-settings"], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    c = json.loads(out.stdout)
+    py = load_settings(str(path))
+    for k in ("particle_distance", "dt", "re_pressure", "re_viscosity", "re_surface", "density",
+              "kinematic_viscosity", "surface_threshold", "relaxation", "collision_distance",
+              "restitution", "cfl", "compressibility", "higher_order_gamma"):
+        assert c[k] == py[k], k
+    assert c["dim"] == py["dim"]
+    assert c["domain_min"] == py["domain_min"] and c["domain_max"] == py["domain_max"]
+    assert c["gravity"] == py["gravity"]
+    assert c["quasi_compressibility_on"] == py["quasi_compressibility_on"]
+    assert c["higher_order_on"] == py["higher_order_on"]
+    assert c["re_max"] == max(py["re_pressure"], py["re_viscosity"], py["re_surface"])
+
+
+def test_cli_rejects_missing_settings(built, tmp_path):
+    _, exe = built
+    out = subprocess.run([exe, "-s", str(tmp_path / "nope.yml")], capture_output=True, text=True)
+    assert out.returncode != 0 and "cannot be found" in out.stdout
+
+
+def test_scene_counts_match_configurations():
+    from mps_gb300 import scenes
+
+    _, _, _, t = scenes.dam_break(0.01)
+    assert (t == 0).sum() == 1250                       # 25 x 50 column
+    _, _, _, t = scenes.dam_break(0.5 / 707, tank=(2.0, 1.2), column=(0.5, 1.0), dt=5e-5)
+    assert (t == 0).sum() == 707 * 1414                 # 999,698
+    _, _, _, t = scenes.hydrostatic(2.5e-3)
+    assert (t == 0).sum() == 160 * 160                  # 25,600
+
+
+def test_csv_round_trip(tmp_path):
+    from mps_gb300 import scenes
+
+    _, pos, vel, t = scenes.dam_break(0.02, tank=(0.4, 0.3), column=(0.1, 0.2))
+    p = tmp_path / "in.csv"
+    scenes.write_csv(p, pos, vel, t, time=0.25)
+    t0, pos2, vel2, t2 = scenes.read_csv(p)
+    assert t0 == 0.25 and np.array_equal(t2, t)
+    assert np.allclose(pos2, pos, atol=5e-7) and np.allclose(vel2, vel, atol=5e-7)
