@@ -31,7 +31,8 @@ enum {
     MPS_ERR_CUDA = 2,        /* a CUDA call failed; the engine should be destroyed */
     MPS_ERR_CAPACITY = 3,    /* a particle had more neighbours than the engine's list capacity */
     MPS_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up (kernel returned early) */
-    MPS_ERR_NO_DEVICE = 5    /* no CUDA device, or not an sm_103 part */
+    MPS_ERR_NO_DEVICE = 5,   /* no CUDA device, or not an sm_103 part */
+    MPS_ERR_NONFINITE = 6    /* a particle position became NaN/inf; it was made a ghost */
 };
 
 enum { MPS_PRECISION_FP64 = 0, MPS_PRECISION_MIXED = 1 };

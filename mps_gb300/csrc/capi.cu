@@ -116,6 +116,7 @@ struct mps_engine {
     NbList nb{};
     Ppe A{};
     Krylov kv{};
+    MatFree mf{};
     int32_t *cand_cnt = nullptr, *cand_base = nullptr;
     CollPair* pairs = nullptr;
     int32_t pair_cap = 0;
@@ -172,6 +173,8 @@ int alloc_state(mps_engine* e, StateBuf& s) {
 int check_status(mps_engine* e) {
     int32_t s = e->hs->status;
     if (s & ST_TIMEOUT) return fail(MPS_ERR_TIMEOUT, "a bounded device-side wait gave up");
+    if (s & ST_NONFINITE)
+        return fail(MPS_ERR_NONFINITE, "a pressure or particle position became non-finite");
     if (s & ST_CAPACITY)
         return fail(MPS_ERR_CAPACITY, "neighbour or collision list capacity exceeded (max neighbours " +
                                           std::to_string(e->hs->max_neighbors) + ", capacity " +
@@ -186,17 +189,17 @@ void enqueue_step(mps_engine* e, bool do_export) {
     cudaStream_t st = e->st;
     const int mixed = e->precision == MPS_PRECISION_MIXED;
     // setNeighbors + calcGravity + calcViscosity + moveParticles
-    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, st);
+    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
     e->swap();
     launch_explicit(c, e->S(), e->buf[e->cur ^ 1], e->sc, mixed, e->ds, st);
     e->swap();
     // setNeighbors + collision
-    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, st);
+    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
     e->swap();
     launch_collision(c, e->S(), e->sc, e->cand_cnt, e->cand_base, nullptr, e->pairs, e->pair_cap,
                      e->sc.scan_tmp, e->ds, st);
     // setNeighbors + calcPressure
-    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, st);
+    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
     e->swap();
     launch_build_list(c, e->S(), e->sc, e->nb, e->ds, st);
     launch_bc_source(c, e->S(), e->nb, e->A, e->ds, st);
@@ -204,16 +207,17 @@ void enqueue_step(mps_engine* e, bool do_export) {
     launch_dirichlet(c, e->S(), e->nb, e->A, e->parent, e->has_surface, e->ds, st);
     cudaEventRecord(e->ev[2], st);
     int64_t mi = e->max_iter > 0 ? e->max_iter : 2 * (int64_t)c.n;
-    if (mixed)
-        launch_solve_mixed(c, e->A, e->kv, e->tol, mi, e->ds, st);
-    else
+    if (mixed) {
+        launch_mixed_setup(c, e->sc, e->A, e->mf, e->kv, st);
+        launch_solve_mixed(c, e->A, e->mf, e->kv, e->tol, mi, e->ds, st);
+    } else
         launch_solve_fp64(c, e->A, e->kv, e->tol, mi, e->ds, st);
     cudaEventRecord(e->ev[3], st);
     // removeNegativePressure, setMinimumPressure, calcPressureGradient,
     // moveParticlesWithPressureGradient, getCourantNumber
     launch_pressure_post(c, e->S(), e->nb, e->kv.x, e->ax, e->ay, e->az, mixed, e->ds, st);
     if (do_export || c.ho_on) {  // setNumberDensity
-        launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, st);
+        launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
         e->swap();
         launch_build_list(c, e->S(), e->sc, e->nb, e->ds, st);
         launch_number_density(c, e->S(), e->nb, st);
@@ -350,6 +354,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     int lc = lattice_count(P.dim, c.re_max / c.l0);
     c.K = std::max(32, ((2 * lc + 8 + 31) / 32) * 32);
     e->nb.n_pad = e->n_pad;
+    e->mf.enabled = c.planar;
 
     int rc = MPS_OK;
     auto bail = [&](int code) {
@@ -373,8 +378,11 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         e->alloc(&e->A.diag32, np) || e->alloc(&e->kv.x, np) || e->alloc(&e->kv.r, np) ||
         e->alloc(&e->kv.p, np) || e->alloc(&e->kv.q, np) || e->alloc(&e->kv.z, np) ||
         e->alloc(&e->kv.inv_diag, np) || e->alloc(&e->kv.r32, np) || e->alloc(&e->kv.p32, np) ||
-        e->alloc(&e->kv.q32, np) || e->alloc(&e->kv.z32, np) || e->alloc(&e->kv.x32, np) ||
-        e->alloc(&e->kv.inv_diag32, np) || e->alloc(&e->kv.barrier, 4) ||
+        e->alloc(&e->kv.s32, np) || e->alloc(&e->kv.w32, np) || e->alloc(&e->kv.x32, np) ||
+        e->alloc(&e->kv.u32, np) ||
+        e->alloc(&e->kv.inv_diag32, np) || e->alloc(&e->kv.barrier, 64) ||
+        e->alloc(&e->kv.totals, 8) || e->alloc(&e->mf.idx8, np * K) ||
+        e->alloc(&e->mf.sell_row, np) ||
         e->alloc(&e->cand_cnt, np + 1) || e->alloc(&e->cand_base, np + 2) ||
         e->alloc(&e->parent, np) || e->alloc(&e->has_surface, np) || e->alloc(&e->ax, np) ||
         e->alloc(&e->ay, np) || e->alloc(&e->az, np) || e->alloc(&e->stage, 3 * np) ||
@@ -383,7 +391,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     e->pair_cap = (int32_t)std::min<size_t>(4 * np + 1024, (size_t)1 << 30);
     if (e->alloc(&e->pairs, e->pair_cap)) return bail(fail(MPS_ERR_CUDA, "cudaMalloc pairs"));
     solver_setup(e->kv, e->n_pad, dev);
-    if (e->alloc(&e->kv.partials, (size_t)e->kv.grid * 8))
+    if (e->alloc(&e->kv.partials, (size_t)e->kv.grid * 16))
         return bail(fail(MPS_ERR_CUDA, "cudaMalloc partials"));
     if (cudaMallocHost(&e->hs, sizeof(DevStats)) != cudaSuccess)
         return bail(fail(MPS_ERR_CUDA, "cudaMallocHost"));
@@ -417,7 +425,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     e->cur = 0;
     // MPS::loadInitialState's setNumberDensity (src/mps.cpp:106)
     CU(cudaMemsetAsync(e->ds, 0, sizeof(DevStats), e->st));
-    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->st);
+    launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, e->st);
     e->swap();
     launch_initial_number_density(c, e->S(), e->sc, e->nb, e->ds, e->st);
     CU(cudaMemcpyAsync(e->hs, e->ds, sizeof(DevStats), cudaMemcpyDeviceToHost, e->st));

@@ -23,6 +23,7 @@ enum : int8_t { BC_IGNORED = 0, BC_SURFACE = 1, BC_INNER = 2 };
 enum : int32_t {
     ST_CAPACITY = 1,  // neighbour list overflow
     ST_TIMEOUT = 2,   // a bounded wait gave up
+    ST_NONFINITE = 4, // a particle position became NaN or infinite
 };
 
 // Constants of one scene, computed on the host with the reference's
@@ -94,7 +95,7 @@ struct SortScratch {
     int32_t *scan_tmp;                  // block sums
 };
 void launch_rebuild(const Consts& c, const StateBuf& in, const StateBuf& out, SortScratch& s,
-                    cudaStream_t st);
+                    DevStats* ds, cudaStream_t st);
 // exclusive scan of n int32 (in-place allowed); out has n+1 entries (total last)
 void launch_exclusive_scan(const int32_t* in, int32_t* out, int32_t n, int32_t* tmp,
                            cudaStream_t st);
@@ -113,11 +114,26 @@ struct Ppe {
     double* src;      // per slot
     double* diag;     // per slot (0 for rows that are not Inner)
     int32_t* offcnt;  // per slot
-    int32_t* col;     // SELL-32, width K: ((slot/32)*K + m)*32 + slot%32
+    int32_t* col;     // SELL-32, width K: ((slot/32)*K + m)*32 + slot%32; padding = (own slot, 0)
     double* val;
     int32_t* slice_w; // max offcnt of each 32-slot slice
-    float* val32;     // FP32 copy of val (mixed path)
+    float* val32;     // FP32 copy of val (mixed path, rows without a matrix-free form)
     float* diag32;
+};
+
+// Compact FP32 form of the PPE operator for the mixed solver (planar
+// scenes): SELL-32 like the FP64 matrix, but each entry is an FP32 value and
+// one index byte: 2 bits for which of the row's 3 candidate column ranges
+// (cells jx = ix-1, ix, ix+1 of its neighbour sweep) holds the column, 6 bits
+// for the offset inside that range; the range starts come from the cell
+// table.  5 B per entry instead of the FP64 matrix's 12 B.
+struct MatFree {
+    uint8_t* idx8;              // SELL-32 layout like Ppe::col
+    int8_t* sell_row;           // 1: this row uses the int32 SELL columns instead
+    const int32_t* skey;        // cell key per slot (from the last rebuild)
+    const int32_t* cs;          // cell start table
+    int32_t numY;
+    int32_t enabled;            // planar scenes only
 };
 
 void launch_initial_number_density(const Consts& c, const StateBuf& s, const SortScratch& sc,
@@ -144,17 +160,21 @@ void launch_number_density(const Consts& c, const StateBuf& s, const NbList& nb,
 // --------------------------------------------------------------- solver.cu
 struct Krylov {
     double *x, *r, *p, *q, *z, *inv_diag;
-    float *r32, *p32, *q32, *z32, *x32, *inv_diag32;
-    double* partials;  // per block, several slots
-    unsigned int* barrier;  // grid barrier counter + generation
-    int32_t grid;      // cooperative grid size
+    float *r32, *p32, *s32, *w32, *x32, *u32, *inv_diag32;
+    double* partials;       // 2 x grid x 8 per-block partial sums
+    unsigned int* barrier;  // monotonically increasing arrival counter
+    double* totals;         // unused scratch (8 doubles)
+    int32_t grid;           // cooperative grid size
     int32_t block;
 };
 void solver_setup(Krylov& k, int32_t n_pad, int device);
 // Solves A x = b; returns through DevStats (iterations, residual, status).
 void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double tol,
                        int64_t max_iter, DevStats* ds, cudaStream_t st);
-void launch_solve_mixed(const Consts& c, const Ppe& A, const Krylov& k, double tol,
-                        int64_t max_iter, DevStats* ds, cudaStream_t st);
+void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const Krylov& k,
+                        double tol, int64_t max_iter, DevStats* ds, cudaStream_t st);
+// FP32 copy of the assembled matrix in the compact layout of MatFree.
+void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, MatFree& mf,
+                        const Krylov& k, cudaStream_t st);
 
 }  // namespace mpsg

@@ -1,24 +1,29 @@
 // Pressure Poisson solve (src/mps.cpp:417-470).
 //
-// Both solvers are single persistent cooperative kernels: one launch per
-// solve, the blocks stay resident and meet at a grid barrier between the
-// phases of an iteration, and the convergence test runs on the device, so no
-// host round trip is needed per iteration.  Every block reduces the per-block
-// partial sums of a dot product in the same fixed order, so all blocks take
-// the same branch and the result is run-to-run deterministic.
+// Both solvers are persistent cooperative kernels: one launch per solve, the
+// blocks stay resident and meet at grid barriers between the phases of an
+// iteration, and the convergence test runs on the device.  A dot product is
+// reduced per block, written as one partial per block, and summed in a fixed
+// order by the last block to reach the barrier, which publishes the total
+// before it releases the others; results are therefore run-to-run
+// deterministic and every block takes the same branch.
 //
-//  * FP64: the Jacobi-preconditioned CG that Eigen::ConjugateGradient runs
-//    with its defaults (zero start, tolerance on the recursive residual
-//    ||r||^2 < max(tol^2 ||b||^2, DBL_MIN), cap 2n), over the SELL-32 FP64
-//    matrix.  Roofline: HBM (12 B per stored entry per iteration) and FP64
+//  * FP64 (k_cg64): the Jacobi-preconditioned CG that Eigen's
+//    ConjugateGradient runs with its defaults (zero start, stop when
+//    ||r||^2 < max(tol^2 ||b||^2, DBL_MIN) on the recursive residual, cap 2n),
+//    over the SELL-32 FP64 matrix; three phases per iteration as Eigen's loop
+//    is written.  Roofline: HBM (12 B per stored entry and iteration) and FP64
 //    issue (one DFMA per entry).
-//  * MIXED: iterative refinement.  The residual r = b - A x and the solution
-//    x stay FP64 (FP64 matrix); each correction A d = r is solved by Jacobi
-//    CG on the FP32 copy of the matrix with FP32 vectors and FP64-accurate
-//    dot products (error-free FP32 products, compensated per thread, FP64
-//    across threads and blocks).
+//  * MIXED (k_cg_mixed): iterative refinement.  x and the residual
+//    r = b - A x stay FP64 (FP64 matrix); each correction A d = r is solved
+//    by Jacobi CG in the Chronopoulos-Gear arrangement (one fused reduction
+//    and two barriers per iteration) on an FP32 form of the operator with
+//    FP32 vectors and FP64-accurate dot products (error-free FP32 products
+//    accumulated with compensation per thread, FP64 across threads and
+//    blocks).  On planar scenes the FP32 matrix is stored with one index
+//    byte per entry (range of the neighbour sweep + offset), 5 B per entry.
 #include <cfloat>
-#include <cstdio>
+#include <cmath>
 
 #include "devutil.cuh"
 #include "engine.cuh"
@@ -27,9 +32,10 @@ namespace mpsg {
 
 namespace {
 
-constexpr int kBlock = 256;
+// One 1024-thread block per SM: 152 blocks meet at each grid barrier.
+constexpr int kBlock = 1024;
 constexpr int kWarps = kBlock / 32;
-constexpr long long kBarrierSpinLimit = 1ll << 24;  // ~1 s with the back-off below
+constexpr long long kSpinLimit = 1ll << 25;  // ~1-2 s with the back-off below
 
 struct SolveArgs {
     int32_t n;          // rows (slots)
@@ -41,120 +47,183 @@ struct SolveArgs {
     int32_t max_refine;
 };
 
-// Grid barrier with a bounded wait: the blocks of a cooperative launch are
-// co-resident, so it always completes; if it somehow does not, the waiting
-// block raises ST_TIMEOUT and every block leaves at its next check.
-__device__ __forceinline__ bool grid_sync(unsigned int* bar, DevStats* ds) {
+// ---------------------------------------------------------------- barriers
+// Grid barrier on one monotonically increasing arrival counter: block b's
+// e-th barrier adds 1 (a release reduction, no reply) and waits until the
+// counter reaches e * gridDim.x.  No block resets anything, so there is no
+// reset race, and the arrivals do not serialise on returning atomics.  The
+// wait is bounded: the blocks of a cooperative launch are co-resident, so it
+// always completes; if it somehow does not, the block raises ST_TIMEOUT and
+// every block leaves at its next barrier.
+struct GridBar {
+    unsigned int* count;
+    unsigned int epoch;  // barriers passed by this block (same in every block)
+    int parity;          // which half of the partials buffer the next reduction uses
+};
+
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void red_release_add(unsigned int* p, unsigned int v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ bool grid_sync(GridBar& gb, DevStats* ds) {
+    __shared__ int s_ok;
     __syncthreads();
-    __shared__ int s_abort;
+    gb.epoch++;
     if (threadIdx.x == 0) {
-        volatile unsigned int* vgen = bar + 1;
-        unsigned int gen = *vgen;
-        __threadfence();
-        unsigned int arrived = atomicAdd(bar, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            long long it = 0;
-            while (*vgen == gen) {
-                if (++it > kBarrierSpinLimit) {
-                    atomicOr(&ds->status, ST_TIMEOUT);
-                    break;
-                }
-                __nanosleep(64);
+        const unsigned int target = gb.epoch * gridDim.x;
+        red_release_add(gb.count, 1u);
+        bool ok = true;
+        long long it = 0;
+        while ((int)(ld_acquire(gb.count) - target) < 0) {
+            if (++it > kSpinLimit) {
+                atomicOr(&ds->status, ST_TIMEOUT);
+                ok = false;
+                break;
             }
+            if (it > 256) __nanosleep(16);
         }
-        __threadfence();
-        s_abort = (*(volatile int*)&ds->status & ST_TIMEOUT) != 0;
+        s_ok = ok && !(*(volatile int*)&ds->status & ST_TIMEOUT);
     }
     __syncthreads();
-    return s_abort == 0;
+    return s_ok != 0;
 }
 
-// Block-level sum of up to 3 doubles; writes partials[slot * G + block].
+// Barrier that also sums M per-thread doubles over the whole grid: each
+// block reduces its threads through shared memory (one warp, fixed order),
+// publishes one partial, and after the barrier every block sums the partials
+// in block order, so all blocks hold bitwise the same totals.  Partials are
+// double-buffered so that a fast block's next reduction never overwrites
+// values a slow block is still reading.
 template <int M>
-__device__ __forceinline__ void block_partials(double (&v)[M], double* partials) {
-    __shared__ double sh[M][kWarps];
+__device__ __forceinline__ bool reduce_sync(const Krylov& kv, GridBar& gb, const double (&v)[M],
+                                            double (&tot)[M], DevStats* ds) {
+    __shared__ double sh[M][kBlock];
+    __shared__ double s_tot[M];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double* part = kv.partials + (size_t)gb.parity * gridDim.x * 8;
+    gb.parity ^= 1;
 #pragma unroll
-    for (int m = 0; m < M; m++) {
-        double x = v[m];
+    for (int m = 0; m < M; m++) sh[m][threadIdx.x] = v[m];
+    __syncthreads();
+    if (warp == 0) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if ((threadIdx.x & 31) == 0) sh[m][threadIdx.x >> 5] = x;
+        for (int m = 0; m < M; m++) {
+            double a = 0.0;
+#pragma unroll 8
+            for (int t = 0; t < kWarps; t++) a += sh[m][lane + 32 * t];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if (lane == 0) part[blockIdx.x * 8 + m] = a;
+        }
+    }
+    if (!grid_sync(gb, ds)) return false;
+    if (warp == 0) {
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+            double a = 0.0;
+            for (int b = lane; b < (int)gridDim.x; b += 32) a += __ldcg(part + b * 8 + m);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if (lane == 0) s_tot[m] = a;
+        }
     }
     __syncthreads();
-    if (threadIdx.x < M) {
-        double s = 0.0;
-        for (int w = 0; w < kWarps; w++) s += sh[threadIdx.x][w];
-        partials[threadIdx.x * gridDim.x + blockIdx.x] = s;
-    }
-    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < M; m++) tot[m] = s_tot[m];
+    return true;
 }
 
-// Every block sums the G partials of slot m in the same order (deterministic).
-template <int M>
-__device__ __forceinline__ void grid_totals(const double* partials, double (&out)[M]) {
-    __shared__ double sh[M][kWarps];
-    const int G = gridDim.x;
-#pragma unroll
-    for (int m = 0; m < M; m++) {
-        double x = 0.0;
-        for (int b = threadIdx.x; b < G; b += blockDim.x) x += __ldcg(partials + m * G + b);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if ((threadIdx.x & 31) == 0) sh[m][threadIdx.x >> 5] = x;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int m = 0; m < M; m++) {
-        double s = 0.0;
-        for (int w = 0; w < kWarps; w++) s += sh[m][w];
-        out[m] = s;
-    }
-    __syncthreads();
-}
-
-// y = A x for the rows of slice `sl`, lane `lane` (FP64 SELL-32).
+// ------------------------------------------------------------------ SpMV
+// y_i = sum over the SELL-32 row (padding entries are (i, 0)) + diag_i x_i,
+// loads batched four at a time so that gathers overlap.
 __device__ __forceinline__ double spmv64_row(const Ppe& A, int K, int sl, int lane, int row,
                                              const double* __restrict__ x, double xi) {
-    const int w = A.slice_w[sl];
-    const size_t base = (size_t)sl * K * 32 + lane;
-    const int cnt = A.offcnt[row];
-    double s = 0.0;
-    for (int m = 0; m < w; m++) {
-        int col = __ldg(A.col + base + (size_t)m * 32);
-        double v = __ldg(A.val + base + (size_t)m * 32);
-        if (m < cnt) s = fma(v, __ldcg(x + col), s);
+    const int w = __ldg(A.slice_w + sl);
+    const int32_t* cp = A.col + (size_t)sl * K * 32 + lane;
+    const double* vp = A.val + (size_t)sl * K * 32 + lane;
+    double s0 = 0.0, s1 = 0.0;
+    int m = 0;
+    for (; m + 4 <= w; m += 4) {
+        int c0 = __ldg(cp + (m + 0) * 32), c1 = __ldg(cp + (m + 1) * 32);
+        int c2 = __ldg(cp + (m + 2) * 32), c3 = __ldg(cp + (m + 3) * 32);
+        double v0 = __ldg(vp + (m + 0) * 32), v1 = __ldg(vp + (m + 1) * 32);
+        double v2 = __ldg(vp + (m + 2) * 32), v3 = __ldg(vp + (m + 3) * 32);
+        double x0 = __ldcg(x + c0), x1 = __ldcg(x + c1), x2 = __ldcg(x + c2), x3 = __ldcg(x + c3);
+        s0 = fma(v0, x0, s0);
+        s1 = fma(v1, x1, s1);
+        s0 = fma(v2, x2, s0);
+        s1 = fma(v3, x3, s1);
     }
-    return fma(A.diag[row], xi, s);
+    for (; m < w; m++) s0 = fma(__ldg(vp + m * 32), __ldcg(x + __ldg(cp + m * 32)), s0);
+    return fma(A.diag[row], xi, s0 + s1);
 }
 
-__device__ __forceinline__ float spmv32_row(const Ppe& A, int K, int sl, int lane, int row,
-                                            const float* __restrict__ x, float xi, int cnt) {
-    const int w = A.slice_w[sl];
-    const size_t base = (size_t)sl * K * 32 + lane;
+// FP32 SELL row (rows without a matrix-free form)
+__device__ __forceinline__ float spmv32_sell_row(const Ppe& A, int K, int row,
+                                                 const float* __restrict__ u) {
+    const int sl = row >> 5, lane = row & 31;
+    const int w = __ldg(A.slice_w + sl);
+    const int32_t* cp = A.col + (size_t)sl * K * 32 + lane;
+    const float* vp = A.val32 + (size_t)sl * K * 32 + lane;
     float s = 0.f;
-    for (int m = 0; m < w; m++) {
-        int col = __ldg(A.col + base + (size_t)m * 32);
-        float v = __ldg(A.val32 + base + (size_t)m * 32);
-        if (m < cnt) s = fmaf(v, __ldcg(x + col), s);
+    for (int m = 0; m < w; m++) s = fmaf(__ldg(vp + m * 32), __ldcg(u + __ldg(cp + m * 32)), s);
+    return s;
+}
+
+// Compact FP32 row: entries (value, range/offset byte); column =
+// start of range + offset.  Loads batched four at a time.
+__device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf, int K, int row,
+                                                 const float* __restrict__ u) {
+    const int sl = row >> 5, lane = row & 31;
+    const int w = __ldg(A.slice_w + sl);
+    const int32_t key = __ldg(mf.skey + row);
+    const int ix = key / mf.numY, iy = key - ix * mf.numY;
+    const int base0 = (ix - 1) * mf.numY + iy - 1;
+    const int s0 = __ldg(mf.cs + base0), s1 = __ldg(mf.cs + base0 + mf.numY),
+              s2 = __ldg(mf.cs + base0 + 2 * mf.numY);
+    const uint8_t* ip = mf.idx8 + (size_t)sl * K * 32 + lane;
+    const float* vp = A.val32 + (size_t)sl * K * 32 + lane;
+    float a0 = 0.f, a1 = 0.f;
+    int m = 0;
+    for (; m + 4 <= w; m += 4) {
+        int c[4];
+        float v[4], x[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int b = __ldg(ip + (m + t) * 32);
+            const int r = b >> 6;
+            c[t] = (r == 0 ? s0 : (r == 1 ? s1 : s2)) + (b & 63);
+            v[t] = __ldg(vp + (m + t) * 32);
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) x[t] = __ldcg(u + c[t]);
+        a0 = fmaf(v[0], x[0], a0);
+        a1 = fmaf(v[1], x[1], a1);
+        a0 = fmaf(v[2], x[2], a0);
+        a1 = fmaf(v[3], x[3], a1);
     }
-    return fmaf(A.diag32[row], xi, s);
+    for (; m < w; m++) {
+        const int b = __ldg(ip + m * 32);
+        const int r = b >> 6;
+        a0 = fmaf(__ldg(vp + m * 32), __ldcg(u + (r == 0 ? s0 : (r == 1 ? s1 : s2)) + (b & 63)), a0);
+    }
+    return a0 + a1;
 }
 
 // ----------------------------------------------------------------- FP64 CG
-__global__ void __launch_bounds__(kBlock) k_cg64(Consts c, Ppe A, Krylov kv, SolveArgs a,
-                                                 DevStats* ds) {
+__global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs a, DevStats* ds) {
+    GridBar gb{kv.barrier, 0u, 0};
     const int lane = threadIdx.x & 31;
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    unsigned int* bar = kv.barrier;
-    double* P = kv.partials;
 
-    // setup: x = 0, r = b, inv_diag, ||b||^2
-    double acc[1] = {0.0};
+    double acc[1] = {0.0}, tot[1];
     for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
         int i = sl * 32 + lane;
         if (i >= a.n) continue;
@@ -165,20 +234,14 @@ __global__ void __launch_bounds__(kBlock) k_cg64(Consts c, Ppe A, Krylov kv, Sol
         kv.r[i] = b;
         acc[0] = fma(b, b, acc[0]);
     }
-    block_partials<1>(acc, P);
-    if (!grid_sync(bar, ds)) return;
-    double tot[1];
-    grid_totals<1>(P, tot);
+    if (!reduce_sync<1>(kv, gb, acc, tot, ds)) return;
     const double rhs2 = tot[0];
     int64_t it = 0;
     double rn2 = rhs2;
-    if (rhs2 == 0.0) {
-        rn2 = 0.0;
-    } else {
+    if (rhs2 > 0.0) {
         const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
         if (!(rn2 < thr)) {
-            // p = M^-1 r, absNew = r.p
-            double a1[1] = {0.0};
+            double a1[1] = {0.0}, t1[1];
             for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
                 int i = sl * 32 + lane;
                 if (i >= a.n) continue;
@@ -187,14 +250,10 @@ __global__ void __launch_bounds__(kBlock) k_cg64(Consts c, Ppe A, Krylov kv, Sol
                 kv.p[i] = p;
                 a1[0] = fma(r, p, a1[0]);
             }
-            block_partials<1>(a1, P + 1 * gridDim.x);
-            if (!grid_sync(bar, ds)) return;
-            double t1[1];
-            grid_totals<1>(P + 1 * gridDim.x, t1);
+            if (!reduce_sync<1>(kv, gb, a1, t1, ds)) return;
             double abs_new = t1[0];
             while (it < a.max_iter) {
-                // q = A p ; p.q
-                double a2[1] = {0.0};
+                double a2[1] = {0.0}, t2[1];
                 for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
                     int i = sl * 32 + lane;
                     if (i >= a.n) continue;
@@ -203,13 +262,9 @@ __global__ void __launch_bounds__(kBlock) k_cg64(Consts c, Ppe A, Krylov kv, Sol
                     kv.q[i] = q;
                     a2[0] = fma(pi, q, a2[0]);
                 }
-                block_partials<1>(a2, P + 2 * gridDim.x);
-                if (!grid_sync(bar, ds)) return;
-                double t2[1];
-                grid_totals<1>(P + 2 * gridDim.x, t2);
+                if (!reduce_sync<1>(kv, gb, a2, t2, ds)) return;
                 const double alpha = abs_new / t2[0];
-                // x += alpha p ; r -= alpha q ; z = M^-1 r ; ||r||^2, r.z
-                double a3[2] = {0.0, 0.0};
+                double a3[2] = {0.0, 0.0}, t3[2];
                 for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
                     int i = sl * 32 + lane;
                     if (i >= a.n) continue;
@@ -221,24 +276,22 @@ __global__ void __launch_bounds__(kBlock) k_cg64(Consts c, Ppe A, Krylov kv, Sol
                     a3[0] = fma(r, r, a3[0]);
                     a3[1] = fma(r, z, a3[1]);
                 }
-                block_partials<2>(a3, P + 3 * gridDim.x);
-                if (!grid_sync(bar, ds)) return;
-                double t3[2];
-                grid_totals<2>(P + 3 * gridDim.x, t3);
+                if (!reduce_sync<2>(kv, gb, a3, t3, ds)) return;
                 rn2 = t3[0];
                 if (rn2 < thr) break;
-                const double abs_old = abs_new;
+                const double beta = t3[1] / abs_new;
                 abs_new = t3[1];
-                const double beta = abs_new / abs_old;
                 for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
                     int i = sl * 32 + lane;
                     if (i >= a.n) continue;
                     kv.p[i] = fma(beta, kv.p[i], kv.z[i]);
                 }
                 it++;
-                if (!grid_sync(bar, ds)) return;
+                if (!grid_sync(gb, ds)) return;
             }
         }
+    } else {
+        rn2 = 0.0;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ds->cg_iterations = it;
@@ -248,7 +301,7 @@ __global__ void __launch_bounds__(kBlock) k_cg64(Consts c, Ppe A, Krylov kv, Sol
 }
 
 // --------------------------------------------------------------- mixed IR
-// Error-free FP32 product accumulated with compensation: (hi, lo) pairs.
+// Error-free FP32 product accumulated with compensation (hi, lo).
 struct F2 {
     float hi, lo;
 };
@@ -263,17 +316,16 @@ __device__ __forceinline__ void acc_prod(F2& a, float x, float y) {
 }
 __device__ __forceinline__ double f2d(const F2& a) { return (double)a.hi + (double)a.lo; }
 
-__global__ void __launch_bounds__(kBlock) k_cg_mixed(Consts c, Ppe A, Krylov kv, SolveArgs a,
-                                                     DevStats* ds) {
+__global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Krylov kv, SolveArgs a,
+                                                        DevStats* ds) {
+    GridBar gb{kv.barrier, 0u, 0};
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gsz = gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
-    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    unsigned int* bar = kv.barrier;
-    double* P = kv.partials;
-    const int G = gridDim.x;
+    const int gwarp = gtid >> 5;
+    const int nwarps = gsz >> 5;
 
-    // setup: x = 0, ||b||^2 (the FP32 matrix copy is made by k_to_fp32)
-    double acc[1] = {0.0};
+    double acc[1] = {0.0}, tot[1];
     for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
         int i = sl * 32 + lane;
         if (i >= a.n) continue;
@@ -281,18 +333,16 @@ __global__ void __launch_bounds__(kBlock) k_cg_mixed(Consts c, Ppe A, Krylov kv,
         double b = A.src[i];
         acc[0] = fma(b, b, acc[0]);
     }
-    block_partials<1>(acc, P);
-    if (!grid_sync(bar, ds)) return;
-    double tot[1];
-    grid_totals<1>(P, tot);
+    if (!reduce_sync<1>(kv, gb, acc, tot, ds)) return;
     const double rhs2 = tot[0];
+    const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
+    const float ithr = (float)(a.inner_tol * a.inner_tol);
     int64_t inner_total = 0;
     int refine = 0;
     double rn2 = rhs2;
-    const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
-    while (rhs2 > 0.0 && refine <= a.max_refine) {
-        // FP64 residual r = b - A x and its norm
-        double a0[1] = {0.0};
+    while (rhs2 > 0.0) {
+        // FP64 residual r = b - A x (x was made complete by the last barrier)
+        double a0[1] = {0.0}, t0[1];
         for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
             int i = sl * 32 + lane;
             if (i >= a.n) continue;
@@ -300,89 +350,73 @@ __global__ void __launch_bounds__(kBlock) k_cg_mixed(Consts c, Ppe A, Krylov kv,
             kv.r[i] = r;
             a0[0] = fma(r, r, a0[0]);
         }
-        block_partials<1>(a0, P + 1 * G);
-        if (!grid_sync(bar, ds)) return;
-        double t0[1];
-        grid_totals<1>(P + 1 * G, t0);
+        if (!reduce_sync<1>(kv, gb, a0, t0, ds)) return;
         rn2 = t0[0];
-        if (rn2 < thr || refine == a.max_refine || inner_total >= a.max_iter) break;
+        if (rn2 < thr || refine >= a.max_refine || inner_total >= a.max_iter) break;
         refine++;
-        // inner Jacobi-CG on the FP32 matrix for A d = r (scaled to unit norm)
+        // inner solve of A d = r / ||r|| (unit right-hand side)
         const float scale = (float)(1.0 / sqrt(rn2));
-        F2 s1 = {0.f, 0.f};
-        for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
-            int i = sl * 32 + lane;
-            if (i >= a.n) continue;
-            float r = (float)(kv.r[i]) * scale;
-            float p = kv.inv_diag32[i] * r;
+        for (int i = gtid; i < a.n; i += gsz) {
+            float r = (float)kv.r[i] * scale;
             kv.r32[i] = r;
-            kv.p32[i] = p;
             kv.x32[i] = 0.f;
-            acc_prod(s1, r, p);
+            kv.p32[i] = 0.f;
+            kv.s32[i] = 0.f;
+            kv.u32[i] = kv.inv_diag32[i] * r;
         }
-        double v1[1] = {f2d(s1)};
-        block_partials<1>(v1, P + 2 * G);
-        if (!grid_sync(bar, ds)) return;
-        double t1[1];
-        grid_totals<1>(P + 2 * G, t1);
-        double abs_new = t1[0];
-        const double r0n2 = 1.0;  // the scaled residual has unit norm
-        const double ithr = a.inner_tol * a.inner_tol * r0n2;
+        if (!grid_sync(gb, ds)) return;
+        float alpha = 0.f, beta = 0.f, gamma_old = 1.f;
         int64_t k = 0;
-        while (inner_total + k < a.max_iter) {
-            F2 s2 = {0.f, 0.f};
-            for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
-                int i = sl * 32 + lane;
-                if (i >= a.n) continue;
-                float pi = kv.p32[i];
-                float q = spmv32_row(A, a.K, sl, lane, i, kv.p32, pi, A.offcnt[i]);
-                kv.q32[i] = q;
-                acc_prod(s2, pi, q);
+        for (;;) {
+            // phase B: w = A u ; gamma = r.u, delta = w.u, rho = r.r
+            F2 g = {0.f, 0.f}, dl = {0.f, 0.f}, rr = {0.f, 0.f};
+            for (int i = gtid; i < a.n; i += gsz) {
+                const float ui = __ldcg(kv.u32 + i);
+                float w;
+                if (mf.enabled && !mf.sell_row[i])
+                    w = fmaf(A.diag32[i], ui, compact_row_sum(A, mf, a.K, i, kv.u32));
+                else
+                    w = fmaf(A.diag32[i], ui, spmv32_sell_row(A, a.K, i, kv.u32));
+                kv.w32[i] = w;
+                const float r = kv.r32[i];
+                acc_prod(g, r, ui);
+                acc_prod(dl, w, ui);
+                acc_prod(rr, r, r);
             }
-            double v2[1] = {f2d(s2)};
-            block_partials<1>(v2, P + 3 * G);
-            if (!grid_sync(bar, ds)) return;
-            double t2[1];
-            grid_totals<1>(P + 3 * G, t2);
-            const float alpha = (float)(abs_new / t2[0]);
-            F2 s3a = {0.f, 0.f}, s3b = {0.f, 0.f};
-            for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
-                int i = sl * 32 + lane;
-                if (i >= a.n) continue;
-                kv.x32[i] = fmaf(alpha, kv.p32[i], kv.x32[i]);
-                float r = fmaf(-alpha, kv.q32[i], kv.r32[i]);
+            double v3[3] = {f2d(g), f2d(dl), f2d(rr)}, t3[3];
+            if (!reduce_sync<3>(kv, gb, v3, t3, ds)) return;
+            if ((float)t3[2] < ithr || inner_total + k >= a.max_iter) break;
+            const float gamma = (float)t3[0], delta = (float)t3[1];
+            if (k == 0) {
+                beta = 0.f;
+                alpha = gamma / delta;
+            } else {
+                beta = gamma / gamma_old;
+                float den = delta - beta * gamma / alpha;
+                if (!(den > 0.f)) break;  // loss of positive definiteness in FP32
+                alpha = gamma / den;
+            }
+            gamma_old = gamma;
+            // phase A: p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; u = M^-1 r
+            for (int i = gtid; i < a.n; i += gsz) {
+                const float u = kv.u32[i];
+                const float p = fmaf(beta, kv.p32[i], u);
+                const float s = fmaf(beta, kv.s32[i], kv.w32[i]);
+                kv.p32[i] = p;
+                kv.s32[i] = s;
+                kv.x32[i] = fmaf(alpha, p, kv.x32[i]);
+                const float r = fmaf(-alpha, s, kv.r32[i]);
                 kv.r32[i] = r;
-                float z = kv.inv_diag32[i] * r;
-                kv.z32[i] = z;
-                acc_prod(s3a, r, r);
-                acc_prod(s3b, r, z);
+                kv.u32[i] = kv.inv_diag32[i] * r;
             }
-            double v3[2] = {f2d(s3a), f2d(s3b)};
-            block_partials<2>(v3, P + 4 * G);
-            if (!grid_sync(bar, ds)) return;
-            double t3[2];
-            grid_totals<2>(P + 4 * G, t3);
             k++;
-            if (t3[0] < ithr) break;
-            const double abs_old = abs_new;
-            abs_new = t3[1];
-            const float beta = (float)(abs_new / abs_old);
-            for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
-                int i = sl * 32 + lane;
-                if (i >= a.n) continue;
-                kv.p32[i] = fmaf(beta, kv.p32[i], kv.z32[i]);
-            }
-            if (!grid_sync(bar, ds)) return;
+            if (!grid_sync(gb, ds)) return;
         }
         inner_total += k;
         // x += d (FP64)
-        const double inv_scale = sqrt(rn2);
-        for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
-            int i = sl * 32 + lane;
-            if (i >= a.n) continue;
-            kv.x[i] = fma((double)kv.x32[i], inv_scale, kv.x[i]);
-        }
-        if (!grid_sync(bar, ds)) return;
+        const double back = sqrt(rn2);
+        for (int i = gtid; i < a.n; i += gsz) kv.x[i] = fma((double)kv.x32[i], back, kv.x[i]);
+        if (!grid_sync(gb, ds)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ds->cg_iterations = inner_total;
@@ -391,18 +425,44 @@ __global__ void __launch_bounds__(kBlock) k_cg_mixed(Consts c, Ppe A, Krylov kv,
     }
 }
 
-// FP32 copy of the FP64 matrix and of the inverse diagonal (before the solve).
-__global__ void k_to_fp32(Ppe A, Krylov kv, int n, int K) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ((n + 31) & ~31)) return;
-    int sl = i >> 5, lane = i & 31;
-    const int w = A.slice_w[sl];
-    const size_t base = (size_t)sl * K * 32 + lane;
+// Mixed-solver setup: FP32 values of the matrix, their compact index bytes,
+// FP32 diagonal and inverse diagonal.  A row whose column lies 64 or more
+// slots into its range keeps the int32 columns (sell_row = 1).
+__global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n) return;
+    const double d = A.diag[k];
+    A.diag32[k] = (float)d;
+    kv.inv_diag32[k] = d != 0.0 ? (float)(1.0 / d) : 1.f;
+    const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
+    const int w = A.slice_w[k >> 5];
+    int8_t sell = 1;
+    if (mf.enabled) {
+        sell = 0;
+        const int32_t key = mf.skey[k];
+        int st[3] = {0, 0, 0};
+        if (key < c.nkeys) {
+            const int ix = key / c.numY, iy = key - ix * c.numY;
+            for (int r = 0; r < 3; r++) st[r] = mf.cs[(ix - 1 + r) * c.numY + iy - 1];
+        }
+        const int cnt = A.offcnt[k];
+        for (int m = 0; m < w; m++) {
+            uint8_t b = 0;  // padding: range 0, offset 0, value 0
+            if (m < cnt) {
+                const int j = A.col[base + (size_t)m * 32];
+                int r = 2;
+                while (r > 0 && j < st[r]) r--;
+                const int off = j - st[r];
+                if (off >= 0 && off < 64)
+                    b = (uint8_t)((r << 6) | off);
+                else
+                    sell = 1;
+            }
+            mf.idx8[base + (size_t)m * 32] = b;
+        }
+    }
+    mf.sell_row[k] = sell;
     for (int m = 0; m < w; m++) A.val32[base + (size_t)m * 32] = (float)A.val[base + (size_t)m * 32];
-    if (i >= n) return;
-    double d = A.diag[i];
-    A.diag32[i] = (float)d;
-    kv.inv_diag32[i] = d != 0.0 ? (float)(1.0 / d) : 1.f;
 }
 
 int coop_grid(const void* fn, int device) {
@@ -410,8 +470,20 @@ int coop_grid(const void* fn, int device) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kBlock, 0);
     if (per < 1) per = 1;
-    if (per > 4) per = 4;
+    if (per > 1) per = 1;
     return sms * per;
+}
+
+SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
+    SolveArgs a;
+    a.n = c.n;
+    a.nslices = (c.n + 31) / 32;
+    a.K = c.K;
+    a.tol = tol;
+    a.max_iter = max_iter;
+    a.inner_tol = 1e-5;
+    a.max_refine = 40;
+    return a;
 }
 
 }  // namespace
@@ -423,40 +495,34 @@ void solver_setup(Krylov& k, int32_t /*n_pad*/, int device) {
     k.block = kBlock;
 }
 
-static SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
-    SolveArgs a;
-    a.n = c.n;
-    a.nslices = (c.n + 31) / 32;
-    a.K = c.K;
-    a.tol = tol;
-    a.max_iter = max_iter;
-    a.inner_tol = 1e-4;
-    a.max_refine = 30;
-    return a;
+void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, MatFree& mf,
+                        const Krylov& k, cudaStream_t st) {
+    mf.skey = sc.skey;
+    mf.cs = sc.cell_start;
+    mf.numY = c.numY;
+    k_mixed_setup<<<(c.n + 255) / 256, 256, 0, st>>>(c, A, mf, k);
+    ++g_launches;
 }
 
 void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double tol,
                        int64_t max_iter, DevStats* ds, cudaStream_t st) {
     SolveArgs a = make_args(c, tol, max_iter);
-    Consts cc = c;
     Ppe AA = A;
     Krylov kk = k;
-    void* args[] = {&cc, &AA, &kk, &a, &ds};
-    cudaMemsetAsync(k.barrier, 0, 2 * sizeof(unsigned int), st);
+    void* args[] = {&AA, &kk, &a, &ds};
+    cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
     cudaLaunchCooperativeKernel((const void*)k_cg64, dim3(k.grid), dim3(kBlock), args, 0, st);
     ++g_launches;
 }
 
-void launch_solve_mixed(const Consts& c, const Ppe& A, const Krylov& k, double tol,
-                        int64_t max_iter, DevStats* ds, cudaStream_t st) {
+void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const Krylov& k,
+                        double tol, int64_t max_iter, DevStats* ds, cudaStream_t st) {
     SolveArgs a = make_args(c, tol, max_iter);
-    Consts cc = c;
     Ppe AA = A;
+    MatFree mm = mf;
     Krylov kk = k;
-    void* args[] = {&cc, &AA, &kk, &a, &ds};
-    k_to_fp32<<<(c.n + 31 + 255) / 256, 256, 0, st>>>(A, k, c.n, c.K);
-    ++g_launches;
-    cudaMemsetAsync(k.barrier, 0, 2 * sizeof(unsigned int), st);
+    void* args[] = {&AA, &mm, &kk, &a, &ds};
+    cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
     cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kBlock), args, 0, st);
     ++g_launches;
 }

@@ -22,11 +22,21 @@ constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
 __global__ void k_keys(Consts c, StateBuf s, int32_t* __restrict__ key, int32_t* __restrict__ rank,
-                       int32_t* __restrict__ count) {
+                       int32_t* __restrict__ count, DevStats* ds) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.n) return;
     int32_t kk = c.nkeys;
-    if (s.type[k] != T_GHOST) kk = cell_key(c, s.x[k], s.y[k], c.planar ? 0.0 : s.z[k]);
+    if (s.type[k] != T_GHOST) {
+        const double x = s.x[k], y = s.y[k], z = c.planar ? 0.0 : s.z[k];
+        if (isfinite(x) && isfinite(y) && isfinite(z)) {
+            kk = cell_key(c, x, y, z);
+        } else {
+            // the reference has no defined behaviour here; the particle is
+            // taken out of the neighbour search and the step reports an error
+            s.type[k] = T_GHOST;
+            atomicOr(&ds->status, ST_NONFINITE);
+        }
+    }
     key[k] = kk;
     rank[k] = atomicAdd(count + kk, 1);
 }
@@ -196,11 +206,11 @@ void launch_exclusive_scan(const int32_t* in, int32_t* out, int32_t n, int32_t* 
 }
 
 void launch_rebuild(const Consts& c, const StateBuf& in, const StateBuf& out, SortScratch& s,
-                    cudaStream_t st) {
+                    DevStats* ds, cudaStream_t st) {
     const int T = 256;
     int nb = (c.n + T - 1) / T;
     cudaMemsetAsync(s.cell_count, 0, sizeof(int32_t) * (c.nkeys + 1), st);
-    k_keys<<<nb, T, 0, st>>>(c, in, s.key, s.rank, s.cell_count);
+    k_keys<<<nb, T, 0, st>>>(c, in, s.key, s.rank, s.cell_count, ds);
     ++g_launches;
     launch_exclusive_scan(s.cell_count, s.cell_start, c.nkeys + 1, s.scan_tmp, st);
     k_scatter<<<nb, T, 0, st>>>(c.n, s.key, s.rank, s.cell_start, s.perm);

@@ -358,6 +358,15 @@ __global__ void __launch_bounds__(kThreads) k_assemble(Consts c, StateBuf s, NbL
     }
     int w = __reduce_max_sync(0xffffffffu, off);
     unsigned tot = __reduce_add_sync(0xffffffffu, (unsigned)off);
+    // pad the row to the slice width with (own slot, 0) so that SpMV loops
+    // need no per-entry predicate
+    if (k < c.n) {
+        const size_t sbase = (size_t)(k >> 5) * c.K * 32 + (k & 31);
+        for (int m = off; m < w; m++) {
+            A.col[sbase + (size_t)m * 32] = k;
+            A.val[sbase + (size_t)m * 32] = 0.0;
+        }
+    }
     if ((threadIdx.x & 31) == 0 && (k >> 5) < (c.n + 31) / 32) {
         A.slice_w[k >> 5] = w;
         if (tot) atomicAdd(&ds->nnz_off, (unsigned long long)tot);
@@ -438,10 +447,12 @@ __global__ void k_cc_apply(Consts c, StateBuf s, const int* __restrict__ par,
 
 // ---------------------------------------------------------------------------
 // solvePoissonEquation's scatter + removeNegativePressure (src/mps.cpp:466-479)
-__global__ void k_pressure_out(int n, const double* __restrict__ x, double* __restrict__ p) {
+__global__ void k_pressure_out(int n, const double* __restrict__ x, double* __restrict__ p,
+                               DevStats* ds) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     double v = x[k];
+    if (!isfinite(v)) atomicOr(&ds->status, ST_NONFINITE);
     p[k] = v < 0.0 ? 0.0 : v;
 }
 
@@ -658,7 +669,7 @@ void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb, 
                           double* ax, double* ay, double* az, int mixed, DevStats* ds,
                           cudaStream_t st) {
     int g = blocks_for(c.n);
-    k_pressure_out<<<g, kThreads, 0, st>>>(c.n, x, s.p);
+    k_pressure_out<<<g, kThreads, 0, st>>>(c.n, x, s.p, ds);
     ++g_launches;
     k_min_pressure<<<g, kThreads, 0, st>>>(c, s, nb);
     ++g_launches;

@@ -14,7 +14,8 @@ import numpy as np
 
 from . import build as _build
 
-MPS_OK, MPS_ERR_ARG, MPS_ERR_CUDA, MPS_ERR_CAPACITY, MPS_ERR_TIMEOUT, MPS_ERR_NO_DEVICE = range(6)
+(MPS_OK, MPS_ERR_ARG, MPS_ERR_CUDA, MPS_ERR_CAPACITY, MPS_ERR_TIMEOUT, MPS_ERR_NO_DEVICE,
+ MPS_ERR_NONFINITE) = range(7)
 FP64, MIXED = 0, 1
 
 

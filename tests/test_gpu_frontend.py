@@ -24,7 +24,7 @@ def test_cli_simulation_matches_oracle(tmp_path):
     exe = build.build_host()
     prm, pos, vel, t = scenes.dam_break(0.02, tank=(0.6, 0.4), column=(0.2, 0.3), dt=2e-3)
     scenes.write_csv(tmp_path / "input.csv", pos, vel, t)
-    text = yaml_text(prm, "input.csv").replace("finish time: 1.0", "finish time: 0.02") \
+    text = yaml_text(prm, "input.csv").replace("finish time: 1.0", "finish time: 0.0201") \
                                       .replace("output interval: 1.0", "output interval: 0.01")
     (tmp_path / "settings.yml").write_text(text)
     out = subprocess.run([exe, "-s", "settings.yml"], cwd=tmp_path, capture_output=True, text=True,
