@@ -135,6 +135,24 @@ int mps_collisions(mps_engine* e, int32_t* pi, int32_t* pj, double* dist, int32_
 
 const char* mps_last_error(void);
 
+/* No counterpart in the reference.  The initial number density ratio pass of
+ * loadInitialState (neighbour search + ratio, the values mps_create computes)
+ * for callers that cannot allocate device memory: a host application that
+ * owns all device memory itself and forbids library allocations, or a
+ * timing-critical loop that cannot take an allocation's implicit
+ * synchronisation.  It allocates nothing: d_pos (n*3 doubles), d_type (n
+ * ints) and d_ndr (n doubles, output) are device pointers the caller owns,
+ * and the scratch is a fixed ~5 MB static device array inside this library
+ * (held on every GPU that loads it until the process exits).  Limits: at most
+ * 65,536 particles and 262,144 bucket cells; larger requests return
+ * MPS_ERR_ARG.  The first call on a device looks up the scratch address
+ * (make it before any stream capture).  Calls share the scratch, so calls
+ * whose GPU work overlaps race: issue them on one stream.  Work is enqueued
+ * on `stream` (a cudaStream_t; NULL = the legacy default stream) and the
+ * call returns without waiting. */
+int mps_number_density_static(const mps_params* prm, int32_t n, const double* d_pos,
+                              const int32_t* d_type, double* d_ndr, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

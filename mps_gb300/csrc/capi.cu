@@ -666,3 +666,8 @@ int mps_collisions(mps_engine* e, int32_t* pi, int32_t* pj, double* dist, int32_
 }
 
 }  // extern "C"
+
+namespace mpsg {
+// Lets the other translation units of the library report through mps_last_error().
+__attribute__((visibility("hidden"))) void set_last_error(const std::string& m) { g_last_error = m; }
+}  // namespace mpsg
