@@ -101,6 +101,12 @@ int mps_destroy(mps_engine* e);
  * keep the defaults. */
 int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_iter);
 
+/* The MIXED solver's preconditioner on planar scenes: an aggregation
+ * multigrid V(1,1) cycle (default on; omega = damped-Jacobi weight in (0,1),
+ * scale = coarse-correction weight in [1,2)), or plain Jacobi when disabled.
+ * No counterpart in the reference (its CG is Jacobi-preconditioned). */
+int mps_set_multigrid(mps_engine* e, int32_t enabled, float omega, float scale);
+
 /* MPS::stepForward (src/mps.cpp:111-130). */
 int mps_step(mps_engine* e, int32_t is_time_to_export, mps_step_stats* stats);
 

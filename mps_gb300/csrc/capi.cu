@@ -117,6 +117,8 @@ struct mps_engine {
     Ppe A{};
     Krylov kv{};
     MatFree mf{};
+    Mg mg{};
+    int32_t mg_requested = 1;
     int32_t *cand_cnt = nullptr, *cand_base = nullptr;
     CollPair* pairs = nullptr;
     int32_t pair_cap = 0;
@@ -209,7 +211,10 @@ void enqueue_step(mps_engine* e, bool do_export) {
     int64_t mi = e->max_iter > 0 ? e->max_iter : 2 * (int64_t)c.n;
     if (mixed) {
         launch_mixed_setup(c, e->sc, e->A, e->mf, e->kv, st);
-        launch_solve_mixed(c, e->A, e->mf, e->kv, e->tol, mi, e->ds, st);
+        Mg g = e->mg;
+        g.enabled = e->mg.enabled && e->mg_requested;
+        launch_mg_setup(c, e->A, e->mf, g, st);
+        launch_solve_mixed(c, e->A, e->mf, g, e->kv, e->tol, mi, e->ds, st);
     } else
         launch_solve_fp64(c, e->A, e->kv, e->tol, mi, e->ds, st);
     cudaEventRecord(e->ev[3], st);
@@ -391,6 +396,34 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     e->pair_cap = (int32_t)std::min<size_t>(4 * np + 1024, (size_t)1 << 30);
     if (e->alloc(&e->pairs, e->pair_cap)) return bail(fail(MPS_ERR_CUDA, "cudaMalloc pairs"));
     solver_setup(e->kv, e->n_pad, dev);
+    // multigrid hierarchy (planar scenes): level 1 = the numX x numY cell grid
+    if (c.planar) {
+        Mg& g = e->mg;
+        g.enabled = 1;
+        g.omega = 0.9f;
+        g.scale = 1.5f;
+        int nx = c.numX, ny = c.numY, l = 1;
+        for (;;) {
+            g.lev[l].nx = nx;
+            g.lev[l].ny = ny;
+            size_t cells = (size_t)nx * ny;
+            if (e->alloc(&g.lev[l].st, 9 * cells) || e->alloc(&g.lev[l].invd, cells) ||
+                e->alloc(&g.lev[l].r, cells) || e->alloc(&g.lev[l].e, cells) ||
+                e->alloc(&g.lev[l].t, cells))
+                return bail(fail(MPS_ERR_CUDA, "cudaMalloc multigrid level"));
+            if (cells <= (size_t)kMgMaxCoarsest || l == kMgMaxLevels - 1) break;
+            nx = (nx + 1) / 2;
+            ny = (ny + 1) / 2;
+            l++;
+        }
+        g.nlev = l;
+        if ((size_t)g.lev[l].nx * g.lev[l].ny > (size_t)kMgMaxCoarsest) g.enabled = 0;
+        g.ngrid = 0;
+        while (g.ngrid + 1 < g.nlev && (size_t)g.lev[g.ngrid + 1].nx * g.lev[g.ngrid + 1].ny > 4096) g.ngrid++;
+        if (e->alloc(&g.e0, np) || e->alloc(&g.res0, np) ||
+            e->alloc(&g.dense, (size_t)kMgMaxCoarsest * kMgMaxCoarsest))
+            return bail(fail(MPS_ERR_CUDA, "cudaMalloc multigrid"));
+    }
     if (e->alloc(&e->kv.partials, (size_t)e->kv.grid * 16))
         return bail(fail(MPS_ERR_CUDA, "cudaMalloc partials"));
     if (cudaMallocHost(&e->hs, sizeof(DevStats)) != cudaSuccess)
@@ -456,6 +489,18 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
     e->tol = tol > 0 ? tol
                      : (precision == MPS_PRECISION_FP64 ? std::numeric_limits<double>::epsilon() : 1e-10);
     e->max_iter = max_iter > 0 ? max_iter : 0;
+    return MPS_OK;
+}
+
+int mps_set_multigrid(mps_engine* e, int32_t enabled, float omega, float scale) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    if (enabled && !e->mg.enabled)
+        return fail(MPS_ERR_ARG, "multigrid needs a planar scene (2-D, constant z)");
+    if (!(omega > 0.f && omega < 1.f) || !(scale >= 1.f && scale < 2.f))
+        return fail(MPS_ERR_ARG, "multigrid weights out of range (0 < omega < 1, 1 <= scale < 2)");
+    e->mg_requested = enabled ? 1 : 0;
+    e->mg.omega = omega;
+    e->mg.scale = scale;
     return MPS_OK;
 }
 

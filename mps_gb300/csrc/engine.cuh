@@ -157,6 +157,35 @@ void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb,
 void launch_number_density(const Consts& c, const StateBuf& s, const NbList& nb,
                            cudaStream_t st);
 
+// Aggregation multigrid preconditioner of the mixed solver (planar scenes).
+// Level 1 aggregates the particles of each bucket cell (the slots of a cell
+// are contiguous), so it is the structured numX x numY cell grid with a
+// 9-point stencil (a particle's neighbours lie in the 3x3 cells around it);
+// each further level aggregates 2x2 cells and is again a 9-point grid.
+// Coarse operators are Galerkin products with piecewise-constant transfer,
+// built in a fixed order (deterministic); the coarsest level (<= 96
+// unknowns) is solved with its dense inverse.
+constexpr int kMgMaxLevels = 16;
+constexpr int kMgMaxCoarsest = 96;
+struct MgLevel {
+    int32_t nx, ny;
+    float* st;    // 9 x (nx*ny), direction d = (dx+1)*3 + (dy+1), d = 4 is the diagonal
+    float* invd;  // 1 / diagonal, 0 for cells without unknowns
+    float *r, *e, *t;
+};
+struct Mg {
+    int32_t enabled;
+    int32_t nlev;   // coarse levels 1..nlev
+    int32_t ngrid;  // levels 1..ngrid run grid-wide; ngrid+1..nlev run in block 0
+    MgLevel lev[kMgMaxLevels];
+    float* e0;      // level-0 correction (per slot)
+    float* res0;    // level-0 residual (per slot)
+    float* dense;   // inverse of the coarsest operator (nc x nc)
+    int32_t nc;
+    float omega;    // damped-Jacobi weight
+    float scale;    // coarse-correction scale
+};
+
 // --------------------------------------------------------------- solver.cu
 struct Krylov {
     double *x, *r, *p, *q, *z, *inv_diag;
@@ -171,8 +200,12 @@ void solver_setup(Krylov& k, int32_t n_pad, int device);
 // Solves A x = b; returns through DevStats (iterations, residual, status).
 void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double tol,
                        int64_t max_iter, DevStats* ds, cudaStream_t st);
-void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const Krylov& k,
-                        double tol, int64_t max_iter, DevStats* ds, cudaStream_t st);
+void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
+                        const Krylov& k, double tol, int64_t max_iter, DevStats* ds,
+                        cudaStream_t st);
+// Per-solve multigrid setup (after launch_mixed_setup).
+void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
+                     cudaStream_t st);
 // FP32 copy of the assembled matrix in the compact layout of MatFree.
 void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, MatFree& mf,
                         const Krylov& k, cudaStream_t st);

@@ -1,0 +1,151 @@
+// Setup of the aggregation multigrid preconditioner used by the mixed
+// pressure solver (the V-cycle itself runs inside k_cg_mixed, solver.cu).
+//
+// Level 1: one unknown per bucket cell (numX x numY, cell index
+// cx * numY + cy, the planar cell key).  Its operator is the Galerkin
+// product P^T A P of the FP32 particle matrix with piecewise-constant P over
+// the Inner particles of each cell; since a particle couples only to the
+// 3x3 cells around its own, the result is a 9-point stencil.  Level l+1
+// aggregates 2x2 cells of level l, again a 9-point stencil.  Every coarse
+// entry is summed by one thread in a fixed order, so the hierarchy is
+// deterministic.  The coarsest level gets an explicit inverse (Gauss-Jordan
+// without pivoting: the Galerkin operator of an SPD matrix is SPD).
+#include "devutil.cuh"
+#include "engine.cuh"
+
+namespace mpsg {
+
+namespace {
+
+__global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= L.nx * L.ny) return;
+    const int cx = I / L.ny, cy = I - cx * L.ny;
+    float st[9];
+#pragma unroll
+    for (int d = 0; d < 9; d++) st[d] = 0.f;
+    const int b = mf.cs[I], e = mf.cs[I + 1];
+    int rs[3][4];
+    if (e > b) {
+        for (int r = 0; r < 3; r++) {
+            const int kk = (cx - 1 + r) * c.numY + cy - 1;
+            for (int q = 0; q < 4; q++) rs[r][q] = mf.cs[kk + q];
+        }
+    }
+    for (int k = b; k < e; k++) {
+        const float dg = A.diag32[k];
+        if (!(dg > 0.f)) continue;  // not an unknown (not Inner)
+        st[4] += dg;
+        const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
+        const int cnt = A.offcnt[k];
+        const bool compact = mf.enabled && !mf.sell_row[k];
+        for (int m = 0; m < cnt; m++) {
+            const float v = A.val32[base + (size_t)m * 32];
+            int dx, dy;
+            if (compact) {
+                const int bt = mf.idx8[base + (size_t)m * 32];
+                const int r = bt >> 6;
+                const int j = rs[r][0] + (bt & 63);
+                dx = r - 1;
+                dy = (j >= rs[r][1]) + (j >= rs[r][2]) - 1;
+            } else {
+                const int j = A.col[base + (size_t)m * 32];
+                const int kj = mf.skey[j];
+                const int jx = kj / c.numY, jy = kj - jx * c.numY;
+                dx = jx - cx;
+                dy = jy - cy;
+            }
+            st[(dx + 1) * 3 + (dy + 1)] += v;
+        }
+    }
+    const int n = L.nx * L.ny;
+#pragma unroll
+    for (int d = 0; d < 9; d++) L.st[(size_t)d * n + I] = st[d];
+    L.invd[I] = st[4] > 0.f ? 1.f / st[4] : 0.f;
+}
+
+__global__ void k_mg_coarsen(MgLevel F, MgLevel C) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nc = C.nx * C.ny;
+    if (I >= nc) return;
+    const int X = I / C.ny, Y = I - X * C.ny;
+    const int nf = F.nx * F.ny;
+    float st[9];
+#pragma unroll
+    for (int d = 0; d < 9; d++) st[d] = 0.f;
+    for (int a = 0; a < 2; a++)
+        for (int bb = 0; bb < 2; bb++) {
+            const int x = 2 * X + a, y = 2 * Y + bb;
+            if (x >= F.nx || y >= F.ny) continue;
+            const int cf = x * F.ny + y;
+            for (int d = 0; d < 9; d++) {
+                const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
+                if (nx < 0 || ny < 0 || nx >= F.nx || ny >= F.ny) continue;
+                const int DX = nx / 2 - X, DY = ny / 2 - Y;
+                st[(DX + 1) * 3 + (DY + 1)] += F.st[(size_t)d * nf + cf];
+            }
+        }
+#pragma unroll
+    for (int d = 0; d < 9; d++) C.st[(size_t)d * nc + I] = st[d];
+    C.invd[I] = st[4] > 0.f ? 1.f / st[4] : 0.f;
+}
+
+// Dense inverse of the coarsest operator; cells without unknowns get an
+// identity row so that the matrix stays invertible (their residual is 0).
+__global__ void k_mg_dense(MgLevel L, float* out) {
+    __shared__ float M[kMgMaxCoarsest][kMgMaxCoarsest];
+    const int n = L.nx * L.ny;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int i = t / n, j = t % n;
+        float v = 0.f;
+        const bool act = L.invd[i] > 0.f;
+        if (!act) {
+            v = (i == j) ? 1.f : 0.f;
+        } else if (L.invd[j] > 0.f) {
+            const int xi = i / L.ny, yi = i % L.ny, xj = j / L.ny, yj = j % L.ny;
+            const int dx = xj - xi, dy = yj - yi;
+            if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) v = L.st[(size_t)((dx + 1) * 3 + (dy + 1)) * n + i];
+        }
+        M[i][j] = v;
+    }
+    __shared__ float fcol[kMgMaxCoarsest];
+    __syncthreads();
+    for (int k = 0; k < n; k++) {
+        const float piv = 1.f / M[k][k];
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) M[k][j] = (j == k ? 1.f : M[k][j]) * piv;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) fcol[i] = M[i][k];
+        __syncthreads();
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            const int i = t / n, j = t % n;
+            if (i == k) continue;
+            const float f = fcol[i];
+            if (j == k)
+                M[i][j] = -f * M[k][k];
+            else
+                M[i][j] -= f * M[k][j];
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) out[t] = M[t / n][t % n];
+}
+
+}  // namespace
+
+void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
+                     cudaStream_t st) {
+    if (!mg.enabled) return;
+    const int T = 256;
+    const MgLevel& L1 = mg.lev[1];
+    k_mg_level1<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(c, A, mf, L1);
+    ++g_launches;
+    for (int l = 1; l < mg.nlev; l++) {
+        const MgLevel& C = mg.lev[l + 1];
+        k_mg_coarsen<<<(C.nx * C.ny + T - 1) / T, T, 0, st>>>(mg.lev[l], C);
+        ++g_launches;
+    }
+    k_mg_dense<<<1, 1024, 0, st>>>(mg.lev[mg.nlev], mg.dense);
+    ++g_launches;
+}
+
+}  // namespace mpsg

@@ -316,8 +316,181 @@ __device__ __forceinline__ void acc_prod(F2& a, float x, float y) {
 }
 __device__ __forceinline__ double f2d(const F2& a) { return (double)a.hi + (double)a.lo; }
 
-__global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Krylov kv, SolveArgs a,
-                                                        DevStats* ds) {
+// Level-0 operator row (FP32): diag_i v_i + off-diagonal sum.
+__device__ __forceinline__ float a0_row(const Ppe& A, const MatFree& mf, int K, int i,
+                                        const float* __restrict__ v) {
+    const float off = (mf.enabled && !mf.sell_row[i]) ? compact_row_sum(A, mf, K, i, v)
+                                                      : spmv32_sell_row(A, K, i, v);
+    return fmaf(A.diag32[i], __ldcg(v + i), off);
+}
+
+// 9-point stencil row of a structured level.
+__device__ __forceinline__ float stencil_row(const MgLevel& L, int I, const float* __restrict__ v) {
+    const int n = L.nx * L.ny;
+    const int x = I / L.ny, y = I - x * L.ny;
+    float acc = 0.f;
+#pragma unroll
+    for (int d = 0; d < 9; d++) {
+        const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
+        if (nx < 0 || ny < 0 || nx >= L.nx || ny >= L.ny) continue;
+        acc = fmaf(__ldcg(L.st + (size_t)d * n + I), __ldcg(v + nx * L.ny + ny), acc);
+    }
+    return acc;
+}
+
+// residual of level l restricted to level l+1 (sum over the 2x2 children)
+__device__ __forceinline__ float restrict_cell(const MgLevel& F, int X, int Y) {
+    float acc = 0.f;
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++) {
+            const int x = 2 * X + a, y = 2 * Y + b;
+            if (x >= F.nx || y >= F.ny) continue;
+            const int c = x * F.ny + y;
+            if (__ldcg(F.invd + c) > 0.f) acc += __ldcg(F.r + c) - stencil_row(F, c, F.e);
+        }
+    return acc;
+}
+
+// Levels lo..hi of the V-cycle run by block 0 alone (they are small): down
+// smoothing + restriction, the dense coarsest solve, prolongation + up
+// smoothing.  Only __syncthreads inside; the caller brackets it with grid
+// barriers.
+__device__ void mg_block_cycle(Mg& mg, int lo) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int l = lo; l < mg.nlev; l++) {
+        MgLevel& L = mg.lev[l];
+        const int n = L.nx * L.ny;
+        for (int I = tid; I < n; I += nt) L.e[I] = mg.omega * L.invd[I] * __ldcg(L.r + I);
+        __syncthreads();
+        MgLevel& C = mg.lev[l + 1];
+        for (int I = tid; I < C.nx * C.ny; I += nt) {
+            const int X = I / C.ny, Y = I - X * C.ny;
+            C.r[I] = restrict_cell(L, X, Y);
+        }
+        __syncthreads();
+    }
+    {
+        MgLevel& L = mg.lev[mg.nlev];
+        const int n = L.nx * L.ny;
+        for (int i = tid; i < n; i += nt) {
+            float acc = 0.f;
+            for (int j = 0; j < n; j++) acc = fmaf(__ldcg(mg.dense + i * n + j), __ldcg(L.r + j), acc);
+            L.e[i] = L.invd[i] > 0.f ? acc : 0.f;
+        }
+        __syncthreads();
+    }
+    for (int l = mg.nlev - 1; l >= lo; l--) {
+        MgLevel& L = mg.lev[l];
+        MgLevel& C = mg.lev[l + 1];
+        const int n = L.nx * L.ny;
+        for (int I = tid; I < n; I += nt) {
+            if (!(L.invd[I] > 0.f)) continue;
+            const int x = I / L.ny, y = I - x * L.ny;
+            L.e[I] = fmaf(mg.scale, __ldcg(C.e + (x / 2) * C.ny + y / 2), __ldcg(L.e + I));
+        }
+        __syncthreads();
+        for (int I = tid; I < n; I += nt) {
+            const float iv = L.invd[I];
+            L.t[I] = iv > 0.f ? fmaf(mg.omega * iv, __ldcg(L.r + I) - stencil_row(L, I, L.e), __ldcg(L.e + I)) : 0.f;
+        }
+        __syncthreads();
+        // copy back (no pointer swap: the other blocks keep the same pointers)
+        for (int I = tid; I < n; I += nt) L.e[I] = __ldcg(L.t + I);
+        __syncthreads();
+    }
+}
+
+// Post-smoothing of a grid level with the prolongation folded in: the
+// corrected value of a cell is e + s * e_parent, computed on the fly for the
+// cell and its 8 neighbours, so prolongation needs no barrier of its own.
+__device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, const MgLevel& C,
+                                                int I) {
+    const int n = L.nx * L.ny;
+    const int x = I / L.ny, y = I - x * L.ny;
+    const float ei = fmaf(mg.scale, __ldcg(C.e + (x / 2) * C.ny + y / 2), __ldcg(L.e + I));
+    float acc = 0.f;
+#pragma unroll
+    for (int d = 0; d < 9; d++) {
+        const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
+        if (nx < 0 || ny < 0 || nx >= L.nx || ny >= L.ny) continue;
+        const float ej = fmaf(mg.scale, __ldcg(C.e + (nx / 2) * C.ny + ny / 2), __ldcg(L.e + nx * L.ny + ny));
+        acc = fmaf(__ldcg(L.st + (size_t)d * n + I), ej, acc);
+    }
+    return fmaf(mg.omega * __ldcg(L.invd + I), __ldcg(L.r + I) - acc, ei);
+}
+
+// u = M r: one symmetric V(1,1) cycle with damped Jacobi smoothing.  The
+// caller has already written e0 = omega D^-1 r (level-0 pre-smoothing, local)
+// and passed a grid barrier.  Restriction is fused with the next level's
+// pre-smoothing, prolongation with the post-smoothing.  Ends after writing u
+// (no trailing barrier).  Every block runs the same barrier sequence.
+__device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& mf, int K,
+                                          const float* __restrict__ r, float* __restrict__ u,
+                                          int n, GridBar& gb, DevStats* ds) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gsz = gridDim.x * blockDim.x;
+    // level 0 residual of the Inner particles (coalesced, one row per thread)
+    for (int i = gtid; i < n; i += gsz)
+        mg.res0[i] = A.diag32[i] > 0.f ? __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0) : 0.f;
+    if (!grid_sync(gb, ds)) return false;
+    // level 1: sum over each cell's contiguous slots; pre-smooth
+    {
+        MgLevel& L1 = mg.lev[1];
+        const int n1 = L1.nx * L1.ny;
+        for (int I = gtid; I < n1; I += gsz) {
+            const int b = __ldg(mf.cs + I), e = __ldg(mf.cs + I + 1);
+            float acc = 0.f;
+            for (int i = b; i < e; i++) acc += __ldcg(mg.res0 + i);
+            L1.r[I] = acc;
+            L1.e[I] = mg.omega * __ldg(L1.invd + I) * acc;
+        }
+    }
+    if (!grid_sync(gb, ds)) return false;
+    // grid-wide levels, down: restrict level l into l+1 and pre-smooth there
+    for (int l = 1; l <= mg.ngrid; l++) {
+        MgLevel& L = mg.lev[l];
+        MgLevel& C = mg.lev[l + 1];
+        const bool smooth = l + 1 <= mg.ngrid;
+        for (int I = gtid; I < C.nx * C.ny; I += gsz) {
+            const int X = I / C.ny, Y = I - X * C.ny;
+            const float rr = restrict_cell(L, X, Y);
+            C.r[I] = rr;
+            if (smooth) C.e[I] = mg.omega * __ldg(C.invd + I) * rr;
+        }
+        if (!grid_sync(gb, ds)) return false;
+    }
+    // small levels in block 0
+    if (blockIdx.x == 0) mg_block_cycle(mg, mg.ngrid + 1);
+    if (!grid_sync(gb, ds)) return false;
+    // grid-wide levels, up: prolongation folded into the post-smoothing
+    for (int l = mg.ngrid; l >= 1; l--) {
+        MgLevel& L = mg.lev[l];
+        MgLevel& C = mg.lev[l + 1];
+        const int nl = L.nx * L.ny;
+        for (int I = gtid; I < nl; I += gsz) L.t[I] = __ldg(L.invd + I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
+        if (!grid_sync(gb, ds)) return false;
+        float* tmp = L.e;
+        L.e = L.t;
+        L.t = tmp;
+    }
+    // level 1 -> 0: prolongate to the Inner particles, then post-smooth
+    {
+        MgLevel& L1 = mg.lev[1];
+        for (int i = gtid; i < n; i += gsz)
+            if (A.diag32[i] > 0.f)
+                mg.e0[i] = fmaf(mg.scale, __ldcg(L1.e + __ldg(mf.skey + i)), __ldcg(mg.e0 + i));
+    }
+    if (!grid_sync(gb, ds)) return false;
+    for (int i = gtid; i < n; i += gsz) {
+        const float dg = A.diag32[i];
+        u[i] = dg > 0.f ? fmaf(mg.omega / dg, __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0), __ldcg(mg.e0 + i))
+                        : 0.f;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg, Krylov kv,
+                                                        SolveArgs a, DevStats* ds) {
     GridBar gb{kv.barrier, 0u, 0};
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsz = gridDim.x * blockDim.x;
@@ -336,7 +509,6 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Krylo
     if (!reduce_sync<1>(kv, gb, acc, tot, ds)) return;
     const double rhs2 = tot[0];
     const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
-    const float ithr = (float)(a.inner_tol * a.inner_tol);
     int64_t inner_total = 0;
     int refine = 0;
     double rn2 = rhs2;
@@ -354,7 +526,10 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Krylo
         rn2 = t0[0];
         if (rn2 < thr || refine >= a.max_refine || inner_total >= a.max_iter) break;
         refine++;
-        // inner solve of A d = r / ||r|| (unit right-hand side)
+        // inner solve of A d = r / ||r|| (unit right-hand side), to the
+        // reduction this refinement still needs (with a 2x margin), but no
+        // tighter than FP32 iterations can resolve
+        const float ithr = (float)fmax(a.inner_tol * a.inner_tol, 0.25 * thr / rn2);
         const float scale = (float)(1.0 / sqrt(rn2));
         for (int i = gtid; i < a.n; i += gsz) {
             float r = (float)kv.r[i] * scale;
@@ -362,9 +537,16 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Krylo
             kv.x32[i] = 0.f;
             kv.p32[i] = 0.f;
             kv.s32[i] = 0.f;
-            kv.u32[i] = kv.inv_diag32[i] * r;
+            if (mg.enabled)
+                mg.e0[i] = mg.omega * kv.inv_diag32[i] * r;
+            else
+                kv.u32[i] = kv.inv_diag32[i] * r;
         }
         if (!grid_sync(gb, ds)) return;
+        if (mg.enabled) {
+            if (!mg_vcycle(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds)) return;
+            if (!grid_sync(gb, ds)) return;
+        }
         float alpha = 0.f, beta = 0.f, gamma_old = 1.f;
         int64_t k = 0;
         for (;;) {
@@ -397,9 +579,9 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Krylo
                 alpha = gamma / den;
             }
             gamma_old = gamma;
-            // phase A: p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; u = M^-1 r
+            // phase A: p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; u = M r
             for (int i = gtid; i < a.n; i += gsz) {
-                const float u = kv.u32[i];
+                const float u = __ldcg(kv.u32 + i);
                 const float p = fmaf(beta, kv.p32[i], u);
                 const float s = fmaf(beta, kv.s32[i], kv.w32[i]);
                 kv.p32[i] = p;
@@ -407,10 +589,17 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Krylo
                 kv.x32[i] = fmaf(alpha, p, kv.x32[i]);
                 const float r = fmaf(-alpha, s, kv.r32[i]);
                 kv.r32[i] = r;
-                kv.u32[i] = kv.inv_diag32[i] * r;
+                if (mg.enabled)
+                    mg.e0[i] = mg.omega * kv.inv_diag32[i] * r;
+                else
+                    kv.u32[i] = kv.inv_diag32[i] * r;
             }
             k++;
             if (!grid_sync(gb, ds)) return;
+            if (mg.enabled) {
+                if (!mg_vcycle(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds)) return;
+                if (!grid_sync(gb, ds)) return;
+            }
         }
         inner_total += k;
         // x += d (FP64)
@@ -481,7 +670,7 @@ SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
     a.K = c.K;
     a.tol = tol;
     a.max_iter = max_iter;
-    a.inner_tol = 1e-5;
+    a.inner_tol = 1e-6;  // FP32 floor of an inner solve's residual reduction
     a.max_refine = 40;
     return a;
 }
@@ -515,13 +704,15 @@ void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double to
     ++g_launches;
 }
 
-void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const Krylov& k,
-                        double tol, int64_t max_iter, DevStats* ds, cudaStream_t st) {
+void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
+                        const Krylov& k, double tol, int64_t max_iter, DevStats* ds,
+                        cudaStream_t st) {
     SolveArgs a = make_args(c, tol, max_iter);
     Ppe AA = A;
     MatFree mm = mf;
+    Mg gg = mg;
     Krylov kk = k;
-    void* args[] = {&AA, &mm, &kk, &a, &ds};
+    void* args[] = {&AA, &mm, &gg, &kk, &a, &ds};
     cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
     cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kBlock), args, 0, st);
     ++g_launches;

@@ -96,6 +96,8 @@ def load(build_if_missing: bool = False):
     L.mps_create.argtypes = [P(MpsParams), C.c_int32, vp, vp, vp, P(vp)]
     L.mps_destroy.argtypes = [vp]
     L.mps_set_solver.argtypes = [vp, C.c_int32, C.c_double, C.c_int64]
+    L.mps_set_multigrid.argtypes = [vp, C.c_int32, C.c_float, C.c_float]
+    L.mps_set_multigrid.restype = C.c_int
     L.mps_step.argtypes = [vp, C.c_int32, P(MpsStepStats)]
     L.mps_run.argtypes = [vp, C.c_int32, P(MpsStepStats)]
     L.mps_download.argtypes = [vp] + [vp] * 8
@@ -171,6 +173,10 @@ class Engine:
 
     def set_solver(self, precision=FP64, tol=0.0, max_iter=0):
         _check(_lib.mps_set_solver(self.h, int(precision), float(tol), int(max_iter)))
+
+    def set_multigrid(self, enabled=True, omega=0.9, scale=1.5):
+        """Preconditioner of the MIXED solver: aggregation multigrid or Jacobi."""
+        _check(_lib.mps_set_multigrid(self.h, 1 if enabled else 0, float(omega), float(scale)))
 
     @staticmethod
     def _stats(st: MpsStepStats) -> dict:
