@@ -112,23 +112,6 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- roofline
-def solver_bytes(precision: int, st: dict, n: int) -> float:
-    """Algorithmic bytes of one pressure solve (one solver launch pair).
-
-    Per stored off-diagonal entry and iteration: column index 4 B plus the
-    value (8 B FP64 / 4 B FP32); per row and iteration the vectors touched
-    once each (FP64: 116 B, FP32 inner: 60 B); the gathered neighbour
-    vector entries are counted once, as the row's own entry.  MIXED adds per
-    refinement the FP64 residual (12 B/entry + 36 B/row) and once the FP32
-    copy of the matrix (12 B/entry + 16 B/row)."""
-    nnz = st["nnz_offdiag"]
-    it = st["cg_iterations"]
-    if precision == 0:
-        return it * (12.0 * nnz + 116.0 * n) + (36.0 * n)
-    ref = st["refinements"] + 1
-    return it * (8.0 * nnz + 60.0 * n) + ref * (12.0 * nnz + 36.0 * n) + (12.0 * nnz + 16.0 * n)
-
-
 def measured_peaks():
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -187,6 +170,140 @@ def cpu_sample(steps: int = 3, workload_name: str = CPU_SAMPLE) -> dict:
                        f"throughput would be lower since CG iterations grow with resolution")}
 
 
+
+# ---------------------------------------------------------------- other workloads
+def _event_timed(stream_ptr, fn):
+    """Device seconds of fn() on the given stream (CUDA events, synchronised)."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(stream_ptr)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    out = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3, out
+
+
+def run_batched(steps: int, warmup: int) -> dict:
+    """64 uneven scenes (seeded: 2k-60k fluid particles, aspect 0.5-2,
+    l0 1e-3..5e-3 m, dam breaks and hydrostatic tanks) advanced together:
+    one graph per step, one persistent launch for all 64 PPE solves."""
+    from mps_gb300 import Batch, scenes
+
+    sc = scenes.batch_scenes(seed=0)
+    nf = sum(int((s[3] == 0).sum()) for s in sc)
+    n = sum(len(s[3]) for s in sc)
+    b = Batch(sc, tol=1e-8)
+    b.step()  # autotuning step
+    for _ in range(warmup):
+        b.step()
+    sec, (stats, _) = _event_timed(b.stream_ptr(), lambda: b.step(steps))
+    info = b.launch_info()
+    its = [s["cg_iterations"] for s in stats]
+    out = {"workload": f"64 scenes (seed 0), {nf} fluid / {n} particles, mixed solver tol 1e-8",
+           "value": nf * steps / sec, "unit": UNIT, "steps": steps,
+           "ms_per_step": 1e3 * sec / steps,
+           "launch": {k: info[k] for k in ("block", "alpha", "grid")},
+           "autotune_ms": [round(x, 3) for x in info["tune_ms"]],
+           "cg_iterations_min_max": [int(min(its)), int(max(its))],
+           "max_rel_residual": float(max(s["cg_relative_residual"] for s in stats)),
+           "cuda_graph_steps": steps if all(s["graph_replayed"] for s in stats) else 0}
+    b.close()
+    return out
+
+
+def run_adjoint() -> dict:
+    """Adjoint of a 200-step trajectory of the hydrostatic tank (0.4 x 0.4 m
+    water, l0 2.5e-3 m: 25,600 fluid particles), FP64, checkpoints every 20
+    steps; loss = mean-squared pressure at 16 wall taps over all steps + squared
+    distance of the final fluid positions to a seeded target; checked against
+    central finite differences (epsilon 1e-6) for gravity and one direction of
+    the initial velocities."""
+    from mps_gb300 import FP64, Engine, Trajectory, scenes
+
+    l0, steps, every = 2.5e-3, 200, 20
+    prm, pos, vel, t = scenes.hydrostatic(l0, size=(0.4, 0.4), dt=1e-3)
+    rng = np.random.default_rng(0)
+    fl = t == scenes.FLUID
+    vel[fl, :2] = rng.normal(0.0, 0.01, (fl.sum(), 2))
+    target = pos[fl] + np.c_[rng.normal(0.0, 0.1 * l0, (fl.sum(), 2)), np.zeros(fl.sum())]
+    taps = scenes.wall_taps(pos, t, l0, 16)
+    eng = Engine(prm, pos, vel, t, precision=FP64)
+    tr = Trajectory(eng, steps, every, taps)
+    g = np.array(prm["gravity"], float)
+
+    def loss(v0, gv):
+        sp, pf, _ = tr.forward(v0, gv)
+        return float(np.mean(sp ** 2) + np.sum((pf[fl] - target) ** 2)), sp, pf
+
+    t0 = time.perf_counter()
+    L, sp, pf = loss(vel, g)
+    t_fwd = time.perf_counter() - t0
+    d_pos = np.zeros_like(pf)
+    d_pos[fl] = 2.0 * (pf[fl] - target)
+    t0 = time.perf_counter()
+    _, gv, gg = tr.backward(2.0 * sp / sp.size, d_pos, None)
+    t_bwd = time.perf_counter() - t0
+    eps = 1e-6
+    gp, gm = g.copy(), g.copy()
+    gp[1] += eps
+    gm[1] -= eps
+    fd_g = (loss(vel, gp)[0] - loss(vel, gm)[0]) / (2 * eps)
+    u = np.zeros_like(vel)
+    u[fl, :2] = rng.normal(size=(fl.sum(), 2))
+    u /= np.linalg.norm(u)
+    fd_v = (loss(vel + eps * u, g)[0] - loss(vel - eps * u, g)[0]) / (2 * eps)
+    ad_v = float(np.sum(gv * u))
+    tr.close()
+    eng.close()
+    return {"workload": f"hydrostatic tank 0.4 x 0.4 m, {int(fl.sum())} fluid / {len(t)} particles, "
+                        f"{steps} steps, checkpoints every {every}, FP64",
+            "forward_s": round(t_fwd, 3), "backward_s": round(t_bwd, 3), "loss": L,
+            "dL_dgy": float(gg[1]), "fd_dL_dgy": fd_g,
+            "rel_err_gravity": abs(gg[1] - fd_g) / max(abs(fd_g), 1e-300),
+            "dL_dv0_dir": ad_v, "fd_dL_dv0_dir": fd_v,
+            "rel_err_velocity_dir": abs(ad_v - fd_v) / max(abs(fd_v), 1e-300)}
+
+
+def run_fp64_2m(steps: int) -> dict:
+    """The plain FP64 step (the reference's Jacobi CG to machine epsilon) at
+    2M fluid particles: dam break 0.5 x 1.0 m column, l0 5e-4 m, dt 5e-5 s."""
+    from mps_gb300 import FP64, Engine
+
+    prm, pos, vel, t = workload("dambreak_2m")
+    nf = int((t == 0).sum())
+    e = Engine(prm, pos, vel, t, precision=FP64)
+    e.step()
+    sec, stats = _event_timed(e.stream_ptr(), lambda: [e.step() for _ in range(steps)])
+    out = {"workload": f"dambreak_2m: {nf} fluid / {len(t)} particles, FP64 solver", "steps": steps,
+           "value": nf * steps / sec, "unit": UNIT, "ms_per_step": 1e3 * sec / steps,
+           "cg_iterations_mean": float(np.mean([s["cg_iterations"] for s in stats])),
+           "ms_solve_mean": float(np.mean([s["ms_solve"] for s in stats])),
+           "solve_gbs": float(np.sum([s["solve_bytes"] for s in stats])
+                              / (np.sum([s["ms_solve"] for s in stats]) / 1e3) / 1e9)}
+    e.close()
+    return out
+
+
+def run_small_case() -> dict:
+    """The reference's own CPU-sized case (1,250 fluid particles, dt 1e-3 s,
+    1,000 steps), FP64 on the GPU (graph replays) and on the CPU oracle."""
+    from mps_gb300 import FP64, Engine
+
+    prm, pos, vel, t = workload("dambreak_small")
+    nf = int((t == 0).sum())
+    e = Engine(prm, pos, vel, t, precision=FP64)
+    t0 = time.perf_counter()
+    st = e.run(1000)
+    gpu_s = time.perf_counter() - t0
+    e.close()
+    return {"workload": f"dambreak_small: {nf} fluid / {len(t)} particles, 1000 steps, FP64",
+            "gpu_wall_s": round(gpu_s, 3), "gpu_value": nf * 1000 / gpu_s,
+            "courant_final": st["courant"], "unit": UNIT}
+
 # ---------------------------------------------------------------- GPU arm
 def run_ours(args, rank: int, world: int, dist):
     import torch
@@ -234,7 +351,7 @@ def run_ours(args, rank: int, world: int, dist):
     # roofline of the dominant kernel (the pressure solve)
     hbm_peak, peak_kind = measured_peaks()
     solve_ms = [s["ms_solve"] for s in stats]
-    sb = [solver_bytes(prec, s, n) for s in stats]
+    sb = [s["solve_bytes"] for s in stats]  # the engine's algorithmic-bytes model
     achieved = sum(sb) / (sum(solve_ms) / 1e3) / 1e9
     row_iters = sum(s["cg_iterations"] for s in stats) * n / len(stats)
     tpr = traffic_per_row_iter("cg_mixed" if prec == MIXED else "cg64")
@@ -306,6 +423,13 @@ def run_ours(args, rank: int, world: int, dist):
                "steps": args.e2e_steps}
     eng.close()
 
+    others = {}
+    if not args.no_others:
+        others["batched"] = run_batched(steps=10, warmup=3)
+        others["adjoint"] = run_adjoint()
+        others["fp64_2m"] = run_fp64_2m(steps=3)
+        others["small_case"] = run_small_case()
+
     if rank != 0:
         return None
     cpu = None
@@ -326,11 +450,13 @@ def run_ours(args, rank: int, world: int, dist):
                    "cache": "working set > L2 (state + neighbour lists + matrix ~ GBs per step)",
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "cuda_graph_steps": int(sum(s["graph_replayed"] for s in stats)),
         "cg_iterations_mean": mean("cg_iterations"), "refinements_mean": mean("refinements"),
         "ms_solve_mean": mean("ms_solve"),
         "roofline": roofline, "fp64": fp64,
         "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
         "accuracy": acc, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+        "other_workloads": others or None,
     }
     return line
 
@@ -364,6 +490,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the batched, adjoint, 2M FP64 and small-case workloads")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -82,6 +82,10 @@ typedef struct {
     int32_t kernel_launches;        /* kernels this step launched */
     int64_t nnz_offdiag;            /* stored off-diagonal PPE entries */
     int32_t max_neighbors;          /* largest neighbour count of the last build */
+    int32_t graph_replayed;         /* 1: the step ran as one CUDA graph replay */
+    double solve_bytes;             /* algorithmic HBM bytes of the pressure solve (model:
+                                       every array the solver kernels stream counted once
+                                       per pass at its stored width) */
 } mps_step_stats;
 
 typedef struct mps_engine mps_engine;
@@ -106,6 +110,13 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
  * scale = coarse-correction weight in [1,2)), or plain Jacobi when disabled.
  * No counterpart in the reference (its CG is Jacobi-preconditioned). */
 int mps_set_multigrid(mps_engine* e, int32_t enabled, float omega, float scale);
+
+/* Non-export steps run as a CUDA graph replay (default on): the first step
+ * at each buffer parity captures the step's kernel sequence, later steps
+ * replay it.  Changing the solver or the multigrid settings drops the
+ * graphs.  Export steps always launch eagerly.  No counterpart in the
+ * reference (its step is a sequence of OpenMP loops). */
+int mps_set_graphs(mps_engine* e, int32_t enabled);
 
 /* MPS::stepForward (src/mps.cpp:111-130). */
 int mps_step(mps_engine* e, int32_t is_time_to_export, mps_step_stats* stats);
@@ -141,6 +152,47 @@ int mps_collisions(mps_engine* e, int32_t* pi, int32_t* pj, double* dist, int32_
 
 const char* mps_last_error(void);
 
+/* ------------------------------------------------------------------------
+ * Differentiable trajectories.  No counterpart in the reference (its step
+ * is not differentiated).  A trajectory runs n_steps of the engine from one
+ * initial condition and maps (initial velocities, initial positions,
+ * gravity) to (pressure at the sensor particles after every step, final
+ * positions and velocities).  mps_trajectory_backward returns the
+ * vector-Jacobian product of that map: a hand-written adjoint of the whole
+ * step, with the step's discrete structure frozen at the forward's values
+ * (neighbour sets, ghosts, surface flags, Dirichlet connections, collision
+ * candidates, the negative-pressure clamp and the minimum-pressure
+ * argument).  Memory is bounded by checkpoints every checkpoint_every steps:
+ * the backward pass recomputes each segment with a tape and walks it in
+ * reverse; the transpose Poisson solve is an FP64 CG (A is symmetric).
+ * Arrays are in particle-id order, xyz interleaved (n*3 doubles).  The
+ * engine's solver setting applies to the forward (FP64 gives the derivative
+ * of exactly what is run).  Not supported with the higher-order source term.
+ * ------------------------------------------------------------------------ */
+typedef struct mps_trajectory mps_trajectory;
+
+/* The engine's current positions, velocities and types become the initial
+ * condition.  sensor_ids: particles whose pressure is recorded per step. */
+int mps_trajectory_create(mps_engine* e, int32_t n_steps, int32_t checkpoint_every,
+                          const int32_t* sensor_ids, int32_t n_sensors, mps_trajectory** out);
+int mps_trajectory_destroy(mps_trajectory* t);
+
+/* Runs the trajectory.  vel0 (n*3) replaces the initial velocities (NULL =
+ * those at create or of the last forward), gravity (3) the engine's gravity
+ * (NULL = keep).  Outputs (any may be NULL): sensor_pressure
+ * [n_steps][n_sensors], pos_final and vel_final (n*3).  The engine is left
+ * at the final state. */
+int mps_trajectory_forward(mps_trajectory* t, const double* vel0, const double* gravity,
+                           double* sensor_pressure, double* pos_final, double* vel_final);
+
+/* Adjoint of the last forward: given dL/d(sensor_pressure), dL/d(pos_final),
+ * dL/d(vel_final) (any may be NULL = zero), returns dL/d(pos0), dL/d(vel0)
+ * (n*3) and dL/d(gravity) (3); planar engines report 0 for z.  Afterwards
+ * the engine holds the forward's final positions, velocities and types. */
+int mps_trajectory_backward(mps_trajectory* t, const double* d_sensor_pressure,
+                            const double* d_pos_final, const double* d_vel_final, double* d_pos0,
+                            double* d_vel0, double* d_gravity);
+
 /* No counterpart in the reference.  The initial number density ratio pass of
  * loadInitialState (neighbour search + ratio, the values mps_create computes)
  * for callers that cannot allocate device memory: a host application that
@@ -158,6 +210,43 @@ const char* mps_last_error(void);
  * call returns without waiting. */
 int mps_number_density_static(const mps_params* prm, int32_t n, const double* d_pos,
                               const int32_t* d_type, double* d_ndr, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Batches: many independent scenes advanced together.  No counterpart in
+ * the reference (one scene per process there).  Each scene is a full engine
+ * with the MIXED solver; a batch step is one CUDA graph in which the scenes'
+ * work before and after the pressure solve runs as parallel branches and
+ * every scene's PPE is solved by ONE persistent cooperative launch whose
+ * blocks are split into a group per scene (each group converges on its own
+ * scene's tolerance).  The solve launch's block size (256/512/1024) and the
+ * exponent alpha of its group-size model (blocks ~ rows^alpha) are picked by
+ * an autotuner on the first step unless set with mps_batch_set_launch.
+ * ------------------------------------------------------------------------ */
+typedef struct mps_batch mps_batch;
+
+/* Scene s has counts[s] particles and settings params[s]; pos, vel (n*3)
+ * and type (n) hold the scenes' arrays one after another. */
+int mps_batch_create(int32_t n_scenes, const mps_params* params, const int32_t* counts,
+                     const double* pos, const double* vel, const int32_t* type, mps_batch** out);
+int mps_batch_destroy(mps_batch* b);
+/* Relative residual target of every scene's solve (default 1e-8), iteration cap. */
+int mps_batch_set_solver(mps_batch* b, double tol, int64_t max_iter);
+/* block = 0: autotune at the next step; else 256, 512 or 1024 with alpha in [0, 3]. */
+int mps_batch_set_launch(mps_batch* b, int32_t block, double alpha);
+/* Current launch shape, and the autotuner's per-candidate solve times (ms) in
+ * the order block in {256, 512, 1024} x alpha in {1.0, 1.25, 1.5}. */
+int mps_batch_launch_info(mps_batch* b, int32_t* block, double* alpha, int32_t* grid,
+                          float* tune_ms, int32_t* n_tune);
+/* Blocks of the solve launch given to each scene (n_scenes entries). */
+int mps_batch_group_blocks(mps_batch* b, int32_t* blocks);
+/* n_steps non-export steps of every scene; stats (n_scenes entries, may be
+ * NULL) of the last step, with ms_step = the batch step's device time. */
+int mps_batch_step(mps_batch* b, int32_t n_steps, mps_step_stats* stats, float* ms_last_step);
+int32_t mps_batch_size(const mps_batch* b);
+/* Borrowed engine of scene s (for downloads and views; not to be destroyed). */
+mps_engine* mps_batch_scene(mps_batch* b, int32_t s);
+/* The cudaStream_t the batch's graph runs on. */
+void* mps_batch_stream(mps_batch* b);
 
 #ifdef __cplusplus
 }

@@ -27,7 +27,7 @@ HOST_EXE = os.path.join(LIB, "mps")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--extended-lambda", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(REPO, "include")]
-ENGINE_SRCS = ["sort.cu", "sweeps.cu", "solver.cu", "mg.cu", "capi.cu", "noalloc.cu"]
+ENGINE_SRCS = ["sort.cu", "sweeps.cu", "solver.cu", "mg.cu", "capi.cu", "adjoint.cu", "batch.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

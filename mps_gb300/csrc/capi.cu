@@ -12,8 +12,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/mps_gb300.h"
-#include "engine.cuh"
+#include "engine_impl.cuh"
 
 using namespace mpsg;
 
@@ -104,53 +103,6 @@ __global__ void k_iota(int n, int32_t* a) {
 
 }  // namespace
 
-struct mps_engine {
-    int device = 0;
-    cudaStream_t st = nullptr;
-    mps_params P{};
-    Consts c{};
-    int n = 0, n_pad = 0;
-    StateBuf buf[2]{};
-    int cur = 0;
-    SortScratch sc{};
-    NbList nb{};
-    Ppe A{};
-    Krylov kv{};
-    MatFree mf{};
-    Mg mg{};
-    int32_t mg_requested = 1;
-    int32_t *cand_cnt = nullptr, *cand_base = nullptr;
-    CollPair* pairs = nullptr;
-    int32_t pair_cap = 0;
-    int32_t* parent = nullptr;
-    int8_t* has_surface = nullptr;
-    double *ax = nullptr, *ay = nullptr, *az = nullptr;
-    double* stage = nullptr;  // 3 n doubles for host transfers
-    int32_t* stage_i = nullptr;
-    DevStats* ds = nullptr;
-    DevStats* hs = nullptr;  // pinned
-    int precision = MPS_PRECISION_FP64;
-    double tol = std::numeric_limits<double>::epsilon();
-    int64_t max_iter = 0;
-    int32_t debug_log_count = 0;
-    int32_t step_launches = 0;
-    cudaEvent_t ev[4]{};
-    std::vector<void*> allocs;
-
-    template <typename T>
-    cudaError_t alloc(T** p, size_t count) {
-        void* q = nullptr;
-        cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
-        if (e == cudaSuccess) {
-            allocs.push_back(q);
-            *p = (T*)q;
-        }
-        return e;
-    }
-    StateBuf& S() { return buf[cur]; }
-    void swap() { cur ^= 1; }
-};
-
 namespace {
 
 int alloc_state(mps_engine* e, StateBuf& s) {
@@ -172,6 +124,12 @@ int alloc_state(mps_engine* e, StateBuf& s) {
     return MPS_OK;
 }
 
+Mg active_mg(const mps_engine* e) {
+    Mg g = e->mg;
+    g.enabled = e->mg.enabled && e->mg_requested;
+    return g;
+}
+
 int check_status(mps_engine* e) {
     int32_t s = e->hs->status;
     if (s & ST_TIMEOUT) return fail(MPS_ERR_TIMEOUT, "a bounded device-side wait gave up");
@@ -184,50 +142,105 @@ int check_status(mps_engine* e) {
     return MPS_OK;
 }
 
-// One MPS::stepForward.  Launches only; the caller synchronises.
-void enqueue_step(mps_engine* e, bool do_export) {
-    g_launches = 0;
+// The step in three parts (the batch interleaves many engines' parts around
+// one shared solve launch).  Launches only; the caller synchronises.  With a
+// tape attached, every phase boundary is also recorded for the adjoint
+// (plus a neighbour list at the step-start positions).
+//
+// Part 1: setNeighbors + calcGravity + calcViscosity + moveParticles,
+// setNeighbors + collision, setNeighbors + setBoundaryCondition +
+// setSourceTerm + setMatrix + ensureDirichletBoundaryConnection.
+void enqueue_pre_solve(mps_engine* e) {
     Consts& c = e->c;
     cudaStream_t st = e->st;
     const int mixed = e->precision == MPS_PRECISION_MIXED;
-    // setNeighbors + calcGravity + calcViscosity + moveParticles
+    const bool taping = e->tape != nullptr;
+    if (taping) tape_phase(e, TAPE_START);
     launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
     e->swap();
+    if (taping) tape_phase(e, TAPE_LIST0);
     launch_explicit(c, e->S(), e->buf[e->cur ^ 1], e->sc, mixed, e->ds, st);
     e->swap();
-    // setNeighbors + collision
+    if (taping) tape_phase(e, TAPE_EXPLICIT);
     launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
     e->swap();
     launch_collision(c, e->S(), e->sc, e->cand_cnt, e->cand_base, nullptr, e->pairs, e->pair_cap,
                      e->sc.scan_tmp, e->ds, st);
-    // setNeighbors + calcPressure
+    if (taping) tape_phase(e, TAPE_COLLISION);
     launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
     e->swap();
     launch_build_list(c, e->S(), e->sc, e->nb, e->ds, st);
+    if (taping) tape_phase(e, TAPE_LIST2);
     launch_bc_source(c, e->S(), e->nb, e->A, e->ds, st);
     launch_assemble(c, e->S(), e->nb, e->A, e->ds, st);
     launch_dirichlet(c, e->S(), e->nb, e->A, e->parent, e->has_surface, e->ds, st);
-    cudaEventRecord(e->ev[2], st);
-    int64_t mi = e->max_iter > 0 ? e->max_iter : 2 * (int64_t)c.n;
-    if (mixed) {
-        launch_mixed_setup(c, e->sc, e->A, e->mf, e->kv, st);
-        Mg g = e->mg;
-        g.enabled = e->mg.enabled && e->mg_requested;
-        launch_mg_setup(c, e->A, e->mf, g, st);
-        launch_solve_mixed(c, e->A, e->mf, g, e->kv, e->tol, mi, e->ds, st);
-    } else
-        launch_solve_fp64(c, e->A, e->kv, e->tol, mi, e->ds, st);
-    cudaEventRecord(e->ev[3], st);
-    // removeNegativePressure, setMinimumPressure, calcPressureGradient,
-    // moveParticlesWithPressureGradient, getCourantNumber
+}
+
+// Mixed solver only: FP32 operator and multigrid hierarchy of this step.
+void enqueue_solver_setup(mps_engine* e) {
+    if (e->precision != MPS_PRECISION_MIXED) return;
+    launch_mixed_setup(e->c, e->sc, e->A, e->mf, e->kv, e->st);
+    launch_mg_setup(e->c, e->A, e->mf, active_mg(e), e->st);
+}
+
+// Part 3: removeNegativePressure, setMinimumPressure, calcPressureGradient,
+// moveParticlesWithPressureGradient, getCourantNumber (+ setNumberDensity).
+void enqueue_post_solve(mps_engine* e, bool do_export) {
+    Consts& c = e->c;
+    cudaStream_t st = e->st;
+    const int mixed = e->precision == MPS_PRECISION_MIXED;
     launch_pressure_post(c, e->S(), e->nb, e->kv.x, e->ax, e->ay, e->az, mixed, e->ds, st);
-    if (do_export || c.ho_on) {  // setNumberDensity
+    if (do_export || c.ho_on) {
         launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
         e->swap();
         launch_build_list(c, e->S(), e->sc, e->nb, e->ds, st);
         launch_number_density(c, e->S(), e->nb, st);
     }
+}
+
+// One MPS::stepForward (src/mps.cpp:111-130).
+void enqueue_step(mps_engine* e, bool do_export) {
+    g_launches = 0;
+    cudaStream_t st = e->st;
+    enqueue_pre_solve(e);
+    // inside a stream capture the solve's timing events are external event
+    // nodes; outside one, plain records
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cap);
+    const unsigned evflag = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
+    cudaEventRecordWithFlags(e->ev[2], st, evflag);
+    enqueue_solver_setup(e);
+    const int64_t mi = e->max_iter > 0 ? e->max_iter : 2 * (int64_t)e->c.n;
+    if (e->precision == MPS_PRECISION_MIXED)
+        launch_solve_mixed(e->c, e->A, e->mf, active_mg(e), e->kv, e->tol, mi, e->ds, st);
+    else
+        launch_solve_fp64(e->c, e->A, e->kv, e->tol, mi, e->ds, st);
+    cudaEventRecordWithFlags(e->ev[3], st, evflag);
+    if (e->tape) tape_phase(e, TAPE_SOLVE);
+    enqueue_post_solve(e, do_export);
     e->step_launches = g_launches;
+}
+
+// Algorithmic bytes of one pressure solve: each array a solver pass streams,
+// counted once at its stored width (gathered vector entries count once, as
+// the row's own entry).  Per stored off-diagonal entry and pass: FP64 12 B
+// (column + value), compact FP32 5 B (value + index byte).  Per row and
+// iteration: FP64 CG 116 B (8 vectors); MIXED inner iteration 65 B with the
+// Jacobi preconditioner, or with the multigrid V-cycle 143 B plus two more
+// level-0 operator passes and ~96 B per coarse-grid cell (two 9-point
+// stencil reads + 6 vector words).  MIXED adds per refinement the FP64
+// residual (12 B/entry + 36 B/row) and once the FP32 operator setup
+// (17 B/entry + 16 B/row written and read).
+double solve_bytes(const mps_engine* e, const DevStats& h) {
+    const double nnz = (double)h.nnz_off, n = (double)e->n, it = (double)h.cg_iterations;
+    if (e->precision == MPS_PRECISION_FP64) return it * (12.0 * nnz + 116.0 * n) + 36.0 * n;
+    const bool mg = e->mg.enabled && e->mg_requested;
+    const double ent = e->c.planar ? 5.0 : 8.0;
+    double per_it = mg ? (3.0 * ent * nnz + 143.0 * n) : (ent * nnz + 65.0 * n);
+    if (mg)
+        for (int l = 1; l <= e->mg.nlev; l++) per_it += 96.0 * e->mg.lev[l].nx * e->mg.lev[l].ny;
+    const double ref = (double)h.refinements + 1.0;
+    return it * per_it + ref * (12.0 * nnz + 36.0 * n) + (17.0 * nnz + 16.0 * n);
 }
 
 void fill_stats(mps_engine* e, mps_step_stats* out) {
@@ -250,13 +263,83 @@ void fill_stats(mps_engine* e, mps_step_stats* out) {
     out->n_surface = h.n_surface;
     out->status = h.status;
     float ms = 0.f, ms2 = 0.f;
-    cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]);
-    cudaEventElapsedTime(&ms2, e->ev[2], e->ev[3]);
+    // events a step did not record (batched steps) read as 0 ms
+    if (cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]) != cudaSuccess) ms = 0.f;
+    if (cudaEventElapsedTime(&ms2, e->ev[2], e->ev[3]) != cudaSuccess) ms2 = 0.f;
+    cudaGetLastError();
     out->ms_step = ms;
     out->ms_solve = ms2;
     out->kernel_launches = e->step_launches;
     out->nnz_offdiag = (int64_t)h.nnz_off;
     out->max_neighbors = h.max_neighbors;
+    out->graph_replayed = e->last_step_graphed;
+    out->solve_bytes = solve_bytes(e, h);
+}
+
+void drop_graphs(mps_engine* e) {
+    for (int p = 0; p < 2; p++)
+        if (e->gexec[p]) {
+            cudaGraphExecDestroy(e->gexec[p]);
+            e->gexec[p] = nullptr;
+        }
+}
+
+// Captures one non-export step (stats reset, kernels, stats read-back) as a
+// graph for the current buffer parity.  Returns false if the capture was
+// refused; the step then runs eagerly and the engine stops trying.
+bool capture_step(mps_engine* e) {
+    const int par = e->cur;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaMemsetAsync(e->ds, 0, sizeof(DevStats), e->st);
+    enqueue_step(e, false);
+    cudaMemcpyAsync(e->hs, e->ds, sizeof(DevStats), cudaMemcpyDeviceToHost, e->st);
+    cudaError_t ce = cudaStreamEndCapture(e->st, &g);
+    const int end_parity = e->cur;
+    e->cur = par;  // nothing ran yet: the launch below performs the swaps
+    cudaGraphExec_t x = nullptr;
+    if (ce == cudaSuccess && g) ce = cudaGraphInstantiate(&x, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (ce != cudaSuccess || !x) {
+        cudaGetLastError();
+        return false;
+    }
+    e->gexec[par] = x;
+    e->graph_launches[par] = e->step_launches;
+    e->graph_end_parity[par] = end_parity;
+    return true;
+}
+
+// One MPS::stepForward: a graph replay for non-export steps where graphs are
+// on, else the kernels launched one by one.  Waits for the step's stats.
+int run_one_step(mps_engine* e, bool do_export, mps_step_stats* stats) {
+    const int par = e->cur;
+    bool graphed = false;
+    if (!do_export && !e->tape && e->use_graph && !e->graph_broken) {
+        if (!e->gexec[par] && !capture_step(e)) e->graph_broken = 1;
+        graphed = e->gexec[par] != nullptr;
+    }
+    if (graphed) {
+        CU(cudaEventRecord(e->ev[0], e->st));
+        CU(cudaGraphLaunch(e->gexec[par], e->st));
+        CU(cudaEventRecord(e->ev[1], e->st));
+        e->cur = e->graph_end_parity[par];
+        e->step_launches = e->graph_launches[par];
+    } else {
+        CU(cudaMemsetAsync(e->ds, 0, sizeof(DevStats), e->st));
+        CU(cudaEventRecord(e->ev[0], e->st));
+        enqueue_step(e, do_export);
+        CU(cudaEventRecord(e->ev[1], e->st));
+        CU(cudaMemcpyAsync(e->hs, e->ds, sizeof(DevStats), cudaMemcpyDeviceToHost, e->st));
+    }
+    e->last_step_graphed = graphed ? 1 : 0;
+    CU(cudaStreamSynchronize(e->st));
+    CU(cudaGetLastError());
+    fill_stats(e, stats);
+    return check_status(e);
 }
 
 }  // namespace
@@ -472,6 +555,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
 int mps_destroy(mps_engine* e) {
     if (!e) return MPS_OK;
     if (e->st) cudaStreamSynchronize(e->st);
+    drop_graphs(e);
     for (void* p : e->allocs) cudaFree(p);
     if (e->hs) cudaFreeHost(e->hs);
     for (auto& ev : e->ev)
@@ -485,6 +569,7 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
     if (!e) return fail(MPS_ERR_ARG, "null engine");
     if (precision != MPS_PRECISION_FP64 && precision != MPS_PRECISION_MIXED)
         return fail(MPS_ERR_ARG, "unknown precision");
+    drop_graphs(e);
     e->precision = precision;
     e->tol = tol > 0 ? tol
                      : (precision == MPS_PRECISION_FP64 ? std::numeric_limits<double>::epsilon() : 1e-10);
@@ -498,24 +583,24 @@ int mps_set_multigrid(mps_engine* e, int32_t enabled, float omega, float scale) 
         return fail(MPS_ERR_ARG, "multigrid needs a planar scene (2-D, constant z)");
     if (!(omega > 0.f && omega < 1.f) || !(scale >= 1.f && scale < 2.f))
         return fail(MPS_ERR_ARG, "multigrid weights out of range (0 < omega < 1, 1 <= scale < 2)");
+    drop_graphs(e);
     e->mg_requested = enabled ? 1 : 0;
     e->mg.omega = omega;
     e->mg.scale = scale;
     return MPS_OK;
 }
 
+int mps_set_graphs(mps_engine* e, int32_t enabled) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    e->use_graph = enabled ? 1 : 0;
+    if (!enabled) drop_graphs(e);
+    return MPS_OK;
+}
+
 int mps_run(mps_engine* e, int32_t n_steps, mps_step_stats* stats) {
     if (!e || n_steps < 0) return fail(MPS_ERR_ARG, "mps_run: bad arguments");
     for (int32_t s = 0; s < n_steps; s++) {
-        CU(cudaMemsetAsync(e->ds, 0, sizeof(DevStats), e->st));
-        CU(cudaEventRecord(e->ev[0], e->st));
-        enqueue_step(e, false);
-        CU(cudaEventRecord(e->ev[1], e->st));
-        CU(cudaMemcpyAsync(e->hs, e->ds, sizeof(DevStats), cudaMemcpyDeviceToHost, e->st));
-        CU(cudaStreamSynchronize(e->st));
-        CU(cudaGetLastError());
-        fill_stats(e, stats);
-        int rc = check_status(e);
+        int rc = run_one_step(e, false, stats);
         if (rc) return rc;
     }
     return MPS_OK;
@@ -523,15 +608,7 @@ int mps_run(mps_engine* e, int32_t n_steps, mps_step_stats* stats) {
 
 int mps_step(mps_engine* e, int32_t is_time_to_export, mps_step_stats* stats) {
     if (!e) return fail(MPS_ERR_ARG, "null engine");
-    CU(cudaMemsetAsync(e->ds, 0, sizeof(DevStats), e->st));
-    CU(cudaEventRecord(e->ev[0], e->st));
-    enqueue_step(e, is_time_to_export != 0);
-    CU(cudaEventRecord(e->ev[1], e->st));
-    CU(cudaMemcpyAsync(e->hs, e->ds, sizeof(DevStats), cudaMemcpyDeviceToHost, e->st));
-    CU(cudaStreamSynchronize(e->st));
-    CU(cudaGetLastError());
-    fill_stats(e, stats);
-    return check_status(e);
+    return run_one_step(e, is_time_to_export != 0, stats);
 }
 
 int mps_download(mps_engine* e, double* pos, double* vel, double* pressure, double* min_pressure,
@@ -714,5 +791,17 @@ int mps_collisions(mps_engine* e, int32_t* pi, int32_t* pj, double* dist, int32_
 
 namespace mpsg {
 // Lets the other translation units of the library report through mps_last_error().
-__attribute__((visibility("hidden"))) void set_last_error(const std::string& m) { g_last_error = m; }
+void set_last_error(const std::string& m) { g_last_error = m; }
+int engine_step(mps_engine* e, bool do_export, mps_step_stats* stats) {
+    return run_one_step(e, do_export, stats);
+}
+void engine_drop_graphs(mps_engine* e) { drop_graphs(e); }
+void engine_pre_solve(mps_engine* e) { enqueue_pre_solve(e); }
+void engine_solver_setup(mps_engine* e) { enqueue_solver_setup(e); }
+void engine_post_solve(mps_engine* e, bool do_export) { enqueue_post_solve(e, do_export); }
+Mg engine_active_mg(const mps_engine* e) { return active_mg(e); }
+int engine_collect(mps_engine* e, mps_step_stats* stats) {
+    fill_stats(e, stats);
+    return check_status(e);
+}
 }  // namespace mpsg

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 namespace mpsg {
 
@@ -203,6 +204,38 @@ void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double to
 void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
                         const Krylov& k, double tol, int64_t max_iter, DevStats* ds,
                         cudaStream_t st);
+// Batched mixed-precision solve: many scenes in one cooperative launch, the
+// blocks split into one group per scene (group sizes ~ rows^alpha), each
+// group with its own barrier, reductions and convergence test.
+struct BatchScene {
+    Consts c;
+    Ppe A;
+    MatFree mf;
+    Mg mg;
+    Krylov kv;
+    DevStats* ds;
+    double tol;
+    int64_t max_iter;
+};
+struct BatchSolve {
+    int32_t n_scenes = 0;
+    void* scenes = nullptr;         // device array of per-scene solve descriptors
+    int2* bmap = nullptr;           // per block: (scene, rank in the scene's group)
+    int32_t* gsize = nullptr;       // per scene: blocks in its group
+    unsigned int* bars = nullptr;   // per scene: barrier counter (128-byte stride)
+    int32_t block = 0, grid = 0;
+    double alpha = 0.0;
+    std::vector<int32_t> group_blocks;
+};
+// Blocks of `block` threads (256, 512 or 1024) co-resident on the device.
+int batch_resident_grid(int block, int device);
+void batch_group_sizes(const std::vector<int32_t>& rows, double alpha, int grid,
+                       std::vector<int32_t>& out);
+// 0 on success; 1 if the device holds fewer blocks than scenes; 2 on a CUDA error.
+int batch_solve_setup(const std::vector<BatchScene>& scenes, int block, double alpha, int device,
+                      BatchSolve& b);
+void batch_solve_free(BatchSolve& b);
+void launch_solve_mixed_batched(const BatchSolve& b, cudaStream_t st);
 // Per-solve multigrid setup (after launch_mixed_setup).
 void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
                      cudaStream_t st);

@@ -22,8 +22,11 @@
 //    accumulated with compensation per thread, FP64 across threads and
 //    blocks).  On planar scenes the FP32 matrix is stored with one index
 //    byte per entry (range of the neighbour sweep + offset), 5 B per entry.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <utility>
+#include <vector>
 
 #include "devutil.cuh"
 #include "engine.cuh"
@@ -32,9 +35,10 @@ namespace mpsg {
 
 namespace {
 
-// One 1024-thread block per SM: 152 blocks meet at each grid barrier.
+// Single-scene solves: one 1024-thread block per SM, 152 blocks meet at
+// each grid barrier.  Batched solves (many scenes in one launch) run the same
+// code on groups of blocks, each group with its own barrier and partials.
 constexpr int kBlock = 1024;
-constexpr int kWarps = kBlock / 32;
 constexpr long long kSpinLimit = 1ll << 25;  // ~1-2 s with the back-off below
 
 struct SolveArgs {
@@ -50,7 +54,7 @@ struct SolveArgs {
 // ---------------------------------------------------------------- barriers
 // Grid barrier on one monotonically increasing arrival counter: block b's
 // e-th barrier adds 1 (a release reduction, no reply) and waits until the
-// counter reaches e * gridDim.x.  No block resets anything, so there is no
+// counter reaches e * (blocks in the group).  No block resets anything, so there is no
 // reset race, and the arrivals do not serialise on returning atomics.  The
 // wait is bounded: the blocks of a cooperative launch are co-resident, so it
 // always completes; if it somehow does not, the block raises ST_TIMEOUT and
@@ -59,7 +63,14 @@ struct GridBar {
     unsigned int* count;
     unsigned int epoch;  // barriers passed by this block (same in every block)
     int parity;          // which half of the partials buffer the next reduction uses
+    int rank;            // this block's index within its group
+    int size;            // blocks in the group (the whole grid for a single scene)
+    double* partials;    // 2 x size x 8 per-block partial sums of the group
 };
+
+__device__ __forceinline__ GridBar whole_grid(const Krylov& kv) {
+    return GridBar{kv.barrier, 0u, 0, (int)blockIdx.x, (int)gridDim.x, kv.partials};
+}
 
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
     unsigned int v;
@@ -76,7 +87,7 @@ __device__ __forceinline__ bool grid_sync(GridBar& gb, DevStats* ds) {
     __syncthreads();
     gb.epoch++;
     if (threadIdx.x == 0) {
-        const unsigned int target = gb.epoch * gridDim.x;
+        const unsigned int target = gb.epoch * (unsigned int)gb.size;
         red_release_add(gb.count, 1u);
         bool ok = true;
         long long it = 0;
@@ -100,13 +111,14 @@ __device__ __forceinline__ bool grid_sync(GridBar& gb, DevStats* ds) {
 // in block order, so all blocks hold bitwise the same totals.  Partials are
 // double-buffered so that a fast block's next reduction never overwrites
 // values a slow block is still reading.
-template <int M>
-__device__ __forceinline__ bool reduce_sync(const Krylov& kv, GridBar& gb, const double (&v)[M],
-                                            double (&tot)[M], DevStats* ds) {
-    __shared__ double sh[M][kBlock];
+template <int M, int BS>
+__device__ __forceinline__ bool reduce_sync(GridBar& gb, const double (&v)[M], double (&tot)[M],
+                                            DevStats* ds) {
+    constexpr int kW = BS / 32;
+    __shared__ double sh[M][BS];
     __shared__ double s_tot[M];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double* part = kv.partials + (size_t)gb.parity * gridDim.x * 8;
+    double* part = gb.partials + (size_t)gb.parity * gb.size * 8;
     gb.parity ^= 1;
 #pragma unroll
     for (int m = 0; m < M; m++) sh[m][threadIdx.x] = v[m];
@@ -116,10 +128,10 @@ __device__ __forceinline__ bool reduce_sync(const Krylov& kv, GridBar& gb, const
         for (int m = 0; m < M; m++) {
             double a = 0.0;
 #pragma unroll 8
-            for (int t = 0; t < kWarps; t++) a += sh[m][lane + 32 * t];
+            for (int t = 0; t < kW; t++) a += sh[m][lane + 32 * t];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-            if (lane == 0) part[blockIdx.x * 8 + m] = a;
+            if (lane == 0) part[gb.rank * 8 + m] = a;
         }
     }
     if (!grid_sync(gb, ds)) return false;
@@ -127,7 +139,7 @@ __device__ __forceinline__ bool reduce_sync(const Krylov& kv, GridBar& gb, const
 #pragma unroll
         for (int m = 0; m < M; m++) {
             double a = 0.0;
-            for (int b = lane; b < (int)gridDim.x; b += 32) a += __ldcg(part + b * 8 + m);
+            for (int b = lane; b < gb.size; b += 32) a += __ldcg(part + b * 8 + m);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
             if (lane == 0) s_tot[m] = a;
@@ -218,7 +230,7 @@ __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf
 
 // ----------------------------------------------------------------- FP64 CG
 __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs a, DevStats* ds) {
-    GridBar gb{kv.barrier, 0u, 0};
+    GridBar gb = whole_grid(kv);
     const int lane = threadIdx.x & 31;
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -234,7 +246,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs 
         kv.r[i] = b;
         acc[0] = fma(b, b, acc[0]);
     }
-    if (!reduce_sync<1>(kv, gb, acc, tot, ds)) return;
+    if (!reduce_sync<1, kBlock>(gb, acc, tot, ds)) return;
     const double rhs2 = tot[0];
     int64_t it = 0;
     double rn2 = rhs2;
@@ -250,7 +262,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs 
                 kv.p[i] = p;
                 a1[0] = fma(r, p, a1[0]);
             }
-            if (!reduce_sync<1>(kv, gb, a1, t1, ds)) return;
+            if (!reduce_sync<1, kBlock>(gb, a1, t1, ds)) return;
             double abs_new = t1[0];
             while (it < a.max_iter) {
                 double a2[1] = {0.0}, t2[1];
@@ -262,7 +274,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs 
                     kv.q[i] = q;
                     a2[0] = fma(pi, q, a2[0]);
                 }
-                if (!reduce_sync<1>(kv, gb, a2, t2, ds)) return;
+                if (!reduce_sync<1, kBlock>(gb, a2, t2, ds)) return;
                 const double alpha = abs_new / t2[0];
                 double a3[2] = {0.0, 0.0}, t3[2];
                 for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
@@ -276,7 +288,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs 
                     a3[0] = fma(r, r, a3[0]);
                     a3[1] = fma(r, z, a3[1]);
                 }
-                if (!reduce_sync<2>(kv, gb, a3, t3, ds)) return;
+                if (!reduce_sync<2, kBlock>(gb, a3, t3, ds)) return;
                 rn2 = t3[0];
                 if (rn2 < thr) break;
                 const double beta = t3[1] / abs_new;
@@ -370,12 +382,16 @@ __device__ void mg_block_cycle(Mg& mg, int lo) {
         __syncthreads();
     }
     {
+        // coarsest level: e = A_c^-1 r, one warp per row (lanes split the row)
         MgLevel& L = mg.lev[mg.nlev];
         const int n = L.nx * L.ny;
-        for (int i = tid; i < n; i += nt) {
+        const int lane = tid & 31;
+        for (int i = tid >> 5; i < n; i += nt >> 5) {
             float acc = 0.f;
-            for (int j = 0; j < n; j++) acc = fmaf(__ldcg(mg.dense + i * n + j), __ldcg(L.r + j), acc);
-            L.e[i] = L.invd[i] > 0.f ? acc : 0.f;
+            for (int j = lane; j < n; j += 32) acc = fmaf(__ldg(mg.dense + i * n + j), __ldcg(L.r + j), acc);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) L.e[i] = __ldg(L.invd + i) > 0.f ? acc : 0.f;
         }
         __syncthreads();
     }
@@ -427,8 +443,8 @@ __device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, 
 __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& mf, int K,
                                           const float* __restrict__ r, float* __restrict__ u,
                                           int n, GridBar& gb, DevStats* ds) {
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int gsz = gridDim.x * blockDim.x;
+    const int gtid = gb.rank * blockDim.x + threadIdx.x;
+    const int gsz = gb.size * blockDim.x;
     // level 0 residual of the Inner particles (coalesced, one row per thread)
     for (int i = gtid; i < n; i += gsz)
         mg.res0[i] = A.diag32[i] > 0.f ? __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0) : 0.f;
@@ -459,8 +475,8 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         }
         if (!grid_sync(gb, ds)) return false;
     }
-    // small levels in block 0
-    if (blockIdx.x == 0) mg_block_cycle(mg, mg.ngrid + 1);
+    // small levels in the group's first block
+    if (gb.rank == 0) mg_block_cycle(mg, mg.ngrid + 1);
     if (!grid_sync(gb, ds)) return false;
     // grid-wide levels, up: prolongation folded into the post-smoothing
     for (int l = mg.ngrid; l >= 1; l--) {
@@ -489,11 +505,14 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     return true;
 }
 
-__global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg, Krylov kv,
-                                                        SolveArgs a, DevStats* ds) {
-    GridBar gb{kv.barrier, 0u, 0};
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int gsz = gridDim.x * blockDim.x;
+// The mixed-precision solve of one scene by one group of BS-thread blocks
+// (the whole grid for a single scene, or one scene's share of a batch).
+template <int BS>
+__device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg& mg,
+                                            const Krylov& kv, const SolveArgs& a, DevStats* ds,
+                                            GridBar& gb) {
+    const int gtid = gb.rank * BS + threadIdx.x;
+    const int gsz = gb.size * BS;
     const int lane = threadIdx.x & 31;
     const int gwarp = gtid >> 5;
     const int nwarps = gsz >> 5;
@@ -506,7 +525,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg
         double b = A.src[i];
         acc[0] = fma(b, b, acc[0]);
     }
-    if (!reduce_sync<1>(kv, gb, acc, tot, ds)) return;
+    if (!reduce_sync<1, BS>(gb, acc, tot, ds)) return;
     const double rhs2 = tot[0];
     const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
     int64_t inner_total = 0;
@@ -522,7 +541,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg
             kv.r[i] = r;
             a0[0] = fma(r, r, a0[0]);
         }
-        if (!reduce_sync<1>(kv, gb, a0, t0, ds)) return;
+        if (!reduce_sync<1, BS>(gb, a0, t0, ds)) return;
         rn2 = t0[0];
         if (rn2 < thr || refine >= a.max_refine || inner_total >= a.max_iter) break;
         refine++;
@@ -566,7 +585,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg
                 acc_prod(rr, r, r);
             }
             double v3[3] = {f2d(g), f2d(dl), f2d(rr)}, t3[3];
-            if (!reduce_sync<3>(kv, gb, v3, t3, ds)) return;
+            if (!reduce_sync<3, BS>(gb, v3, t3, ds)) return;
             if ((float)t3[2] < ithr || inner_total + k >= a.max_iter) break;
             const float gamma = (float)t3[0], delta = (float)t3[1];
             if (k == 0) {
@@ -607,11 +626,39 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg
         for (int i = gtid; i < a.n; i += gsz) kv.x[i] = fma((double)kv.x32[i], back, kv.x[i]);
         if (!grid_sync(gb, ds)) return;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (gb.rank == 0 && threadIdx.x == 0) {
         ds->cg_iterations = inner_total;
         ds->refinements = refine;
         ds->cg_rel_residual = rhs2 > 0.0 ? sqrt(rn2 / rhs2) : 0.0;
     }
+}
+
+__global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg, Krylov kv,
+                                                        SolveArgs a, DevStats* ds) {
+    GridBar gb = whole_grid(kv);
+    solve_mixed<kBlock>(A, mf, mg, kv, a, ds, gb);
+}
+
+// Many scenes in one persistent launch: block b belongs to group bmap[b].x
+// (one scene) with rank bmap[b].y; each group converges on its own.
+struct SceneSolve {
+    Ppe A;
+    MatFree mf;
+    Mg mg;
+    Krylov kv;
+    SolveArgs a;
+    DevStats* ds;
+};
+
+template <int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_cg_mixed_batched(const SceneSolve* __restrict__ scenes,
+                                                               const int2* __restrict__ bmap,
+                                                               const int32_t* __restrict__ gsize,
+                                                               unsigned int* bars) {
+    const int2 m = bmap[blockIdx.x];
+    SceneSolve s = scenes[m.x];
+    GridBar gb{bars + 32 * m.x, 0u, 0, m.y, gsize[m.x], s.kv.partials};
+    solve_mixed<BS>(s.A, s.mf, s.mg, s.kv, s.a, s.ds, gb);
 }
 
 // Mixed-solver setup: FP32 values of the matrix, their compact index bytes,
@@ -701,6 +748,109 @@ void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double to
     void* args[] = {&AA, &kk, &a, &ds};
     cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
     cudaLaunchCooperativeKernel((const void*)k_cg64, dim3(k.grid), dim3(kBlock), args, 0, st);
+    ++g_launches;
+}
+
+// ----------------------------------------------------------- batched solve
+namespace {
+template <int BS, int MINB>
+int resident_grid(int device) {
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)k_cg_mixed_batched<BS, MINB>, BS, 0);
+    return sms * (per < 1 ? 1 : per);
+}
+}  // namespace
+
+int batch_resident_grid(int block, int device) {
+    switch (block) {
+        case 256: return resident_grid<256, 4>(device);
+        case 512: return resident_grid<512, 2>(device);
+        case 1024: return resident_grid<1024, 1>(device);
+        default: return 0;
+    }
+}
+
+void batch_group_sizes(const std::vector<int32_t>& rows, double alpha, int grid,
+                       std::vector<int32_t>& out) {
+    const int ns = (int)rows.size();
+    out.assign(ns, 1);
+    std::vector<double> w(ns);
+    double tot = 0.0;
+    for (int s = 0; s < ns; s++) tot += (w[s] = std::pow((double)std::max(rows[s], 1), alpha));
+    int used = 0;
+    std::vector<std::pair<double, int>> frac;
+    for (int s = 0; s < ns; s++) {
+        const double want = grid * w[s] / tot;
+        out[s] = std::max(1, (int)want);
+        used += out[s];
+        frac.push_back({want - (int)want, s});
+    }
+    std::sort(frac.begin(), frac.end(), [](auto& a, auto& b) { return a.first > b.first; });
+    for (size_t k = 0; used < grid && k < frac.size(); k++, used++) out[frac[k].second]++;
+    while (used > grid) {  // the floor of 1 block per scene overshot: trim the largest
+        int big = 0;
+        for (int s = 1; s < ns; s++)
+            if (out[s] > out[big]) big = s;
+        if (out[big] <= 1) break;
+        out[big]--;
+        used--;
+    }
+}
+
+int batch_solve_setup(const std::vector<BatchScene>& scenes, int block, double alpha, int device,
+                      BatchSolve& b) {
+    batch_solve_free(b);
+    const int ns = (int)scenes.size();
+    const int grid = batch_resident_grid(block, device);
+    if (grid < ns || ns == 0) return 1;
+    std::vector<int32_t> rows(ns), gs;
+    for (int s = 0; s < ns; s++) rows[s] = scenes[s].c.n;
+    batch_group_sizes(rows, alpha, grid, gs);
+    std::vector<SceneSolve> hs(ns);
+    std::vector<int2> bmap;
+    for (int s = 0; s < ns; s++) {
+        const BatchScene& q = scenes[s];
+        hs[s] = SceneSolve{q.A, q.mf, q.mg, q.kv, make_args(q.c, q.tol, q.max_iter), q.ds};
+        for (int r = 0; r < gs[s]; r++) bmap.push_back(make_int2(s, r));
+    }
+    if (cudaMalloc(&b.scenes, sizeof(SceneSolve) * ns) != cudaSuccess ||
+        cudaMalloc(&b.bmap, sizeof(int2) * bmap.size()) != cudaSuccess ||
+        cudaMalloc(&b.gsize, sizeof(int32_t) * ns) != cudaSuccess ||
+        cudaMalloc(&b.bars, sizeof(unsigned int) * 32 * ns) != cudaSuccess) {
+        batch_solve_free(b);
+        return 2;
+    }
+    cudaMemcpy(b.scenes, hs.data(), sizeof(SceneSolve) * ns, cudaMemcpyHostToDevice);
+    cudaMemcpy(b.bmap, bmap.data(), sizeof(int2) * bmap.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(b.gsize, gs.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice);
+    b.n_scenes = ns;
+    b.block = block;
+    b.grid = (int32_t)bmap.size();
+    b.alpha = alpha;
+    b.group_blocks = gs;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+void batch_solve_free(BatchSolve& b) {
+    if (b.scenes) cudaFree(b.scenes);
+    if (b.bmap) cudaFree(b.bmap);
+    if (b.gsize) cudaFree(b.gsize);
+    if (b.bars) cudaFree(b.bars);
+    b = BatchSolve{};
+}
+
+void launch_solve_mixed_batched(const BatchSolve& b, cudaStream_t st) {
+    const SceneSolve* sc = (const SceneSolve*)b.scenes;
+    const int2* bm = b.bmap;
+    const int32_t* gs = b.gsize;
+    unsigned int* bars = b.bars;
+    void* args[] = {&sc, &bm, &gs, &bars};
+    cudaMemsetAsync(b.bars, 0, sizeof(unsigned int) * 32 * b.n_scenes, st);
+    const void* fn = b.block == 256   ? (const void*)k_cg_mixed_batched<256, 4>
+                     : b.block == 512 ? (const void*)k_cg_mixed_batched<512, 2>
+                                      : (const void*)k_cg_mixed_batched<1024, 1>;
+    cudaLaunchCooperativeKernel(fn, dim3(b.grid), dim3(b.block), args, 0, st);
     ++g_launches;
 }
 

@@ -528,32 +528,37 @@ __global__ void __launch_bounds__(kThreads) k_move2(Consts c, StateBuf s, const 
                                                     const double* __restrict__ ay,
                                                     const double* __restrict__ az, DevStats* ds) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= c.n || s.type[k] != T_FLUID) return;
-    double a0 = ax[k], a1 = ay[k];
-    double vx = dadd(s.vx[k], dmul(a0, c.dt));
-    double vy = dadd(s.vy[k], dmul(a1, c.dt));
-    double x = dadd(s.x[k], dmul(dmul(a0, c.dt), c.dt));
-    double y = dadd(s.y[k], dmul(dmul(a1, c.dt), c.dt));
-    double vz = 0.0, z = c.z0;
-    if (!PLANAR) {
-        double a2 = az[k];
-        vz = dadd(s.vz[k], dmul(a2, c.dt));
-        z = dadd(s.z[k], dmul(dmul(a2, c.dt), c.dt));
-        s.vz[k] = vz;
-        s.z[k] = z;
+    double cour = 0.0;  // Courant numbers are >= 0: 0 is neutral for the max
+    if (k < c.n && s.type[k] == T_FLUID) {
+        double a0 = ax[k], a1 = ay[k];
+        double vx = dadd(s.vx[k], dmul(a0, c.dt));
+        double vy = dadd(s.vy[k], dmul(a1, c.dt));
+        double x = dadd(s.x[k], dmul(dmul(a0, c.dt), c.dt));
+        double y = dadd(s.y[k], dmul(dmul(a1, c.dt), c.dt));
+        double vz = 0.0, z = c.z0;
+        if (!PLANAR) {
+            double a2 = az[k];
+            vz = dadd(s.vz[k], dmul(a2, c.dt));
+            z = dadd(s.z[k], dmul(dmul(a2, c.dt), c.dt));
+            s.vz[k] = vz;
+            s.z[k] = z;
+        }
+        s.vx[k] = vx;
+        s.vy[k] = vy;
+        s.x[k] = x;
+        s.y[k] = y;
+        if (outside_domain(c, x, y, z)) {
+            s.type[k] = T_GHOST;
+            atomicAdd(&ds->n_new_ghosts, 1);
+        } else {
+            double sp = dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz));
+            cour = ddiv(dmul(dsqrt(sp), c.dt), c.l0);
+        }
     }
-    s.vx[k] = vx;
-    s.vy[k] = vy;
-    s.x[k] = x;
-    s.y[k] = y;
-    if (outside_domain(c, x, y, z)) {
-        s.type[k] = T_GHOST;
-        atomicAdd(&ds->n_new_ghosts, 1);
-        return;
-    }
-    double sp = dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz));
-    double cour = ddiv(dmul(dsqrt(sp), c.dt), c.l0);
-    atomic_max_nonneg_double(&ds->courant_bits, cour);
+    // one atomic per warp instead of one per particle
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cour = fmax(cour, __shfl_xor_sync(0xffffffffu, cour, o));
+    if ((threadIdx.x & 31) == 0 && cour > 0.0) atomic_max_nonneg_double(&ds->courant_bits, cour);
 }
 
 // MPS::setNumberDensity's ratio (src/mps.cpp:627-641)

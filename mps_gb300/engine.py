@@ -63,6 +63,8 @@ class MpsStepStats(C.Structure):
         ("kernel_launches", C.c_int32),
         ("nnz_offdiag", C.c_int64),
         ("max_neighbors", C.c_int32),
+        ("graph_replayed", C.c_int32),
+        ("solve_bytes", C.c_double),
     ]
 
 
@@ -76,7 +78,9 @@ _lib = None
 
 
 def library_path() -> str:
-    return _build.ENGINE_SO
+    """The engine library: MPS_GB300_LIB if set (an alternative build), else
+    the in-tree build."""
+    return os.environ.get("MPS_GB300_LIB") or _build.ENGINE_SO
 
 
 def load(build_if_missing: bool = False):
@@ -98,6 +102,8 @@ def load(build_if_missing: bool = False):
     L.mps_set_solver.argtypes = [vp, C.c_int32, C.c_double, C.c_int64]
     L.mps_set_multigrid.argtypes = [vp, C.c_int32, C.c_float, C.c_float]
     L.mps_set_multigrid.restype = C.c_int
+    L.mps_set_graphs.argtypes = [vp, C.c_int32]
+    L.mps_set_graphs.restype = C.c_int
     L.mps_step.argtypes = [vp, C.c_int32, P(MpsStepStats)]
     L.mps_run.argtypes = [vp, C.c_int32, P(MpsStepStats)]
     L.mps_download.argtypes = [vp] + [vp] * 8
@@ -109,6 +115,31 @@ def load(build_if_missing: bool = False):
     L.mps_neighbors.argtypes = [vp, vp, vp, vp, P(C.c_int64)]
     L.mps_system.argtypes = [vp, vp, vp, vp, vp, P(C.c_int64)]
     L.mps_collisions.argtypes = [vp, vp, vp, vp, P(C.c_int32)]
+    L.mps_trajectory_create.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32, P(vp)]
+    L.mps_trajectory_destroy.argtypes = [vp]
+    L.mps_trajectory_forward.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.mps_trajectory_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    for name in ("mps_trajectory_create", "mps_trajectory_destroy", "mps_trajectory_forward",
+                 "mps_trajectory_backward"):
+        getattr(L, name).restype = C.c_int
+    L.mps_batch_create.argtypes = [C.c_int32, P(MpsParams), vp, vp, vp, vp, P(vp)]
+    L.mps_batch_destroy.argtypes = [vp]
+    L.mps_batch_set_solver.argtypes = [vp, C.c_double, C.c_int64]
+    L.mps_batch_set_launch.argtypes = [vp, C.c_int32, C.c_double]
+    L.mps_batch_launch_info.argtypes = [vp, P(C.c_int32), P(C.c_double), P(C.c_int32), vp,
+                                        P(C.c_int32)]
+    L.mps_batch_group_blocks.argtypes = [vp, vp]
+    L.mps_batch_step.argtypes = [vp, C.c_int32, P(MpsStepStats), P(C.c_float)]
+    L.mps_batch_size.argtypes = [vp]
+    L.mps_batch_size.restype = C.c_int32
+    L.mps_batch_scene.argtypes = [vp, C.c_int32]
+    L.mps_batch_scene.restype = C.c_void_p
+    L.mps_batch_stream.argtypes = [vp]
+    L.mps_batch_stream.restype = C.c_void_p
+    for name in ("mps_batch_create", "mps_batch_destroy", "mps_batch_set_solver",
+                 "mps_batch_set_launch", "mps_batch_launch_info", "mps_batch_group_blocks",
+                 "mps_batch_step"):
+        getattr(L, name).restype = C.c_int
     L.mps_last_error.restype = C.c_char_p
     for name in ("mps_create", "mps_destroy", "mps_set_solver", "mps_step", "mps_run",
                  "mps_download", "mps_upload", "mps_neighbors", "mps_system", "mps_collisions"):
@@ -144,6 +175,19 @@ def _p(a):
 class Engine:
     """One MPS scene on the current CUDA device (see include/mps_gb300.h)."""
 
+    @classmethod
+    def borrowed(cls, handle, n: int) -> "Engine":
+        """A view of an engine owned elsewhere (a batch's scene): not destroyed here."""
+        e = cls.__new__(cls)
+        e.n = int(n)
+        e.h = None
+        e._borrowed = C.c_void_p(handle)
+        return e
+
+    @property
+    def _h(self):
+        return self.h if self.h is not None else getattr(self, "_borrowed", None)
+
     def __init__(self, params: dict, pos, vel, types, precision=FP64, tol=0.0, max_iter=0):
         L = load()
         self.n = int(len(types))
@@ -169,14 +213,18 @@ class Engine:
 
     def stream_ptr(self) -> int:
         """cudaStream_t the engine launches on (for events around its work)."""
-        return int(_lib.mps_stream(self.h) or 0)
+        return int(_lib.mps_stream(self._h) or 0)
 
     def set_solver(self, precision=FP64, tol=0.0, max_iter=0):
-        _check(_lib.mps_set_solver(self.h, int(precision), float(tol), int(max_iter)))
+        _check(_lib.mps_set_solver(self._h, int(precision), float(tol), int(max_iter)))
 
     def set_multigrid(self, enabled=True, omega=0.9, scale=1.5):
         """Preconditioner of the MIXED solver: aggregation multigrid or Jacobi."""
-        _check(_lib.mps_set_multigrid(self.h, 1 if enabled else 0, float(omega), float(scale)))
+        _check(_lib.mps_set_multigrid(self._h, 1 if enabled else 0, float(omega), float(scale)))
+
+    def set_graphs(self, enabled=True):
+        """Non-export steps as CUDA graph replays (default) or eager launches."""
+        _check(_lib.mps_set_graphs(self._h, 1 if enabled else 0))
 
     @staticmethod
     def _stats(st: MpsStepStats) -> dict:
@@ -184,12 +232,12 @@ class Engine:
 
     def step(self, export=False) -> dict:
         st = MpsStepStats()
-        _check(_lib.mps_step(self.h, 1 if export else 0, C.byref(st)))
+        _check(_lib.mps_step(self._h, 1 if export else 0, C.byref(st)))
         return self._stats(st)
 
     def run(self, n_steps: int) -> dict:
         st = MpsStepStats()
-        _check(_lib.mps_run(self.h, int(n_steps), C.byref(st)))
+        _check(_lib.mps_run(self._h, int(n_steps), C.byref(st)))
         return self._stats(st)
 
     def state(self) -> dict:
@@ -197,42 +245,159 @@ class Engine:
         d = dict(pos=np.zeros((n, 3)), vel=np.zeros((n, 3)), pressure=np.zeros(n),
                  min_pressure=np.zeros(n), ndr=np.zeros(n), type=np.zeros(n, np.int32),
                  bc=np.zeros(n, np.int32), dirichlet=np.zeros(n, np.int32))
-        _check(_lib.mps_download(self.h, *[_p(d[k]) for k in (
+        _check(_lib.mps_download(self._h, *[_p(d[k]) for k in (
             "pos", "vel", "pressure", "min_pressure", "ndr", "type", "bc", "dirichlet")]))
         return d
 
     def download_into(self, pos=None, vel=None, pressure=None, ndr=None, types=None, bc=None):
-        _check(_lib.mps_download(self.h, _p(pos), _p(vel), _p(pressure), None, _p(ndr),
+        _check(_lib.mps_download(self._h, _p(pos), _p(vel), _p(pressure), None, _p(ndr),
                                  _p(types), _p(bc), None))
 
     def upload(self, pos=None, vel=None, types=None):
-        _check(_lib.mps_upload(self.h, _p(pos), _p(vel), _p(types)))
+        _check(_lib.mps_upload(self._h, _p(pos), _p(vel), _p(types)))
 
     def neighbors(self):
         tot = C.c_int64()
-        _check(_lib.mps_neighbors(self.h, None, None, None, C.byref(tot)))
+        _check(_lib.mps_neighbors(self._h, None, None, None, C.byref(tot)))
         off = np.zeros(self.n + 1, np.int64)
         ids = np.zeros(tot.value, np.int32)
         dist = np.zeros(tot.value)
-        _check(_lib.mps_neighbors(self.h, _p(off), _p(ids), _p(dist), C.byref(tot)))
+        _check(_lib.mps_neighbors(self._h, _p(off), _p(ids), _p(dist), C.byref(tot)))
         return off, ids, dist
 
     def system(self):
         nnz = C.c_int64()
         src = np.zeros(self.n)
-        _check(_lib.mps_system(self.h, _p(src), None, None, None, C.byref(nnz)))
+        _check(_lib.mps_system(self._h, _p(src), None, None, None, C.byref(nnz)))
         rp = np.zeros(self.n + 1, np.int64)
         col = np.zeros(nnz.value, np.int32)
         val = np.zeros(nnz.value)
-        _check(_lib.mps_system(self.h, _p(src), _p(rp), _p(col), _p(val), C.byref(nnz)))
+        _check(_lib.mps_system(self._h, _p(src), _p(rp), _p(col), _p(val), C.byref(nnz)))
         return src, rp, col, val
 
     def collisions(self):
         cnt = C.c_int32()
-        _check(_lib.mps_collisions(self.h, None, None, None, C.byref(cnt)))
+        _check(_lib.mps_collisions(self._h, None, None, None, C.byref(cnt)))
         a = np.zeros(cnt.value, np.int32)
         b = np.zeros(cnt.value, np.int32)
         d = np.zeros(cnt.value)
         if cnt.value:
-            _check(_lib.mps_collisions(self.h, _p(a), _p(b), _p(d), C.byref(cnt)))
+            _check(_lib.mps_collisions(self._h, _p(a), _p(b), _p(d), C.byref(cnt)))
         return a, b, d
+
+
+class Trajectory:
+    """n_steps of an engine from its current state, with the adjoint of the
+    whole step (include/mps_gb300.h, mps_trajectory_*).  Arrays are numpy,
+    particle-id order, shape (n, 3) for vectors."""
+
+    def __init__(self, engine: Engine, n_steps: int, checkpoint_every: int = 20, sensors=()):
+        self.engine = engine
+        self.n = engine.n
+        self.steps = int(n_steps)
+        self.sensors = np.ascontiguousarray(sensors, np.int32)
+        h = C.c_void_p()
+        _check(_lib.mps_trajectory_create(engine._h, self.steps, int(checkpoint_every),
+                                          _p(self.sensors) if len(self.sensors) else None,
+                                          len(self.sensors), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.mps_trajectory_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, vel0=None, gravity=None):
+        """-> (sensor pressure [steps, n_sensors], final positions, final velocities)."""
+        v0 = None if vel0 is None else np.ascontiguousarray(vel0, np.float64).reshape(self.n, 3)
+        g = None if gravity is None else np.ascontiguousarray(gravity, np.float64).reshape(3)
+        sp = np.zeros((self.steps, len(self.sensors)))
+        pos = np.zeros((self.n, 3))
+        vel = np.zeros((self.n, 3))
+        _check(_lib.mps_trajectory_forward(self.h, _p(v0), _p(g), _p(sp) if sp.size else None,
+                                           _p(pos), _p(vel)))
+        return sp, pos, vel
+
+    def backward(self, d_sensor=None, d_pos=None, d_vel=None):
+        """Vector-Jacobian product of the last forward -> (dL/dpos0, dL/dvel0, dL/dgravity)."""
+        def arr(a, shape):
+            return None if a is None else np.ascontiguousarray(a, np.float64).reshape(shape)
+        ds = arr(d_sensor, (self.steps, len(self.sensors)))
+        dp, dv = arr(d_pos, (self.n, 3)), arr(d_vel, (self.n, 3))
+        gp, gv, gg = np.zeros((self.n, 3)), np.zeros((self.n, 3)), np.zeros(3)
+        _check(_lib.mps_trajectory_backward(self.h, _p(ds) if ds is not None and ds.size else None,
+                                            _p(dp), _p(dv), _p(gp), _p(gv), _p(gg)))
+        return gp, gv, gg
+
+
+class Batch:
+    """Many independent scenes advanced together with one shared solve launch
+    per step (include/mps_gb300.h, mps_batch_*)."""
+
+    def __init__(self, scenes, tol=1e-8, max_iter=0):
+        """scenes: list of (params, pos[n,3], vel[n,3], types[n])."""
+        L = load()
+        self.counts = np.array([len(s[3]) for s in scenes], np.int32)
+        prms = (MpsParams * len(scenes))(*[make_params(s[0]) for s in scenes])
+        pos = np.ascontiguousarray(np.concatenate([np.asarray(s[1], np.float64).reshape(-1, 3)
+                                                   for s in scenes]))
+        vel = np.ascontiguousarray(np.concatenate([np.asarray(s[2], np.float64).reshape(-1, 3)
+                                                   for s in scenes]))
+        typ = np.ascontiguousarray(np.concatenate([np.asarray(s[3], np.int32) for s in scenes]))
+        h = C.c_void_p()
+        _check(L.mps_batch_create(len(scenes), prms, _p(self.counts), _p(pos), _p(vel), _p(typ),
+                                  C.byref(h)))
+        self.h = h
+        self.set_solver(tol, max_iter)
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.mps_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.counts)
+
+    def set_solver(self, tol=1e-8, max_iter=0):
+        _check(_lib.mps_batch_set_solver(self.h, float(tol), int(max_iter)))
+
+    def set_launch(self, block=0, alpha=1.0):
+        """block 0: autotune at the next step; else 256/512/1024 threads and alpha."""
+        _check(_lib.mps_batch_set_launch(self.h, int(block), float(alpha)))
+
+    def launch_info(self) -> dict:
+        blk, al, grid, nt = C.c_int32(), C.c_double(), C.c_int32(), C.c_int32()
+        ms = np.zeros(16, np.float32)
+        _check(_lib.mps_batch_launch_info(self.h, C.byref(blk), C.byref(al), C.byref(grid),
+                                          _p(ms), C.byref(nt)))
+        gb = np.zeros(len(self), np.int32)
+        if blk.value:
+            _check(_lib.mps_batch_group_blocks(self.h, _p(gb)))
+        return {"block": blk.value, "alpha": al.value, "grid": grid.value,
+                "tune_ms": ms[:nt.value].tolist(), "group_blocks": gb.tolist()}
+
+    def step(self, n_steps=1):
+        """-> (list of per-scene stats dicts of the last step, batch step ms)."""
+        st = (MpsStepStats * len(self))()
+        ms = C.c_float()
+        _check(_lib.mps_batch_step(self.h, int(n_steps), st, C.byref(ms)))
+        return [Engine._stats(s) for s in st], ms.value
+
+    def stream_ptr(self) -> int:
+        return int(_lib.mps_batch_stream(self.h) or 0)
+
+    def scene(self, s: int) -> Engine:
+        """Borrowed engine view of scene s (state(), neighbors(), ...)."""
+        return Engine.borrowed(_lib.mps_batch_scene(self.h, int(s)), int(self.counts[s]))

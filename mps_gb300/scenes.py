@@ -134,3 +134,41 @@ def hydrostatic(l0, size=(0.4, 0.4), tank_height=None, dt=1e-3, wall_layers=2, d
                              wall_layers, dummy_layers)
     prm = baseline_physics(l0, dt, (-margin, -margin, 0.0), (size[0] + margin, th + margin, 0.0))
     return prm, pos, vel, t
+
+
+def batch_scenes(seed=0, n_scenes=64, fluid_range=(2000, 60000), aspect_range=(0.5, 2.0),
+                 l0_range=(1e-3, 5e-3)):
+    """Independent uneven scenes for one batch: per scene a seeded fluid
+    particle count, column aspect (height / width) and particle distance,
+    alternately a dam break (column in the left corner of a tank 4x its
+    width and 1.2x its height) and a hydrostatic tank (column filling the
+    tank's width), with the dam-break physics at dt = 0.1 s/m x l0 (the
+    1,250-particle case's dt / l0).  Returns a list of (params, pos, vel, types)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(n_scenes):
+        nf = int(rng.integers(fluid_range[0], fluid_range[1] + 1))
+        aspect = float(rng.uniform(*aspect_range))
+        l0 = float(rng.uniform(*l0_range))
+        cols = max(2, int(round(math.sqrt(nf / aspect))))
+        rows = max(2, int(round(nf / cols)))
+        w, h = cols * l0, rows * l0
+        dt = 0.1 * l0
+        if s % 2 == 0:
+            out.append(dam_break(l0, tank=(4 * w, 1.2 * h), column=(w, h), dt=dt,
+                                 margin=2 * l0 * 10))
+        else:
+            out.append(hydrostatic(l0, size=(w, h), dt=dt, margin=2 * l0 * 10))
+    return out
+
+
+def wall_taps(pos, types, l0, count=16):
+    """`count` wall particles of the innermost bottom wall row (the row just
+    below the fluid), evenly spread over its length: pressure taps."""
+    wall = np.flatnonzero(types == WALL)
+    fluid_y = pos[types == FLUID, 1].min()
+    below = wall[pos[wall, 1] < fluid_y]
+    row = below[np.isclose(pos[below, 1], pos[below, 1].max(), rtol=0, atol=0.25 * l0)]
+    row = row[np.argsort(pos[row, 0])]
+    idx = np.linspace(0, len(row) - 1, count).round().astype(int)
+    return row[idx].astype(np.int32)

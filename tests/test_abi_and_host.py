@@ -117,3 +117,32 @@ def test_csv_round_trip(tmp_path):
     t0, pos2, vel2, t2 = scenes.read_csv(p)
     assert t0 == 0.25 and np.array_equal(t2, t)
     assert np.allclose(pos2, pos, atol=5e-7) and np.allclose(vel2, vel, atol=5e-7)
+
+
+def test_batch_scenes_are_seeded_and_in_range():
+    from mps_gb300 import scenes
+
+    a = scenes.batch_scenes(seed=0)
+    b = scenes.batch_scenes(seed=0)
+    assert len(a) == 64
+    for (pa, xa, va, ta), (pb, xb, vb, tb) in zip(a, b):
+        assert pa == pb and np.array_equal(xa, xb) and np.array_equal(ta, tb)
+        nf = int((ta == scenes.FLUID).sum())
+        assert 1900 <= nf <= 61000
+        l0 = pa["particle_distance"]
+        assert 1e-3 <= l0 <= 5e-3 and abs(pa["dt"] - 0.1 * l0) < 1e-15
+        assert pa["re_pressure"] == 3.1 * l0 and pa["collision_distance"] == 0.5 * l0
+    total = sum(int((t == scenes.FLUID).sum()) for _, _, _, t in a)
+    assert 1.5e6 < total < 2.5e6
+
+
+def test_wall_taps_sit_under_the_fluid():
+    from mps_gb300 import scenes
+
+    l0 = 2.5e-3
+    prm, pos, vel, t = scenes.hydrostatic(l0, size=(0.4, 0.4))
+    taps = scenes.wall_taps(pos, t, l0, 16)
+    assert len(taps) == 16 and len(set(taps.tolist())) == 16
+    assert np.all(t[taps] == scenes.WALL)
+    assert np.allclose(pos[taps, 1], pos[t == scenes.FLUID, 1].min() - l0)
+    assert np.all(np.diff(pos[taps, 0]) > 0)
