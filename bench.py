@@ -163,12 +163,37 @@ def cpu_sample(steps: int = 3, workload_name: str = CPU_SAMPLE) -> dict:
     tot = sum(d["times"])
     return {"value": d["nf"] * len(d["times"]) / tot, "unit": UNIT, "cores": cores,
             "kind": "port",
-            "sample": (f"{len(d['times'])} full steps of the dam break at l0=0.5/200 m "
-                       f"({d['nf']} fluid particles, same tank, physics and dt) on the CPU oracle, "
-                       f"FP64 CG to machine epsilon solved twice per step as the reference "
-                       f"(CG iterations {d['its']}), {tot:.1f} s; the 1M workload's CPU "
-                       f"throughput would be lower since CG iterations grow with resolution")}
+            "sample": (f"{len(d['times'])} full steps of {workload_name} "
+                       f"({d['nf']} fluid particles) on the CPU oracle, FP64 CG to machine "
+                       f"epsilon solved twice per step as the reference (CG iterations "
+                       f"{_its_summary(d['its'])}), {tot:.1f} s"
+                       + ("; the 1M workload's CPU throughput would be lower since CG "
+                          "iterations grow with resolution" if workload_name == CPU_SAMPLE else ""))}
 
+
+def _its_summary(its):
+    return str(its) if len(its) <= 5 else f"mean {np.mean(its):.1f}, max {max(its)}"
+
+
+
+# ---------------------------------------------------------------- replicas
+def max_over_ranks(seconds: float, dist, device=None) -> float:
+    """The slowest rank's time (replicas: the job ends when the last one does)."""
+    if dist is None:
+        return seconds
+    import torch
+
+    if device is None:
+        device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(fluid_particles: int, steps: int, seconds: float, world: int) -> float:
+    """Whole-job particle-steps/s of `world` replicas that each advanced
+    `fluid_particles` for `steps` steps, timed by the slowest rank."""
+    return world * fluid_particles * steps / seconds
 
 
 # ---------------------------------------------------------------- other workloads
@@ -221,11 +246,13 @@ def run_adjoint() -> dict:
     steps; loss = mean-squared pressure at 16 wall taps over all steps + squared
     distance of the final fluid positions to a seeded target; checked against
     central finite differences (epsilon 1e-6) for gravity and one direction of
-    the initial velocities."""
+    the initial velocities.  dt = 0.1 s/m x l0 = 2.5e-4 s, the 1,250-particle
+    case's dt / l0: at dt = 1e-3 s this resolution is unstable (the Courant
+    number passes 6 within 10 steps), and so is any gradient of it."""
     from mps_gb300 import FP64, Engine, Trajectory, scenes
 
     l0, steps, every = 2.5e-3, 200, 20
-    prm, pos, vel, t = scenes.hydrostatic(l0, size=(0.4, 0.4), dt=1e-3)
+    prm, pos, vel, t = scenes.hydrostatic(l0, size=(0.4, 0.4), dt=0.1 * l0)
     rng = np.random.default_rng(0)
     fl = t == scenes.FLUID
     vel[fl, :2] = rng.normal(0.0, 0.01, (fl.sum(), 2))
@@ -260,7 +287,7 @@ def run_adjoint() -> dict:
     tr.close()
     eng.close()
     return {"workload": f"hydrostatic tank 0.4 x 0.4 m, {int(fl.sum())} fluid / {len(t)} particles, "
-                        f"{steps} steps, checkpoints every {every}, FP64",
+                        f"dt {prm['dt']:.2e} s, {steps} steps, checkpoints every {every}, FP64",
             "forward_s": round(t_fwd, 3), "backward_s": round(t_bwd, 3), "loss": L,
             "dL_dgy": float(gg[1]), "fd_dL_dgy": fd_g,
             "rel_err_gravity": abs(gg[1] - fd_g) / max(abs(fd_g), 1e-300),
@@ -300,9 +327,11 @@ def run_small_case() -> dict:
     st = e.run(1000)
     gpu_s = time.perf_counter() - t0
     e.close()
+    cpu = cpu_sample(steps=1000, workload_name="dambreak_small")
     return {"workload": f"dambreak_small: {nf} fluid / {len(t)} particles, 1000 steps, FP64",
             "gpu_wall_s": round(gpu_s, 3), "gpu_value": nf * 1000 / gpu_s,
-            "courant_final": st["courant"], "unit": UNIT}
+            "courant_final": st["courant"], "unit": UNIT,
+            "cpu_oracle": {k: cpu[k] for k in ("value", "cores", "kind", "sample")}}
 
 # ---------------------------------------------------------------- GPU arm
 def run_ours(args, rank: int, world: int, dist):
@@ -341,11 +370,8 @@ def run_ours(args, rank: int, world: int, dist):
     with ClockSampler(dev) as clk:
         sec, stats = timed(eng, args.steps)
     clocks = clk.summary()
-    if dist:
-        t = torch.tensor([sec], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        sec = float(t.item())
-    value = world * nf * args.steps / sec
+    sec = max_over_ranks(sec, dist)
+    value = replica_throughput(nf, args.steps, sec, world)
     warm_state = eng.state()
 
     # roofline of the dominant kernel (the pressure solve)
@@ -369,11 +395,8 @@ def run_ours(args, rank: int, world: int, dist):
         for _ in range(args.warmup):
             e64.step()
         sec64, st64 = timed(e64, args.steps)
-        if dist:
-            t = torch.tensor([sec64], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            sec64 = float(t.item())
-        fp64 = {"value": world * nf * args.steps / sec64, "ms_per_step": 1e3 * sec64 / args.steps,
+        sec64 = max_over_ranks(sec64, dist)
+        fp64 = {"value": replica_throughput(nf, args.steps, sec64, world), "ms_per_step": 1e3 * sec64 / args.steps,
                 "cg_iterations_mean": float(np.mean([s["cg_iterations"] for s in st64])),
                 "ms_solve_mean": float(np.mean([s["ms_solve"] for s in st64]))}
         e64.close()
@@ -412,11 +435,8 @@ def run_ours(args, rank: int, world: int, dist):
             eng.download_into(pos=hpos, vel=hvel, pressure=hp, ndr=hndr, types=htype, bc=hbc)
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([te], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
-        e2e = {"value": world * nf * args.e2e_steps / te, "unit": UNIT,
+        te = max_over_ranks(te, dist)
+        e2e = {"value": replica_throughput(nf, args.e2e_steps, te, world), "unit": UNIT,
                "h2d_bytes_per_step": int(hpos.nbytes + hvel.nbytes + htype.nbytes),
                "d2h_bytes_per_step": int(hpos.nbytes + hvel.nbytes + hp.nbytes + hndr.nbytes
                                          + htype.nbytes + hbc.nbytes),
@@ -424,7 +444,7 @@ def run_ours(args, rank: int, world: int, dist):
     eng.close()
 
     others = {}
-    if not args.no_others:
+    if not args.no_others and world == 1:  # single-GPU runs only: keeps scaling runs short
         others["batched"] = run_batched(steps=10, warmup=3)
         others["adjoint"] = run_adjoint()
         others["fp64_2m"] = run_fp64_2m(steps=3)

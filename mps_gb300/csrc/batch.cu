@@ -80,6 +80,7 @@ int configure(mps_batch* b, int block, double alpha) {
         mf.skey = e->sc.skey;
         mf.cs = e->sc.cell_start;
         mf.numY = e->c.numY;
+        mf.nkeys = e->c.nkeys;
         sc.push_back(BatchScene{e->c, e->A, mf, engine_active_mg(e), kv, e->ds, b->tol, mi});
     }
     const int rc = batch_solve_setup(sc, block, alpha, b->device, b->bs);

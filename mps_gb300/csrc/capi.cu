@@ -110,6 +110,9 @@ int alloc_state(mps_engine* e, StateBuf& s) {
     CU(e->alloc(&s.x, n));
     CU(e->alloc(&s.y, n));
     CU(e->alloc(&s.z, n));
+    CU(e->alloc(&s.xf, n));
+    CU(e->alloc(&s.yf, n));
+    CU(e->alloc(&s.zf, n));
     CU(e->alloc(&s.vx, n));
     CU(e->alloc(&s.vy, n));
     CU(e->alloc(&s.vz, n));
@@ -422,6 +425,23 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     c.t_s = sq_threshold(c.re_s);
     c.t_max = sq_threshold(c.re_max);
     c.t_cd = sq_threshold(c.cd);
+    {
+        // FP32 pre-filter bounds: coordinates of magnitude <= M round to FP32
+        // within 2^-24 M, so an FP32 distance is within 4 * 2^-23 * M of the
+        // exact one (two roundings per coordinate, three coordinates, and the
+        // subtraction); FP32 arithmetic adds a relative 1e-6, covered by 1e-5.
+        double M = 0.0;
+        for (int d = 0; d < 3; d++) M = std::max({M, std::fabs(P.domain_min[d]), std::fabs(P.domain_max[d])});
+        M += 10.0 * c.re_max;
+        const double delta = 4.0 * std::ldexp(1.0, -23) * M;
+        auto fbound = [&](double re) {
+            const double r = (re + delta) * (1.0 + 1e-5);
+            return std::nextafter((float)(r * r), std::numeric_limits<float>::infinity());
+        };
+        c.ft_max = fbound(c.re_max);
+        c.ft_v = fbound(c.re_v);
+        c.ft_cd = fbound(c.cd);
+    }
     ref_values(P.dim, c.l0, c.re_p, &c.n0_p, &c.lam_p);
     ref_values(P.dim, c.l0, c.re_v, &c.n0_v, &c.lam_v);
     ref_values(P.dim, c.l0, c.re_s, &c.n0_s, &c.lam_s);
@@ -479,6 +499,8 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     e->pair_cap = (int32_t)std::min<size_t>(4 * np + 1024, (size_t)1 << 30);
     if (e->alloc(&e->pairs, e->pair_cap)) return bail(fail(MPS_ERR_CUDA, "cudaMalloc pairs"));
     solver_setup(e->kv, e->n_pad, dev);
+    if (e->kv.grid <= 0)
+        return bail(fail(MPS_ERR_NO_DEVICE, "the persistent solver does not fit co-resident on this device"));
     // multigrid hierarchy (planar scenes): level 1 = the numX x numY cell grid
     if (c.planar) {
         Mg& g = e->mg;

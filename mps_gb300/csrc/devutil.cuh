@@ -86,6 +86,20 @@ __device__ __forceinline__ double dist2(const StateBuf& s, int i, int j, double 
     return r;
 }
 
+// FP32 pre-filter: true if candidate j is certainly farther from (fx, fy,
+// fz) than the radius whose FP32 bound is `bound` (see Consts::ft_max).
+template <bool PLANAR>
+__device__ __forceinline__ bool far32(const StateBuf& s, int j, float fx, float fy, float fz,
+                                      float bound) {
+    const float dx = s.xf[j] - fx, dy = s.yf[j] - fy;
+    float r = dx * dx + dy * dy;
+    if (!PLANAR) {
+        const float dz = s.zf[j] - fz;
+        r += dz * dz;
+    }
+    return r > bound;
+}
+
 __device__ __forceinline__ void atomic_max_nonneg_double(unsigned long long* a, double v) {
     atomicMax(a, (unsigned long long)__double_as_longlong(v));
 }

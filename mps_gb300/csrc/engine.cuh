@@ -46,6 +46,11 @@ struct Consts {
     // squared-distance thresholds: sqrt_rn(d2) < re  <=>  d2 < t_*
     double t_p, t_v, t_s, t_max, t_cd;
     double n0_p, n0_v, n0_s, lam_p, lam_v, lam_s;
+    // FP32 squared-distance bounds of the candidate pre-filter: a candidate
+    // whose FP32 squared distance exceeds one of these is certainly outside
+    // that radius in exact FP64 (margin: the FP32 rounding of coordinates of
+    // magnitude up to the domain bound), so only the rest get the exact test
+    float ft_max, ft_v, ft_cd;
     double beta_n0s;    // beta * n0 (src/mps.cpp:271)
     double visc_a;      // nu * (2 dim) / (n0 lambda)           src/mps.cpp:182
     double mat_c;       // 2 D / (lambda n0)                     src/mps.cpp:343
@@ -60,6 +65,7 @@ struct Consts {
 
 struct StateBuf {
     double *x, *y, *z, *vx, *vy, *vz;
+    float *xf, *yf, *zf;  // FP32 copies of the positions (written by the rebuild gather)
     double *p, *minp, *ndr, *nd_last;
     int32_t* id;
     int8_t *type, *bc, *dir;
@@ -134,6 +140,7 @@ struct MatFree {
     const int32_t* skey;        // cell key per slot (from the last rebuild)
     const int32_t* cs;          // cell start table
     int32_t numY;
+    int32_t nkeys;              // cells (ghost slots carry the sentinel key nkeys)
     int32_t enabled;            // planar scenes only
 };
 

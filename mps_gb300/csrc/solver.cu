@@ -49,6 +49,7 @@ struct SolveArgs {
     int64_t max_iter;
     double inner_tol;
     int32_t max_refine;
+    int32_t win_cap;    // shared-memory operand window (floats); 0 = gather from global
 };
 
 // ---------------------------------------------------------------- barriers
@@ -176,25 +177,35 @@ __device__ __forceinline__ double spmv64_row(const Ppe& A, int K, int sl, int la
     return fma(A.diag[row], xi, s0 + s1);
 }
 
+// Vector entry c of the operand: from the block's shared-memory window
+// (slots lo..) or straight from global memory.
+template <bool SMEM>
+__device__ __forceinline__ float ld_vec(const float* __restrict__ v, int c, int lo) {
+    if (SMEM) return v[c - lo];
+    return __ldcg(v + c);
+}
+
 // FP32 SELL row (rows without a matrix-free form)
+template <bool SMEM>
 __device__ __forceinline__ float spmv32_sell_row(const Ppe& A, int K, int row,
-                                                 const float* __restrict__ u) {
+                                                 const float* __restrict__ u, int lo) {
     const int sl = row >> 5, lane = row & 31;
     const int w = __ldg(A.slice_w + sl);
     const int32_t* cp = A.col + (size_t)sl * K * 32 + lane;
     const float* vp = A.val32 + (size_t)sl * K * 32 + lane;
     float s = 0.f;
-    for (int m = 0; m < w; m++) s = fmaf(__ldg(vp + m * 32), __ldcg(u + __ldg(cp + m * 32)), s);
+    for (int m = 0; m < w; m++) s = fmaf(__ldg(vp + m * 32), ld_vec<SMEM>(u, __ldg(cp + m * 32), lo), s);
     return s;
 }
 
 // Compact FP32 row: entries (value, range/offset byte); column =
 // start of range + offset.  Loads batched four at a time.
+template <bool SMEM>
 __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf, int K, int row,
-                                                 const float* __restrict__ u) {
+                                                 const float* __restrict__ u, int lo) {
     const int sl = row >> 5, lane = row & 31;
     const int w = __ldg(A.slice_w + sl);
-    const int32_t key = __ldg(mf.skey + row);
+    const int32_t key = min(__ldg(mf.skey + row), mf.nkeys - 1);  // ghosts: sentinel nkeys
     const int ix = key / mf.numY, iy = key - ix * mf.numY;
     const int base0 = (ix - 1) * mf.numY + iy - 1;
     const int s0 = __ldg(mf.cs + base0), s1 = __ldg(mf.cs + base0 + mf.numY),
@@ -214,7 +225,7 @@ __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf
             v[t] = __ldg(vp + (m + t) * 32);
         }
 #pragma unroll
-        for (int t = 0; t < 4; t++) x[t] = __ldcg(u + c[t]);
+        for (int t = 0; t < 4; t++) x[t] = ld_vec<SMEM>(u, c[t], lo);
         a0 = fmaf(v[0], x[0], a0);
         a1 = fmaf(v[1], x[1], a1);
         a0 = fmaf(v[2], x[2], a0);
@@ -223,9 +234,62 @@ __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf
     for (; m < w; m++) {
         const int b = __ldg(ip + m * 32);
         const int r = b >> 6;
-        a0 = fmaf(__ldg(vp + m * 32), __ldcg(u + (r == 0 ? s0 : (r == 1 ? s1 : s2)) + (b & 63)), a0);
+        a0 = fmaf(__ldg(vp + m * 32), ld_vec<SMEM>(u, (r == 0 ? s0 : (r == 1 ? s1 : s2)) + (b & 63), lo), a0);
     }
     return a0 + a1;
+}
+
+// Shared-memory window of an operand for one chunk of BS consecutive rows.
+// Slots are sorted by cell key (x-major), so every neighbour of the chunk's
+// rows lies in the cells from (ix_first-1, iy_first-1) to (ix_last+1,
+// iy_last+1) of the chunk's first and last rows: one contiguous slot range.
+// The block copies that range into shared memory (coalesced) and the rows
+// gather from there instead of from L2.  Windows larger than `cap` entries
+// (and non-planar scenes, whose keys are 3-D) fall back to global gathers.
+struct Window {
+    const float* v;  // operand: shared window or the global array
+    int lo;          // first slot held by the window
+    bool smem;
+};
+
+template <int BS>
+__device__ __forceinline__ Window stage_window(const MatFree& mf, int n, int r0,
+                                               const float* __restrict__ v, float* win, int cap) {
+    __shared__ int s_lohi[2];
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = 1 << 30;
+        if (mf.enabled && cap > 0) {
+            const int rl = min(r0 + BS, n) - 1;
+            int kf = __ldg(mf.skey + r0), kl = __ldg(mf.skey + rl);
+            kf = min(kf, mf.nkeys - 1);  // ghost slots carry the sentinel key nkeys
+            kl = min(kl, mf.nkeys - 1);
+            const int ixf = kf / mf.numY, iyf = kf - ixf * mf.numY;
+            const int ixl = kl / mf.numY, iyl = kl - ixl * mf.numY;
+            const int kmin = max((ixf - 1) * mf.numY + iyf - 1, 0);
+            const int kmax = min((ixl + 1) * mf.numY + iyl + 1, mf.nkeys - 1);
+            lo = __ldg(mf.cs + kmin);
+            hi = __ldg(mf.cs + kmax + 1);
+        }
+        s_lohi[0] = lo;
+        s_lohi[1] = hi;
+    }
+    __syncthreads();
+    const int lo = s_lohi[0], hi = s_lohi[1];
+    if (hi - lo > cap) return Window{v, 0, false};
+    for (int j = lo + (int)threadIdx.x; j < hi; j += BS) win[j - lo] = __ldcg(v + j);
+    __syncthreads();
+    return Window{win, lo, true};
+}
+
+// Off-diagonal part of row i of the FP32 operator applied to the window's operand.
+__device__ __forceinline__ float off_row(const Ppe& A, const MatFree& mf, int K, int i,
+                                         const Window& w) {
+    const bool compact = mf.enabled && !mf.sell_row[i];
+    if (w.smem)
+        return compact ? compact_row_sum<true>(A, mf, K, i, w.v, w.lo)
+                       : spmv32_sell_row<true>(A, K, i, w.v, w.lo);
+    return compact ? compact_row_sum<false>(A, mf, K, i, w.v, 0)
+                   : spmv32_sell_row<false>(A, K, i, w.v, 0);
 }
 
 // ----------------------------------------------------------------- FP64 CG
@@ -330,10 +394,8 @@ __device__ __forceinline__ double f2d(const F2& a) { return (double)a.hi + (doub
 
 // Level-0 operator row (FP32): diag_i v_i + off-diagonal sum.
 __device__ __forceinline__ float a0_row(const Ppe& A, const MatFree& mf, int K, int i,
-                                        const float* __restrict__ v) {
-    const float off = (mf.enabled && !mf.sell_row[i]) ? compact_row_sum(A, mf, K, i, v)
-                                                      : spmv32_sell_row(A, K, i, v);
-    return fmaf(A.diag32[i], __ldcg(v + i), off);
+                                        const Window& w) {
+    return fmaf(A.diag32[i], w.smem ? w.v[i - w.lo] : __ldcg(w.v + i), off_row(A, mf, K, i, w));
 }
 
 // 9-point stencil row of a structured level.
@@ -440,14 +502,20 @@ __device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, 
 // and passed a grid barrier.  Restriction is fused with the next level's
 // pre-smoothing, prolongation with the post-smoothing.  Ends after writing u
 // (no trailing barrier).  Every block runs the same barrier sequence.
+template <int BS>
 __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& mf, int K,
                                           const float* __restrict__ r, float* __restrict__ u,
-                                          int n, GridBar& gb, DevStats* ds) {
-    const int gtid = gb.rank * blockDim.x + threadIdx.x;
-    const int gsz = gb.size * blockDim.x;
-    // level 0 residual of the Inner particles (coalesced, one row per thread)
-    for (int i = gtid; i < n; i += gsz)
-        mg.res0[i] = A.diag32[i] > 0.f ? __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0) : 0.f;
+                                          int n, GridBar& gb, DevStats* ds, float* win, int cap) {
+    const int gtid = gb.rank * BS + threadIdx.x;
+    const int gsz = gb.size * BS;
+    // level 0 residual of the Inner particles (one row per thread, chunks of
+    // BS rows with their e0 window in shared memory)
+    for (int base = gb.rank * BS; base < n; base += gsz) {
+        const Window w = stage_window<BS>(mf, n, base, mg.e0, win, cap);
+        const int i = base + threadIdx.x;
+        if (i < n) mg.res0[i] = A.diag32[i] > 0.f ? __ldcg(r + i) - a0_row(A, mf, K, i, w) : 0.f;
+        __syncthreads();
+    }
     if (!grid_sync(gb, ds)) return false;
     // level 1: sum over each cell's contiguous slots; pre-smooth
     {
@@ -497,10 +565,15 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
                 mg.e0[i] = fmaf(mg.scale, __ldcg(L1.e + __ldg(mf.skey + i)), __ldcg(mg.e0 + i));
     }
     if (!grid_sync(gb, ds)) return false;
-    for (int i = gtid; i < n; i += gsz) {
-        const float dg = A.diag32[i];
-        u[i] = dg > 0.f ? fmaf(mg.omega / dg, __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0), __ldcg(mg.e0 + i))
-                        : 0.f;
+    for (int base = gb.rank * BS; base < n; base += gsz) {
+        const Window w = stage_window<BS>(mf, n, base, mg.e0, win, cap);
+        const int i = base + threadIdx.x;
+        if (i < n) {
+            const float dg = A.diag32[i];
+            u[i] = dg > 0.f ? fmaf(mg.omega / dg, __ldcg(r + i) - a0_row(A, mf, K, i, w), __ldcg(mg.e0 + i))
+                            : 0.f;
+        }
+        __syncthreads();
     }
     return true;
 }
@@ -510,7 +583,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
 template <int BS>
 __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg& mg,
                                             const Krylov& kv, const SolveArgs& a, DevStats* ds,
-                                            GridBar& gb) {
+                                            GridBar& gb, float* win) {
     const int gtid = gb.rank * BS + threadIdx.x;
     const int gsz = gb.size * BS;
     const int lane = threadIdx.x & 31;
@@ -563,7 +636,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
         }
         if (!grid_sync(gb, ds)) return;
         if (mg.enabled) {
-            if (!mg_vcycle(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds)) return;
+            if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds, win, a.win_cap)) return;
             if (!grid_sync(gb, ds)) return;
         }
         float alpha = 0.f, beta = 0.f, gamma_old = 1.f;
@@ -571,18 +644,22 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
         for (;;) {
             // phase B: w = A u ; gamma = r.u, delta = w.u, rho = r.r
             F2 g = {0.f, 0.f}, dl = {0.f, 0.f}, rr = {0.f, 0.f};
-            for (int i = gtid; i < a.n; i += gsz) {
-                const float ui = __ldcg(kv.u32 + i);
-                float w;
-                if (mf.enabled && !mf.sell_row[i])
-                    w = fmaf(A.diag32[i], ui, compact_row_sum(A, mf, a.K, i, kv.u32));
-                else
-                    w = fmaf(A.diag32[i], ui, spmv32_sell_row(A, a.K, i, kv.u32));
-                kv.w32[i] = w;
-                const float r = kv.r32[i];
-                acc_prod(g, r, ui);
-                acc_prod(dl, w, ui);
-                acc_prod(rr, r, r);
+            for (int base = gb.rank * BS; base < a.n; base += gsz) {
+                const Window win_u = stage_window<BS>(mf, a.n, base, kv.u32, win, a.win_cap);
+                const int i = base + threadIdx.x;
+                if (i < a.n) {
+                    // rows that are not unknowns (diagonal 0: Surface, Ignored,
+                    // ghosts) have only zero entries: w = +0 without the gathers
+                    const float ui = __ldcg(kv.u32 + i);
+                    const float dg = A.diag32[i];
+                    const float w = dg > 0.f ? fmaf(dg, ui, off_row(A, mf, a.K, i, win_u)) : 0.f;
+                    kv.w32[i] = w;
+                    const float r = kv.r32[i];
+                    acc_prod(g, r, ui);
+                    acc_prod(dl, w, ui);
+                    acc_prod(rr, r, r);
+                }
+                __syncthreads();
             }
             double v3[3] = {f2d(g), f2d(dl), f2d(rr)}, t3[3];
             if (!reduce_sync<3, BS>(gb, v3, t3, ds)) return;
@@ -616,7 +693,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
             k++;
             if (!grid_sync(gb, ds)) return;
             if (mg.enabled) {
-                if (!mg_vcycle(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds)) return;
+                if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds, win, a.win_cap)) return;
                 if (!grid_sync(gb, ds)) return;
             }
         }
@@ -635,8 +712,9 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
 
 __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg, Krylov kv,
                                                         SolveArgs a, DevStats* ds) {
+    extern __shared__ float s_win[];
     GridBar gb = whole_grid(kv);
-    solve_mixed<kBlock>(A, mf, mg, kv, a, ds, gb);
+    solve_mixed<kBlock>(A, mf, mg, kv, a, ds, gb, s_win);
 }
 
 // Many scenes in one persistent launch: block b belongs to group bmap[b].x
@@ -655,10 +733,11 @@ __global__ void __launch_bounds__(BS, MINB) k_cg_mixed_batched(const SceneSolve*
                                                                const int2* __restrict__ bmap,
                                                                const int32_t* __restrict__ gsize,
                                                                unsigned int* bars) {
+    extern __shared__ float s_win[];
     const int2 m = bmap[blockIdx.x];
     SceneSolve s = scenes[m.x];
     GridBar gb{bars + 32 * m.x, 0u, 0, m.y, gsize[m.x], s.kv.partials};
-    solve_mixed<BS>(s.A, s.mf, s.mg, s.kv, s.a, s.ds, gb);
+    solve_mixed<BS>(s.A, s.mf, s.mg, s.kv, s.a, s.ds, gb, s_win);
 }
 
 // Mixed-solver setup: FP32 values of the matrix, their compact index bytes,
@@ -701,13 +780,21 @@ __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
     for (int m = 0; m < w; m++) A.val32[base + (size_t)m * 32] = (float)A.val[base + (size_t)m * 32];
 }
 
-int coop_grid(const void* fn, int device) {
+// Shared-memory operand window of the mixed solver: 8 floats per thread.
+constexpr int win_cap_for(int bs) { return 8 * bs; }
+
+// Co-resident blocks of a persistent kernel (0 if the configuration does not
+// fit, which the launchers report instead of launching).  Kernels with a
+// dynamic shared window opt in to more than the default 48 KB first.
+int coop_grid(const void* fn, int device, int block, size_t smem, int max_per_sm) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kBlock, 0);
-    if (per < 1) per = 1;
-    if (per > 1) per = 1;
-    return sms * per;
+    if (smem > 0) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, smem) != cudaSuccess) {
+        cudaGetLastError();
+        per = 0;
+    }
+    return sms * std::min(per, max_per_sm);
 }
 
 SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
@@ -719,14 +806,15 @@ SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
     a.max_iter = max_iter;
     a.inner_tol = 1e-6;  // FP32 floor of an inner solve's residual reduction
     a.max_refine = 40;
+    a.win_cap = 0;
     return a;
 }
 
 }  // namespace
 
 void solver_setup(Krylov& k, int32_t /*n_pad*/, int device) {
-    int g1 = coop_grid((const void*)k_cg64, device);
-    int g2 = coop_grid((const void*)k_cg_mixed, device);
+    int g1 = coop_grid((const void*)k_cg64, device, kBlock, 0, 1);
+    int g2 = coop_grid((const void*)k_cg_mixed, device, kBlock, sizeof(float) * win_cap_for(kBlock), 1);
     k.grid = g1 < g2 ? g1 : g2;
     k.block = kBlock;
 }
@@ -736,6 +824,7 @@ void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, Ma
     mf.skey = sc.skey;
     mf.cs = sc.cell_start;
     mf.numY = c.numY;
+    mf.nkeys = c.nkeys;
     k_mixed_setup<<<(c.n + 255) / 256, 256, 0, st>>>(c, A, mf, k);
     ++g_launches;
 }
@@ -755,10 +844,8 @@ void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double to
 namespace {
 template <int BS, int MINB>
 int resident_grid(int device) {
-    int sms = 0, per = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)k_cg_mixed_batched<BS, MINB>, BS, 0);
-    return sms * (per < 1 ? 1 : per);
+    return coop_grid((const void*)k_cg_mixed_batched<BS, MINB>, device, BS,
+                     sizeof(float) * win_cap_for(BS), MINB);
 }
 }  // namespace
 
@@ -812,6 +899,7 @@ int batch_solve_setup(const std::vector<BatchScene>& scenes, int block, double a
     for (int s = 0; s < ns; s++) {
         const BatchScene& q = scenes[s];
         hs[s] = SceneSolve{q.A, q.mf, q.mg, q.kv, make_args(q.c, q.tol, q.max_iter), q.ds};
+        hs[s].a.win_cap = win_cap_for(block);
         for (int r = 0; r < gs[s]; r++) bmap.push_back(make_int2(s, r));
     }
     if (cudaMalloc(&b.scenes, sizeof(SceneSolve) * ns) != cudaSuccess ||
@@ -850,7 +938,8 @@ void launch_solve_mixed_batched(const BatchSolve& b, cudaStream_t st) {
     const void* fn = b.block == 256   ? (const void*)k_cg_mixed_batched<256, 4>
                      : b.block == 512 ? (const void*)k_cg_mixed_batched<512, 2>
                                       : (const void*)k_cg_mixed_batched<1024, 1>;
-    cudaLaunchCooperativeKernel(fn, dim3(b.grid), dim3(b.block), args, 0, st);
+    cudaLaunchCooperativeKernel(fn, dim3(b.grid), dim3(b.block), args,
+                                sizeof(float) * win_cap_for(b.block), st);
     ++g_launches;
 }
 
@@ -858,13 +947,15 @@ void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const 
                         const Krylov& k, double tol, int64_t max_iter, DevStats* ds,
                         cudaStream_t st) {
     SolveArgs a = make_args(c, tol, max_iter);
+    a.win_cap = win_cap_for(kBlock);
     Ppe AA = A;
     MatFree mm = mf;
     Mg gg = mg;
     Krylov kk = k;
     void* args[] = {&AA, &mm, &gg, &kk, &a, &ds};
     cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
-    cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kBlock), args, 0, st);
+    cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kBlock), args,
+                                sizeof(float) * a.win_cap, st);
     ++g_launches;
 }
 

@@ -92,12 +92,17 @@ __global__ void k_gather(int n, const int32_t* __restrict__ perm, const int32_t*
     if (k >= n) return;
     int o = perm[k];
     skey[k] = key[o];
-    out.x[k] = in.x[o];
-    out.y[k] = in.y[o];
+    const double x = in.x[o], y = in.y[o];
+    out.x[k] = x;
+    out.y[k] = y;
+    out.xf[k] = (float)x;
+    out.yf[k] = (float)y;
     out.vx[k] = in.vx[o];
     out.vy[k] = in.vy[o];
     if (!planar) {
-        out.z[k] = in.z[o];
+        const double z = in.z[o];
+        out.z[k] = z;
+        out.zf[k] = (float)z;
         out.vz[k] = in.vz[o];
     }
     out.p[k] = in.p[o];

@@ -32,9 +32,10 @@ template <bool PLANAR>
 __device__ double sweep_number_density_p(const Consts& c, const StateBuf& s, const int32_t* cs,
                                          int32_t key, int k) {
     double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
+    const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
     double nd = 0.0;
     for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
-        if (j == k) return;
+        if (j == k || far32<PLANAR>(s, j, fx, fy, fz, c.ft_max)) return;
         double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
         if (d2 < c.t_max && d2 < c.t_p) nd = dadd(nd, weight(dsqrt(d2), c.re_p));
     });
@@ -58,11 +59,12 @@ __global__ void __launch_bounds__(kThreads) k_explicit(Consts c, StateBuf in, St
     double nd_last = in.nd_last[k];
     if (t == T_FLUID) {
         const int32_t key = skey[k];
+        const float fx = in.xf[k], fy = in.yf[k], fz = PLANAR ? 0.f : in.zf[k];
         double ax, ay, az;
         if (!MIXED) {
             double tx = 0.0, ty = 0.0, tz = 0.0;
             for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
-                if (j == k) return;
+                if (j == k || far32<PLANAR>(in, j, fx, fy, fz, c.ft_v)) return;
                 double d2 = dist2<PLANAR>(in, k, j, x, y, z);
                 if (d2 < c.t_max && d2 < c.t_v) {
                     double w = weight(dsqrt(d2), c.re_v);
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(kThreads) k_explicit(Consts c, StateBuf in, St
             float tx = 0.f, ty = 0.f, tz = 0.f;
             const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
             for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
-                if (j == k) return;
+                if (j == k || far32<PLANAR>(in, j, fx, fy, fz, c.ft_v)) return;
                 double d2 = dist2<PLANAR>(in, k, j, x, y, z);
                 if (d2 < c.t_max && d2 < c.t_v) {
                     float w = c.fre_v * rsqrtf((float)d2) - 1.f;
@@ -140,10 +142,11 @@ __device__ __forceinline__ int for_each_collision(const Consts& c, const StateBu
                                                   const int32_t* cs, int32_t key, int k,
                                                   CollPair* out) {
     double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
+    const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
     int32_t idi = s.id[k];
     int m = 0;
     for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
-        if (j == k) return;
+        if (j == k || far32<PLANAR>(s, j, fx, fy, fz, c.ft_cd)) return;
         double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
         if (!(d2 < c.t_max && d2 < c.t_cd)) return;
         if (s.type[j] == T_FLUID && s.id[j] >= idi) return;
@@ -250,11 +253,12 @@ __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
         return;
     }
     double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
+    const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
     double nd = 0.0;
     int m = 0;
     const int np = nb.n_pad;
     for_each_candidate<PLANAR>(c, cs, skey[k], [&](int j) {
-        if (j == k) return;
+        if (j == k || far32<PLANAR>(s, j, fx, fy, fz, c.ft_max)) return;
         double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
         if (!(d2 < c.t_max)) return;
         double dist = dsqrt(d2);
