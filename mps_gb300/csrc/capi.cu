@@ -462,6 +462,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     int lc = lattice_count(P.dim, c.re_max / c.l0);
     c.K = std::max(32, ((2 * lc + 8 + 31) / 32) * 32);
     e->nb.n_pad = e->n_pad;
+    e->mf.rs_stride = e->n_pad;
     e->mf.enabled = c.planar;
 
     int rc = MPS_OK;
@@ -490,7 +491,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         e->alloc(&e->kv.u32, np) ||
         e->alloc(&e->kv.inv_diag32, np) || e->alloc(&e->kv.barrier, 64) ||
         e->alloc(&e->kv.totals, 8) || e->alloc(&e->mf.idx8, np * K) ||
-        e->alloc(&e->mf.sell_row, np) ||
+        e->alloc(&e->mf.sell_row, np) || e->alloc(&e->mf.rs, 3 * np) ||
         e->alloc(&e->cand_cnt, np + 1) || e->alloc(&e->cand_base, np + 2) ||
         e->alloc(&e->parent, np) || e->alloc(&e->has_surface, np) || e->alloc(&e->ax, np) ||
         e->alloc(&e->ay, np) || e->alloc(&e->az, np) || e->alloc(&e->stage, 3 * np) ||

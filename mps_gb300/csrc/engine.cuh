@@ -124,9 +124,16 @@ struct Ppe {
     int32_t* col;     // SELL-32, width K: ((slot/32)*K + m)*32 + slot%32; padding = (own slot, 0)
     double* val;
     int32_t* slice_w; // max offcnt of each 32-slot slice
-    float* val32;     // FP32 copy of val (mixed path, rows without a matrix-free form)
+    float* val32;     // FP32 copy of val, quad layout (qsell_index) for the mixed solver
     float* diag32;
 };
+
+// Quad SELL-32 layout of the mixed solver's FP32 operator: entry m of slot k
+// at ((k/32) * K/4 + m/4) * 128 + (k%32) * 4 + m%4, i.e. each thread's next
+// four entries are one 16-byte word and the warp's words are contiguous.
+__host__ __device__ __forceinline__ size_t qsell_index(int k, int m, int K) {
+    return ((size_t)(k >> 5) * (K >> 2) + (m >> 2)) * 128 + (size_t)(k & 31) * 4 + (m & 3);
+}
 
 // Compact FP32 form of the PPE operator for the mixed solver (planar
 // scenes): SELL-32 like the FP64 matrix, but each entry is an FP32 value and
@@ -135,8 +142,10 @@ struct Ppe {
 // for the offset inside that range; the range starts come from the cell
 // table.  5 B per entry instead of the FP64 matrix's 12 B.
 struct MatFree {
-    uint8_t* idx8;              // SELL-32 layout like Ppe::col
+    uint8_t* idx8;              // quad SELL-32 layout like Ppe::val32
     int8_t* sell_row;           // 1: this row uses the int32 SELL columns instead
+    int32_t* rs;                // per slot: the 3 range starts (3 x rs_stride)
+    int32_t rs_stride;
     const int32_t* skey;        // cell key per slot (from the last rebuild)
     const int32_t* cs;          // cell start table
     int32_t numY;

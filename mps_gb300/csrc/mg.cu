@@ -40,10 +40,10 @@ __global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L) {
         const int cnt = A.offcnt[k];
         const bool compact = mf.enabled && !mf.sell_row[k];
         for (int m = 0; m < cnt; m++) {
-            const float v = A.val32[base + (size_t)m * 32];
+            const float v = A.val32[qsell_index(k, m, c.K)];
             int dx, dy;
             if (compact) {
-                const int bt = mf.idx8[base + (size_t)m * 32];
+                const int bt = mf.idx8[qsell_index(k, m, c.K)];
                 const int r = bt >> 6;
                 const int j = rs[r][0] + (bt & 63);
                 dx = r - 1;

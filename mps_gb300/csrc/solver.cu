@@ -49,7 +49,6 @@ struct SolveArgs {
     int64_t max_iter;
     double inner_tol;
     int32_t max_refine;
-    int32_t win_cap;    // shared-memory operand window (floats); 0 = gather from global
 };
 
 // ---------------------------------------------------------------- barriers
@@ -177,119 +176,56 @@ __device__ __forceinline__ double spmv64_row(const Ppe& A, int K, int sl, int la
     return fma(A.diag[row], xi, s0 + s1);
 }
 
-// Vector entry c of the operand: from the block's shared-memory window
-// (slots lo..) or straight from global memory.
-template <bool SMEM>
-__device__ __forceinline__ float ld_vec(const float* __restrict__ v, int c, int lo) {
-    if (SMEM) return v[c - lo];
-    return __ldcg(v + c);
-}
-
-// FP32 SELL row (rows without a matrix-free form)
-template <bool SMEM>
+// FP32 SELL row (rows without a compact form): int32 columns of the FP64
+// matrix, FP32 values in the quad layout.
 __device__ __forceinline__ float spmv32_sell_row(const Ppe& A, int K, int row,
-                                                 const float* __restrict__ u, int lo) {
+                                                 const float* __restrict__ u) {
     const int sl = row >> 5, lane = row & 31;
     const int w = __ldg(A.slice_w + sl);
     const int32_t* cp = A.col + (size_t)sl * K * 32 + lane;
-    const float* vp = A.val32 + (size_t)sl * K * 32 + lane;
+    const float* vq = A.val32 + qsell_index(row, 0, K);
     float s = 0.f;
-    for (int m = 0; m < w; m++) s = fmaf(__ldg(vp + m * 32), ld_vec<SMEM>(u, __ldg(cp + m * 32), lo), s);
+    for (int m = 0; m < w; m++)
+        s = fmaf(__ldg(vq + (m >> 2) * 128 + (m & 3)), __ldcg(u + __ldg(cp + m * 32)), s);
     return s;
 }
 
-// Compact FP32 row: entries (value, range/offset byte); column =
-// start of range + offset.  Loads batched four at a time.
-template <bool SMEM>
+// Compact FP32 row: per group of four entries one 16-byte value word and one
+// 4-byte word of index bytes (2 bits: which of the row's three candidate
+// ranges, 6 bits: offset in it); the range starts are stored per row.
 __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf, int K, int row,
-                                                 const float* __restrict__ u, int lo) {
-    const int sl = row >> 5, lane = row & 31;
+                                                 const float* __restrict__ u) {
+    const int sl = row >> 5;
     const int w = __ldg(A.slice_w + sl);
-    const int32_t key = min(__ldg(mf.skey + row), mf.nkeys - 1);  // ghosts: sentinel nkeys
-    const int ix = key / mf.numY, iy = key - ix * mf.numY;
-    const int base0 = (ix - 1) * mf.numY + iy - 1;
-    const int s0 = __ldg(mf.cs + base0), s1 = __ldg(mf.cs + base0 + mf.numY),
-              s2 = __ldg(mf.cs + base0 + 2 * mf.numY);
-    const uint8_t* ip = mf.idx8 + (size_t)sl * K * 32 + lane;
-    const float* vp = A.val32 + (size_t)sl * K * 32 + lane;
+    const int s0 = __ldg(mf.rs + row), s1 = __ldg(mf.rs + mf.rs_stride + row),
+              s2 = __ldg(mf.rs + 2 * mf.rs_stride + row);
+    const size_t q0 = qsell_index(row, 0, K) >> 2;  // in 16-byte words
+    const float4* vp = reinterpret_cast<const float4*>(A.val32) + q0;
+    const uint32_t* ip = reinterpret_cast<const uint32_t*>(mf.idx8) + q0;
     float a0 = 0.f, a1 = 0.f;
-    int m = 0;
-    for (; m + 4 <= w; m += 4) {
-        int c[4];
-        float v[4], x[4];
+    const int groups = (w + 3) >> 2;
+    for (int g = 0; g < groups; g++) {
+        const float4 v = __ldg(vp + g * 32);
+        const uint32_t b4 = __ldg(ip + g * 32);
+        float x[4];
 #pragma unroll
         for (int t = 0; t < 4; t++) {
-            const int b = __ldg(ip + (m + t) * 32);
-            const int r = b >> 6;
-            c[t] = (r == 0 ? s0 : (r == 1 ? s1 : s2)) + (b & 63);
-            v[t] = __ldg(vp + (m + t) * 32);
+            const uint32_t b = (b4 >> (8 * t)) & 255u;
+            const uint32_t r = b >> 6;
+            x[t] = __ldcg(u + (r == 0 ? s0 : (r == 1 ? s1 : s2)) + (int)(b & 63u));
         }
-#pragma unroll
-        for (int t = 0; t < 4; t++) x[t] = ld_vec<SMEM>(u, c[t], lo);
-        a0 = fmaf(v[0], x[0], a0);
-        a1 = fmaf(v[1], x[1], a1);
-        a0 = fmaf(v[2], x[2], a0);
-        a1 = fmaf(v[3], x[3], a1);
-    }
-    for (; m < w; m++) {
-        const int b = __ldg(ip + m * 32);
-        const int r = b >> 6;
-        a0 = fmaf(__ldg(vp + m * 32), ld_vec<SMEM>(u, (r == 0 ? s0 : (r == 1 ? s1 : s2)) + (b & 63), lo), a0);
+        a0 = fmaf(v.x, x[0], a0);
+        a1 = fmaf(v.y, x[1], a1);
+        a0 = fmaf(v.z, x[2], a0);
+        a1 = fmaf(v.w, x[3], a1);
     }
     return a0 + a1;
 }
 
-// Shared-memory window of an operand for one chunk of BS consecutive rows.
-// Slots are sorted by cell key (x-major), so every neighbour of the chunk's
-// rows lies in the cells from (ix_first-1, iy_first-1) to (ix_last+1,
-// iy_last+1) of the chunk's first and last rows: one contiguous slot range.
-// The block copies that range into shared memory (coalesced) and the rows
-// gather from there instead of from L2.  Windows larger than `cap` entries
-// (and non-planar scenes, whose keys are 3-D) fall back to global gathers.
-struct Window {
-    const float* v;  // operand: shared window or the global array
-    int lo;          // first slot held by the window
-    bool smem;
-};
-
-template <int BS>
-__device__ __forceinline__ Window stage_window(const MatFree& mf, int n, int r0,
-                                               const float* __restrict__ v, float* win, int cap) {
-    __shared__ int s_lohi[2];
-    if (threadIdx.x == 0) {
-        int lo = 0, hi = 1 << 30;
-        if (mf.enabled && cap > 0) {
-            const int rl = min(r0 + BS, n) - 1;
-            int kf = __ldg(mf.skey + r0), kl = __ldg(mf.skey + rl);
-            kf = min(kf, mf.nkeys - 1);  // ghost slots carry the sentinel key nkeys
-            kl = min(kl, mf.nkeys - 1);
-            const int ixf = kf / mf.numY, iyf = kf - ixf * mf.numY;
-            const int ixl = kl / mf.numY, iyl = kl - ixl * mf.numY;
-            const int kmin = max((ixf - 1) * mf.numY + iyf - 1, 0);
-            const int kmax = min((ixl + 1) * mf.numY + iyl + 1, mf.nkeys - 1);
-            lo = __ldg(mf.cs + kmin);
-            hi = __ldg(mf.cs + kmax + 1);
-        }
-        s_lohi[0] = lo;
-        s_lohi[1] = hi;
-    }
-    __syncthreads();
-    const int lo = s_lohi[0], hi = s_lohi[1];
-    if (hi - lo > cap) return Window{v, 0, false};
-    for (int j = lo + (int)threadIdx.x; j < hi; j += BS) win[j - lo] = __ldcg(v + j);
-    __syncthreads();
-    return Window{win, lo, true};
-}
-
-// Off-diagonal part of row i of the FP32 operator applied to the window's operand.
+// Off-diagonal part of row i of the FP32 operator.
 __device__ __forceinline__ float off_row(const Ppe& A, const MatFree& mf, int K, int i,
-                                         const Window& w) {
-    const bool compact = mf.enabled && !mf.sell_row[i];
-    if (w.smem)
-        return compact ? compact_row_sum<true>(A, mf, K, i, w.v, w.lo)
-                       : spmv32_sell_row<true>(A, K, i, w.v, w.lo);
-    return compact ? compact_row_sum<false>(A, mf, K, i, w.v, 0)
-                   : spmv32_sell_row<false>(A, K, i, w.v, 0);
+                                         const float* __restrict__ v) {
+    return (mf.enabled && !mf.sell_row[i]) ? compact_row_sum(A, mf, K, i, v) : spmv32_sell_row(A, K, i, v);
 }
 
 // ----------------------------------------------------------------- FP64 CG
@@ -394,8 +330,8 @@ __device__ __forceinline__ double f2d(const F2& a) { return (double)a.hi + (doub
 
 // Level-0 operator row (FP32): diag_i v_i + off-diagonal sum.
 __device__ __forceinline__ float a0_row(const Ppe& A, const MatFree& mf, int K, int i,
-                                        const Window& w) {
-    return fmaf(A.diag32[i], w.smem ? w.v[i - w.lo] : __ldcg(w.v + i), off_row(A, mf, K, i, w));
+                                        const float* __restrict__ v) {
+    return fmaf(A.diag32[i], __ldcg(v + i), off_row(A, mf, K, i, v));
 }
 
 // 9-point stencil row of a structured level.
@@ -407,22 +343,57 @@ __device__ __forceinline__ float stencil_row(const MgLevel& L, int I, const floa
     for (int d = 0; d < 9; d++) {
         const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
         if (nx < 0 || ny < 0 || nx >= L.nx || ny >= L.ny) continue;
-        acc = fmaf(__ldcg(L.st + (size_t)d * n + I), __ldcg(v + nx * L.ny + ny), acc);
+        acc = fmaf(__ldg(L.st + (size_t)d * n + I), __ldcg(v + nx * L.ny + ny), acc);
     }
     return acc;
 }
 
-// residual of level l restricted to level l+1 (sum over the 2x2 children)
+// residual of level l restricted to level l+1 (sum over the 2x2 children).
+// The children's 4 x 9 loads are predicated, not branched around, so they
+// are all in flight together; stencils and inverse diagonals are read-only
+// during the solve (read-only cache), the vectors are not (L2).
 __device__ __forceinline__ float restrict_cell(const MgLevel& F, int X, int Y) {
-    float acc = 0.f;
-    for (int a = 0; a < 2; a++)
-        for (int b = 0; b < 2; b++) {
-            const int x = 2 * X + a, y = 2 * Y + b;
-            if (x >= F.nx || y >= F.ny) continue;
-            const int c = x * F.ny + y;
-            if (__ldcg(F.invd + c) > 0.f) acc += __ldcg(F.r + c) - stencil_row(F, c, F.e);
+    const int n = F.nx * F.ny;
+    float res[4];
+#pragma unroll
+    for (int ab = 0; ab < 4; ab++) {
+        const int x = 2 * X + (ab >> 1), y = 2 * Y + (ab & 1);
+        const bool in = x < F.nx && y < F.ny;
+        const int c = in ? x * F.ny + y : 0;
+        const bool act = in && __ldg(F.invd + c) > 0.f;
+        float s = 0.f;
+#pragma unroll
+        for (int d = 0; d < 9; d++) {
+            const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
+            if (act && nx >= 0 && ny >= 0 && nx < F.nx && ny < F.ny)
+                s = fmaf(__ldg(F.st + (size_t)d * n + c), __ldcg(F.e + nx * F.ny + ny), s);
         }
+        res[ab] = act ? __ldcg(F.r + c) - s : 0.f;
+    }
+    // the children in the order (0,0), (0,1), (1,0), (1,1)
+    float acc = 0.f;
+#pragma unroll
+    for (int ab = 0; ab < 4; ab++) acc += res[ab];
     return acc;
+}
+
+// Post-smoothing of a grid level with the prolongation folded in: the
+// corrected value of a cell is e + s * e_parent, computed on the fly for the
+// cell and its 8 neighbours, so prolongation needs no barrier of its own.
+__device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, const MgLevel& C,
+                                                int I) {
+    const int n = L.nx * L.ny;
+    const int x = I / L.ny, y = I - x * L.ny;
+    const float ei = fmaf(mg.scale, __ldcg(C.e + (x / 2) * C.ny + y / 2), __ldcg(L.e + I));
+    float acc = 0.f;
+#pragma unroll
+    for (int d = 0; d < 9; d++) {
+        const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
+        if (nx < 0 || ny < 0 || nx >= L.nx || ny >= L.ny) continue;
+        const float ej = fmaf(mg.scale, __ldcg(C.e + (nx / 2) * C.ny + ny / 2), __ldcg(L.e + nx * L.ny + ny));
+        acc = fmaf(__ldg(L.st + (size_t)d * n + I), ej, acc);
+    }
+    return fmaf(mg.omega * __ldg(L.invd + I), __ldcg(L.r + I) - acc, ei);
 }
 
 // Levels lo..hi of the V-cycle run by block 0 alone (they are small): down
@@ -434,7 +405,7 @@ __device__ void mg_block_cycle(Mg& mg, int lo) {
     for (int l = lo; l < mg.nlev; l++) {
         MgLevel& L = mg.lev[l];
         const int n = L.nx * L.ny;
-        for (int I = tid; I < n; I += nt) L.e[I] = mg.omega * L.invd[I] * __ldcg(L.r + I);
+        for (int I = tid; I < n; I += nt) L.e[I] = mg.omega * __ldg(L.invd + I) * __ldcg(L.r + I);
         __syncthreads();
         MgLevel& C = mg.lev[l + 1];
         for (int I = tid; I < C.nx * C.ny; I += nt) {
@@ -461,40 +432,20 @@ __device__ void mg_block_cycle(Mg& mg, int lo) {
         MgLevel& L = mg.lev[l];
         MgLevel& C = mg.lev[l + 1];
         const int n = L.nx * L.ny;
-        for (int I = tid; I < n; I += nt) {
-            if (!(L.invd[I] > 0.f)) continue;
-            const int x = I / L.ny, y = I - x * L.ny;
-            L.e[I] = fmaf(mg.scale, __ldcg(C.e + (x / 2) * C.ny + y / 2), __ldcg(L.e + I));
+        // prolongation folded into the post-smoothing
+        for (int I = tid; I < n; I += nt) L.t[I] = __ldg(L.invd + I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
+        __syncthreads();
+        if (l > lo) {
+            // only this block ever touches level l: swap its own pointers
+            float* tmp = L.e;
+            L.e = L.t;
+            L.t = tmp;
+        } else {
+            // level lo is read by every block afterwards: copy back
+            for (int I = tid; I < n; I += nt) L.e[I] = __ldcg(L.t + I);
+            __syncthreads();
         }
-        __syncthreads();
-        for (int I = tid; I < n; I += nt) {
-            const float iv = L.invd[I];
-            L.t[I] = iv > 0.f ? fmaf(mg.omega * iv, __ldcg(L.r + I) - stencil_row(L, I, L.e), __ldcg(L.e + I)) : 0.f;
-        }
-        __syncthreads();
-        // copy back (no pointer swap: the other blocks keep the same pointers)
-        for (int I = tid; I < n; I += nt) L.e[I] = __ldcg(L.t + I);
-        __syncthreads();
     }
-}
-
-// Post-smoothing of a grid level with the prolongation folded in: the
-// corrected value of a cell is e + s * e_parent, computed on the fly for the
-// cell and its 8 neighbours, so prolongation needs no barrier of its own.
-__device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, const MgLevel& C,
-                                                int I) {
-    const int n = L.nx * L.ny;
-    const int x = I / L.ny, y = I - x * L.ny;
-    const float ei = fmaf(mg.scale, __ldcg(C.e + (x / 2) * C.ny + y / 2), __ldcg(L.e + I));
-    float acc = 0.f;
-#pragma unroll
-    for (int d = 0; d < 9; d++) {
-        const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
-        if (nx < 0 || ny < 0 || nx >= L.nx || ny >= L.ny) continue;
-        const float ej = fmaf(mg.scale, __ldcg(C.e + (nx / 2) * C.ny + ny / 2), __ldcg(L.e + nx * L.ny + ny));
-        acc = fmaf(__ldcg(L.st + (size_t)d * n + I), ej, acc);
-    }
-    return fmaf(mg.omega * __ldcg(L.invd + I), __ldcg(L.r + I) - acc, ei);
 }
 
 // u = M r: one symmetric V(1,1) cycle with damped Jacobi smoothing.  The
@@ -505,17 +456,12 @@ __device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, 
 template <int BS>
 __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& mf, int K,
                                           const float* __restrict__ r, float* __restrict__ u,
-                                          int n, GridBar& gb, DevStats* ds, float* win, int cap) {
+                                          int n, GridBar& gb, DevStats* ds) {
     const int gtid = gb.rank * BS + threadIdx.x;
     const int gsz = gb.size * BS;
-    // level 0 residual of the Inner particles (one row per thread, chunks of
-    // BS rows with their e0 window in shared memory)
-    for (int base = gb.rank * BS; base < n; base += gsz) {
-        const Window w = stage_window<BS>(mf, n, base, mg.e0, win, cap);
-        const int i = base + threadIdx.x;
-        if (i < n) mg.res0[i] = A.diag32[i] > 0.f ? __ldcg(r + i) - a0_row(A, mf, K, i, w) : 0.f;
-        __syncthreads();
-    }
+    // level 0 residual of the Inner particles (coalesced, one row per thread)
+    for (int i = gtid; i < n; i += gsz)
+        mg.res0[i] = A.diag32[i] > 0.f ? __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0) : 0.f;
     if (!grid_sync(gb, ds)) return false;
     // level 1: sum over each cell's contiguous slots; pre-smooth
     {
@@ -565,15 +511,10 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
                 mg.e0[i] = fmaf(mg.scale, __ldcg(L1.e + __ldg(mf.skey + i)), __ldcg(mg.e0 + i));
     }
     if (!grid_sync(gb, ds)) return false;
-    for (int base = gb.rank * BS; base < n; base += gsz) {
-        const Window w = stage_window<BS>(mf, n, base, mg.e0, win, cap);
-        const int i = base + threadIdx.x;
-        if (i < n) {
-            const float dg = A.diag32[i];
-            u[i] = dg > 0.f ? fmaf(mg.omega / dg, __ldcg(r + i) - a0_row(A, mf, K, i, w), __ldcg(mg.e0 + i))
-                            : 0.f;
-        }
-        __syncthreads();
+    for (int i = gtid; i < n; i += gsz) {
+        const float dg = A.diag32[i];
+        u[i] = dg > 0.f ? fmaf(mg.omega / dg, __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0), __ldcg(mg.e0 + i))
+                        : 0.f;
     }
     return true;
 }
@@ -583,7 +524,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
 template <int BS>
 __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg& mg,
                                             const Krylov& kv, const SolveArgs& a, DevStats* ds,
-                                            GridBar& gb, float* win) {
+                                            GridBar& gb) {
     const int gtid = gb.rank * BS + threadIdx.x;
     const int gsz = gb.size * BS;
     const int lane = threadIdx.x & 31;
@@ -636,7 +577,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
         }
         if (!grid_sync(gb, ds)) return;
         if (mg.enabled) {
-            if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds, win, a.win_cap)) return;
+            if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds)) return;
             if (!grid_sync(gb, ds)) return;
         }
         float alpha = 0.f, beta = 0.f, gamma_old = 1.f;
@@ -644,22 +585,17 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
         for (;;) {
             // phase B: w = A u ; gamma = r.u, delta = w.u, rho = r.r
             F2 g = {0.f, 0.f}, dl = {0.f, 0.f}, rr = {0.f, 0.f};
-            for (int base = gb.rank * BS; base < a.n; base += gsz) {
-                const Window win_u = stage_window<BS>(mf, a.n, base, kv.u32, win, a.win_cap);
-                const int i = base + threadIdx.x;
-                if (i < a.n) {
-                    // rows that are not unknowns (diagonal 0: Surface, Ignored,
-                    // ghosts) have only zero entries: w = +0 without the gathers
-                    const float ui = __ldcg(kv.u32 + i);
-                    const float dg = A.diag32[i];
-                    const float w = dg > 0.f ? fmaf(dg, ui, off_row(A, mf, a.K, i, win_u)) : 0.f;
-                    kv.w32[i] = w;
-                    const float r = kv.r32[i];
-                    acc_prod(g, r, ui);
-                    acc_prod(dl, w, ui);
-                    acc_prod(rr, r, r);
-                }
-                __syncthreads();
+            for (int i = gtid; i < a.n; i += gsz) {
+                // rows that are not unknowns (diagonal 0: Surface, Ignored,
+                // ghosts) have only zero entries: w = +0 without the gathers
+                const float ui = __ldcg(kv.u32 + i);
+                const float dg = A.diag32[i];
+                const float w = dg > 0.f ? fmaf(dg, ui, off_row(A, mf, a.K, i, kv.u32)) : 0.f;
+                kv.w32[i] = w;
+                const float r = kv.r32[i];
+                acc_prod(g, r, ui);
+                acc_prod(dl, w, ui);
+                acc_prod(rr, r, r);
             }
             double v3[3] = {f2d(g), f2d(dl), f2d(rr)}, t3[3];
             if (!reduce_sync<3, BS>(gb, v3, t3, ds)) return;
@@ -693,7 +629,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
             k++;
             if (!grid_sync(gb, ds)) return;
             if (mg.enabled) {
-                if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds, win, a.win_cap)) return;
+                if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds)) return;
                 if (!grid_sync(gb, ds)) return;
             }
         }
@@ -712,9 +648,8 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
 
 __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg, Krylov kv,
                                                         SolveArgs a, DevStats* ds) {
-    extern __shared__ float s_win[];
     GridBar gb = whole_grid(kv);
-    solve_mixed<kBlock>(A, mf, mg, kv, a, ds, gb, s_win);
+    solve_mixed<kBlock>(A, mf, mg, kv, a, ds, gb);
 }
 
 // Many scenes in one persistent launch: block b belongs to group bmap[b].x
@@ -733,16 +668,17 @@ __global__ void __launch_bounds__(BS, MINB) k_cg_mixed_batched(const SceneSolve*
                                                                const int2* __restrict__ bmap,
                                                                const int32_t* __restrict__ gsize,
                                                                unsigned int* bars) {
-    extern __shared__ float s_win[];
     const int2 m = bmap[blockIdx.x];
     SceneSolve s = scenes[m.x];
     GridBar gb{bars + 32 * m.x, 0u, 0, m.y, gsize[m.x], s.kv.partials};
-    solve_mixed<BS>(s.A, s.mf, s.mg, s.kv, s.a, s.ds, gb, s_win);
+    solve_mixed<BS>(s.A, s.mf, s.mg, s.kv, s.a, s.ds, gb);
 }
 
-// Mixed-solver setup: FP32 values of the matrix, their compact index bytes,
-// FP32 diagonal and inverse diagonal.  A row whose column lies 64 or more
-// slots into its range keeps the int32 columns (sell_row = 1).
+// Mixed-solver setup: FP32 values of the matrix and their compact index
+// bytes (quad layout, padded to a multiple of four entries with value 0 and
+// index 0), the row's three range starts, FP32 diagonal and inverse
+// diagonal.  A row whose column lies 64 or more slots into its range keeps
+// the int32 columns (sell_row = 1).
 __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.n) return;
@@ -751,6 +687,7 @@ __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
     kv.inv_diag32[k] = d != 0.0 ? (float)(1.0 / d) : 1.f;
     const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
     const int w = A.slice_w[k >> 5];
+    const int wq = (w + 3) & ~3;
     int8_t sell = 1;
     if (mf.enabled) {
         sell = 0;
@@ -760,8 +697,9 @@ __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
             const int ix = key / c.numY, iy = key - ix * c.numY;
             for (int r = 0; r < 3; r++) st[r] = mf.cs[(ix - 1 + r) * c.numY + iy - 1];
         }
+        for (int r = 0; r < 3; r++) mf.rs[(size_t)r * mf.rs_stride + k] = st[r];
         const int cnt = A.offcnt[k];
-        for (int m = 0; m < w; m++) {
+        for (int m = 0; m < wq; m++) {
             uint8_t b = 0;  // padding: range 0, offset 0, value 0
             if (m < cnt) {
                 const int j = A.col[base + (size_t)m * 32];
@@ -773,15 +711,13 @@ __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
                 else
                     sell = 1;
             }
-            mf.idx8[base + (size_t)m * 32] = b;
+            mf.idx8[qsell_index(k, m, c.K)] = b;
         }
     }
     mf.sell_row[k] = sell;
-    for (int m = 0; m < w; m++) A.val32[base + (size_t)m * 32] = (float)A.val[base + (size_t)m * 32];
+    for (int m = 0; m < wq; m++)
+        A.val32[qsell_index(k, m, c.K)] = m < w ? (float)A.val[base + (size_t)m * 32] : 0.f;
 }
-
-// Shared-memory operand window of the mixed solver: 8 floats per thread.
-constexpr int win_cap_for(int bs) { return 8 * bs; }
 
 // Co-resident blocks of a persistent kernel (0 if the configuration does not
 // fit, which the launchers report instead of launching).  Kernels with a
@@ -806,7 +742,6 @@ SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
     a.max_iter = max_iter;
     a.inner_tol = 1e-6;  // FP32 floor of an inner solve's residual reduction
     a.max_refine = 40;
-    a.win_cap = 0;
     return a;
 }
 
@@ -814,7 +749,7 @@ SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
 
 void solver_setup(Krylov& k, int32_t /*n_pad*/, int device) {
     int g1 = coop_grid((const void*)k_cg64, device, kBlock, 0, 1);
-    int g2 = coop_grid((const void*)k_cg_mixed, device, kBlock, sizeof(float) * win_cap_for(kBlock), 1);
+    int g2 = coop_grid((const void*)k_cg_mixed, device, kBlock, 0, 1);
     k.grid = g1 < g2 ? g1 : g2;
     k.block = kBlock;
 }
@@ -844,8 +779,7 @@ void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double to
 namespace {
 template <int BS, int MINB>
 int resident_grid(int device) {
-    return coop_grid((const void*)k_cg_mixed_batched<BS, MINB>, device, BS,
-                     sizeof(float) * win_cap_for(BS), MINB);
+    return coop_grid((const void*)k_cg_mixed_batched<BS, MINB>, device, BS, 0, MINB);
 }
 }  // namespace
 
@@ -899,7 +833,6 @@ int batch_solve_setup(const std::vector<BatchScene>& scenes, int block, double a
     for (int s = 0; s < ns; s++) {
         const BatchScene& q = scenes[s];
         hs[s] = SceneSolve{q.A, q.mf, q.mg, q.kv, make_args(q.c, q.tol, q.max_iter), q.ds};
-        hs[s].a.win_cap = win_cap_for(block);
         for (int r = 0; r < gs[s]; r++) bmap.push_back(make_int2(s, r));
     }
     if (cudaMalloc(&b.scenes, sizeof(SceneSolve) * ns) != cudaSuccess ||
@@ -938,8 +871,7 @@ void launch_solve_mixed_batched(const BatchSolve& b, cudaStream_t st) {
     const void* fn = b.block == 256   ? (const void*)k_cg_mixed_batched<256, 4>
                      : b.block == 512 ? (const void*)k_cg_mixed_batched<512, 2>
                                       : (const void*)k_cg_mixed_batched<1024, 1>;
-    cudaLaunchCooperativeKernel(fn, dim3(b.grid), dim3(b.block), args,
-                                sizeof(float) * win_cap_for(b.block), st);
+    cudaLaunchCooperativeKernel(fn, dim3(b.grid), dim3(b.block), args, 0, st);
     ++g_launches;
 }
 
@@ -947,15 +879,13 @@ void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const 
                         const Krylov& k, double tol, int64_t max_iter, DevStats* ds,
                         cudaStream_t st) {
     SolveArgs a = make_args(c, tol, max_iter);
-    a.win_cap = win_cap_for(kBlock);
     Ppe AA = A;
     MatFree mm = mf;
     Mg gg = mg;
     Krylov kk = k;
     void* args[] = {&AA, &mm, &gg, &kk, &a, &ds};
     cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
-    cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kBlock), args,
-                                sizeof(float) * a.win_cap, st);
+    cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kBlock), args, 0, st);
     ++g_launches;
 }
 
