@@ -192,7 +192,13 @@ __device__ __forceinline__ float spmv32_sell_row(const Ppe& A, int K, int row,
 
 // Compact FP32 row: per group of four entries one 16-byte value word and one
 // 4-byte word of index bytes (2 bits: which of the row's three candidate
-// ranges, 6 bits: offset in it); the range starts are stored per row.
+// ranges, 6 bits: offset in it); the range starts are stored per row.  The
+// loads of kGroups groups are issued before any of their gathers and those
+// before the multiply-adds, so that a warp keeps several groups' memory
+// traffic in flight (a warp issues in order: it stalls at the first use of
+// a load).  Summation order is per group (a0: entries 0, 2; a1: 1, 3), the
+// same for any kGroups.
+constexpr int kGroups = 2;
 __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf, int K, int row,
                                                  const float* __restrict__ u) {
     const int sl = row >> 5;
@@ -202,18 +208,41 @@ __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf
     const size_t q0 = qsell_index(row, 0, K) >> 2;  // in 16-byte words
     const float4* vp = reinterpret_cast<const float4*>(A.val32) + q0;
     const uint32_t* ip = reinterpret_cast<const uint32_t*>(mf.idx8) + q0;
+    auto col = [&](uint32_t b4, int t) {
+        const uint32_t b = (b4 >> (8 * t)) & 255u;
+        const uint32_t r = b >> 6;
+        return (r == 0 ? s0 : (r == 1 ? s1 : s2)) + (int)(b & 63u);
+    };
     float a0 = 0.f, a1 = 0.f;
     const int groups = (w + 3) >> 2;
-    for (int g = 0; g < groups; g++) {
+    int g = 0;
+    for (; g + kGroups <= groups; g += kGroups) {
+        float4 v[kGroups];
+        uint32_t b4[kGroups];
+#pragma unroll
+        for (int q = 0; q < kGroups; q++) {
+            v[q] = __ldg(vp + (g + q) * 32);
+            b4[q] = __ldg(ip + (g + q) * 32);
+        }
+        float x[kGroups][4];
+#pragma unroll
+        for (int q = 0; q < kGroups; q++)
+#pragma unroll
+            for (int t = 0; t < 4; t++) x[q][t] = __ldcg(u + col(b4[q], t));
+#pragma unroll
+        for (int q = 0; q < kGroups; q++) {
+            a0 = fmaf(v[q].x, x[q][0], a0);
+            a1 = fmaf(v[q].y, x[q][1], a1);
+            a0 = fmaf(v[q].z, x[q][2], a0);
+            a1 = fmaf(v[q].w, x[q][3], a1);
+        }
+    }
+    for (; g < groups; g++) {
         const float4 v = __ldg(vp + g * 32);
         const uint32_t b4 = __ldg(ip + g * 32);
         float x[4];
 #pragma unroll
-        for (int t = 0; t < 4; t++) {
-            const uint32_t b = (b4 >> (8 * t)) & 255u;
-            const uint32_t r = b >> 6;
-            x[t] = __ldcg(u + (r == 0 ? s0 : (r == 1 ? s1 : s2)) + (int)(b & 63u));
-        }
+        for (int t = 0; t < 4; t++) x[t] = __ldcg(u + col(b4, t));
         a0 = fmaf(v.x, x[0], a0);
         a1 = fmaf(v.y, x[1], a1);
         a0 = fmaf(v.z, x[2], a0);
@@ -334,6 +363,11 @@ __device__ __forceinline__ float a0_row(const Ppe& A, const MatFree& mf, int K, 
     return fmaf(A.diag32[i], __ldcg(v + i), off_row(A, mf, K, i, v));
 }
 
+// Loads of multigrid data: the vectors change during the solve (L2), the
+// stencils and inverse diagonals do not (read-only cache).
+__device__ __forceinline__ float ldv(const float* p, int i) { return __ldcg(p + i); }
+__device__ __forceinline__ float ldc(const float* p, size_t i) { return __ldg(p + i); }
+
 // 9-point stencil row of a structured level.
 __device__ __forceinline__ float stencil_row(const MgLevel& L, int I, const float* __restrict__ v) {
     const int n = L.nx * L.ny;
@@ -350,8 +384,9 @@ __device__ __forceinline__ float stencil_row(const MgLevel& L, int I, const floa
 
 // residual of level l restricted to level l+1 (sum over the 2x2 children).
 // The children's 4 x 9 loads are predicated, not branched around, so they
-// are all in flight together; stencils and inverse diagonals are read-only
-// during the solve (read-only cache), the vectors are not (L2).
+// are all in flight together.  Callers skip coarse cells without unknowns
+// (their children have none either: the Galerkin diagonal of an aggregate
+// with an unknown is positive).
 __device__ __forceinline__ float restrict_cell(const MgLevel& F, int X, int Y) {
     const int n = F.nx * F.ny;
     float res[4];
@@ -360,15 +395,15 @@ __device__ __forceinline__ float restrict_cell(const MgLevel& F, int X, int Y) {
         const int x = 2 * X + (ab >> 1), y = 2 * Y + (ab & 1);
         const bool in = x < F.nx && y < F.ny;
         const int c = in ? x * F.ny + y : 0;
-        const bool act = in && __ldg(F.invd + c) > 0.f;
+        const bool act = in && ldc(F.invd, c) > 0.f;
         float s = 0.f;
 #pragma unroll
         for (int d = 0; d < 9; d++) {
             const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
             if (act && nx >= 0 && ny >= 0 && nx < F.nx && ny < F.ny)
-                s = fmaf(__ldg(F.st + (size_t)d * n + c), __ldcg(F.e + nx * F.ny + ny), s);
+                s = fmaf(ldc(F.st, (size_t)d * n + c), ldv(F.e, nx * F.ny + ny), s);
         }
-        res[ab] = act ? __ldcg(F.r + c) - s : 0.f;
+        res[ab] = act ? ldv(F.r, c) - s : 0.f;
     }
     // the children in the order (0,0), (0,1), (1,0), (1,1)
     float acc = 0.f;
@@ -377,74 +412,86 @@ __device__ __forceinline__ float restrict_cell(const MgLevel& F, int X, int Y) {
     return acc;
 }
 
-// Post-smoothing of a grid level with the prolongation folded in: the
-// corrected value of a cell is e + s * e_parent, computed on the fly for the
-// cell and its 8 neighbours, so prolongation needs no barrier of its own.
+// Post-smoothing of a level with the prolongation folded in: the corrected
+// value of a cell is e + s * e_parent, computed on the fly for the cell and
+// its 8 neighbours, so prolongation needs no pass or barrier of its own.
 __device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, const MgLevel& C,
                                                 int I) {
     const int n = L.nx * L.ny;
     const int x = I / L.ny, y = I - x * L.ny;
-    const float ei = fmaf(mg.scale, __ldcg(C.e + (x / 2) * C.ny + y / 2), __ldcg(L.e + I));
+    const float ei = fmaf(mg.scale, ldv(C.e, (x / 2) * C.ny + y / 2), ldv(L.e, I));
     float acc = 0.f;
 #pragma unroll
     for (int d = 0; d < 9; d++) {
         const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
         if (nx < 0 || ny < 0 || nx >= L.nx || ny >= L.ny) continue;
-        const float ej = fmaf(mg.scale, __ldcg(C.e + (nx / 2) * C.ny + ny / 2), __ldcg(L.e + nx * L.ny + ny));
-        acc = fmaf(__ldg(L.st + (size_t)d * n + I), ej, acc);
+        const float ej = fmaf(mg.scale, ldv(C.e, (nx / 2) * C.ny + ny / 2), ldv(L.e, nx * L.ny + ny));
+        acc = fmaf(ldc(L.st, (size_t)d * n + I), ej, acc);
     }
-    return fmaf(mg.omega * __ldg(L.invd + I), __ldcg(L.r + I) - acc, ei);
+    return fmaf(mg.omega * ldc(L.invd, I), ldv(L.r, I) - acc, ei);
 }
 
-// Levels lo..hi of the V-cycle run by block 0 alone (they are small): down
-// smoothing + restriction, the dense coarsest solve, prolongation + up
-// smoothing.  Only __syncthreads inside; the caller brackets it with grid
-// barriers.
-__device__ void mg_block_cycle(Mg& mg, int lo) {
+// Levels lo..nlev of the V-cycle, run by the group's first block alone (they
+// are small): down smoothing + restriction, the dense coarsest solve, up
+// smoothing with the prolongation folded in.  Only __syncthreads inside; the
+// caller brackets it with grid barriers.  `lv` are this block's views of the
+// levels (their e/t roles swap after each up-smoothing).
+__device__ void mg_block_levels(const Mg& mg, int lo, MgLevel* lv) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int l = lo; l < mg.nlev; l++) {
-        MgLevel& L = mg.lev[l];
+        MgLevel& L = lv[l];
         const int n = L.nx * L.ny;
-        for (int I = tid; I < n; I += nt) L.e[I] = mg.omega * __ldg(L.invd + I) * __ldcg(L.r + I);
+        for (int I = tid; I < n; I += nt) L.e[I] = mg.omega * ldc(L.invd, I) * ldv(L.r, I);
         __syncthreads();
-        MgLevel& C = mg.lev[l + 1];
+        MgLevel& C = lv[l + 1];
         for (int I = tid; I < C.nx * C.ny; I += nt) {
             const int X = I / C.ny, Y = I - X * C.ny;
-            C.r[I] = restrict_cell(L, X, Y);
+            C.r[I] = ldc(C.invd, I) > 0.f ? restrict_cell(L, X, Y) : 0.f;
         }
         __syncthreads();
     }
     {
         // coarsest level: e = A_c^-1 r, one warp per row (lanes split the row)
-        MgLevel& L = mg.lev[mg.nlev];
+        MgLevel& L = lv[mg.nlev];
         const int n = L.nx * L.ny;
         const int lane = tid & 31;
         for (int i = tid >> 5; i < n; i += nt >> 5) {
             float acc = 0.f;
-            for (int j = lane; j < n; j += 32) acc = fmaf(__ldg(mg.dense + i * n + j), __ldcg(L.r + j), acc);
+            for (int j = lane; j < n; j += 32) acc = fmaf(__ldg(mg.dense + i * n + j), ldv(L.r, j), acc);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) L.e[i] = __ldg(L.invd + i) > 0.f ? acc : 0.f;
+            if (lane == 0) L.e[i] = ldc(L.invd, i) > 0.f ? acc : 0.f;
         }
         __syncthreads();
     }
     for (int l = mg.nlev - 1; l >= lo; l--) {
-        MgLevel& L = mg.lev[l];
-        MgLevel& C = mg.lev[l + 1];
+        MgLevel& L = lv[l];
+        MgLevel& C = lv[l + 1];
         const int n = L.nx * L.ny;
-        // prolongation folded into the post-smoothing
-        for (int I = tid; I < n; I += nt) L.t[I] = __ldg(L.invd + I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
+        for (int I = tid; I < n; I += nt) L.t[I] = ldc(L.invd, I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
         __syncthreads();
-        if (l > lo) {
-            // only this block ever touches level l: swap its own pointers
-            float* tmp = L.e;
-            L.e = L.t;
-            L.t = tmp;
-        } else {
-            // level lo is read by every block afterwards: copy back
-            for (int I = tid; I < n; I += nt) L.e[I] = __ldcg(L.t + I);
-            __syncthreads();
-        }
+        // the views are this block's own: swap instead of copying
+        float* tmp = L.e;
+        L.e = L.t;
+        L.t = tmp;
+    }
+}
+
+__device__ void mg_block_cycle(Mg& mg, int lo) {
+    const int tid = threadIdx.x;
+    MgLevel v[kMgMaxLevels];
+    for (int l = lo; l <= mg.nlev; l++) v[l] = mg.lev[l];
+    mg_block_levels(mg, lo, v);
+    // after the swap level lo's correction sits in its t array: copy it to
+    // e, where every block reads it
+    const int nlo = v[lo].nx * v[lo].ny;
+    if (v[lo].e != mg.lev[lo].e)
+        for (int i = tid; i < nlo; i += blockDim.x) mg.lev[lo].e[i] = __ldcg(v[lo].e + i);
+    __syncthreads();
+    // levels above lo keep their swapped roles in this block's copy
+    for (int l = lo + 1; l <= mg.nlev; l++) {
+        mg.lev[l].e = v[l].e;
+        mg.lev[l].t = v[l].t;
     }
 }
 
@@ -483,9 +530,10 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         const bool smooth = l + 1 <= mg.ngrid;
         for (int I = gtid; I < C.nx * C.ny; I += gsz) {
             const int X = I / C.ny, Y = I - X * C.ny;
-            const float rr = restrict_cell(L, X, Y);
+            const float iv = __ldg(C.invd + I);
+            const float rr = iv > 0.f ? restrict_cell(L, X, Y) : 0.f;
             C.r[I] = rr;
-            if (smooth) C.e[I] = mg.omega * __ldg(C.invd + I) * rr;
+            if (smooth) C.e[I] = mg.omega * iv * rr;
         }
         if (!grid_sync(gb, ds)) return false;
     }
@@ -720,12 +768,15 @@ __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
 }
 
 // Co-resident blocks of a persistent kernel (0 if the configuration does not
-// fit, which the launchers report instead of launching).  Kernels with a
-// dynamic shared window opt in to more than the default 48 KB first.
+// fit, which the launchers report instead of launching).  A kernel that asks
+// for dynamic shared memory opts in to it first.
 int coop_grid(const void* fn, int device, int block, size_t smem, int max_per_sm) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (smem > 0) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the solvers stream their operators through L1: keep the shared-memory
+    // carve-out at what their static arrays need
+    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxL1);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, smem) != cudaSuccess) {
         cudaGetLastError();
         per = 0;

@@ -25,6 +25,34 @@ __device__ __forceinline__ bool outside_domain(const Consts& c, double x, double
            c.dmax[2] < z;
 }
 
+// Visits, in sweep order, the candidates of particle k that survive the FP32
+// pre-filter at `bound`: pass 1 collects them in a local list, pass 2 calls
+// f(j), where f runs the exact FP64 test and the work.  Splitting the sweep
+// keeps the FP64 work on compact lists, with nearly all lanes of a warp busy.
+// More survivors than the list holds: f(j) for every candidate (f's exact
+// test then selects the same neighbours in the same order).
+constexpr int kNear = 64;
+template <bool PLANAR, class F>
+__device__ __forceinline__ void for_each_near(const Consts& c, const StateBuf& s,
+                                              const int32_t* __restrict__ cs, int32_t key, int k,
+                                              float bound, F&& f) {
+    const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
+    int cand[kNear];
+    int ns = 0;
+    for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
+        if (j == k || far32<PLANAR>(s, j, fx, fy, fz, bound)) return;
+        if (ns < kNear) cand[ns] = j;
+        ns++;
+    });
+    if (ns <= kNear) {
+        for (int q = 0; q < ns; q++) f(cand[q]);
+    } else {
+        for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
+            if (j != k) f(j);
+        });
+    }
+}
+
 // Number density at re_p over a particle's current neighbours (d < re_max),
 // in sweep order: the value a later setNumberDensity reads from the stale
 // list of a particle that has just become a ghost (src/mps.cpp:590-593).
@@ -59,12 +87,10 @@ __global__ void __launch_bounds__(kThreads) k_explicit(Consts c, StateBuf in, St
     double nd_last = in.nd_last[k];
     if (t == T_FLUID) {
         const int32_t key = skey[k];
-        const float fx = in.xf[k], fy = in.yf[k], fz = PLANAR ? 0.f : in.zf[k];
         double ax, ay, az;
         if (!MIXED) {
             double tx = 0.0, ty = 0.0, tz = 0.0;
-            for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
-                if (j == k || far32<PLANAR>(in, j, fx, fy, fz, c.ft_v)) return;
+            for_each_near<PLANAR>(c, in, cs, key, k, c.ft_v, [&](int j) {
                 double d2 = dist2<PLANAR>(in, k, j, x, y, z);
                 if (d2 < c.t_max && d2 < c.t_v) {
                     double w = weight(dsqrt(d2), c.re_v);
@@ -81,8 +107,7 @@ __global__ void __launch_bounds__(kThreads) k_explicit(Consts c, StateBuf in, St
             // exact FP64 one.
             float tx = 0.f, ty = 0.f, tz = 0.f;
             const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
-            for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
-                if (j == k || far32<PLANAR>(in, j, fx, fy, fz, c.ft_v)) return;
+            for_each_near<PLANAR>(c, in, cs, key, k, c.ft_v, [&](int j) {
                 double d2 = dist2<PLANAR>(in, k, j, x, y, z);
                 if (d2 < c.t_max && d2 < c.t_v) {
                     float w = c.fre_v * rsqrtf((float)d2) - 1.f;
@@ -246,35 +271,64 @@ __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
                                                          const int32_t* __restrict__ skey,
                                                          const int32_t* __restrict__ cs, NbList nb,
                                                          DevStats* ds) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= c.n) return;
-    if (s.type[k] == T_GHOST) {
-        nb.cnt[k] = 0;
-        return;
-    }
-    double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
-    const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
-    double nd = 0.0;
-    int m = 0;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = k < c.n && s.type[k] != T_GHOST;
     const int np = nb.n_pad;
-    for_each_candidate<PLANAR>(c, cs, skey[k], [&](int j) {
-        if (j == k || far32<PLANAR>(s, j, fx, fy, fz, c.ft_max)) return;
-        double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
-        if (!(d2 < c.t_max)) return;
-        double dist = dsqrt(d2);
-        double w = weight(dist, c.re_p);
-        if (dist < c.re_p) nd = dadd(nd, w);
-        if (m < c.K) {
-            nb.slot[(size_t)m * np + k] = j;
-            nb.dist[(size_t)m * np + k] = dist;
-            nb.wp[(size_t)m * np + k] = w;
+    int m = 0;
+    if (valid) {
+        const double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
+        const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
+        // Pass 1: the candidates that survive the FP32 pre-filter, in sweep
+        // order.  Pass 2 then runs the exact FP64 test, square root and
+        // division on these compact per-particle lists, with nearly all lanes
+        // of a warp busy (a candidate survives for only part of a warp).
+        int ns = 0;
+        for_each_candidate<PLANAR>(c, cs, skey[k], [&](int j) {
+            if (j == k || far32<PLANAR>(s, j, fx, fy, fz, c.ft_max)) return;
+            if (ns < c.K) nb.slot[(size_t)ns * np + k] = j;
+            ns++;
+        });
+        double nd = 0.0;
+        if (ns <= c.K) {
+            // exact test, compacting in place (order kept): src/mps.cpp:585-619
+            for (int q = 0; q < ns; q++) {
+                const int j = nb.slot[(size_t)q * np + k];
+                const double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
+                if (!(d2 < c.t_max)) continue;
+                const double dist = dsqrt(d2);
+                const double w = weight(dist, c.re_p);
+                if (dist < c.re_p) nd = dadd(nd, w);  // src/mps.cpp:573-583
+                const size_t e = (size_t)m * np + k;
+                nb.slot[e] = j;
+                nb.dist[e] = dist;
+                nb.wp[e] = w;
+                m++;
+            }
+        } else {
+            // more survivors than the list holds: the exact one-pass sweep
+            for_each_candidate<PLANAR>(c, cs, skey[k], [&](int j) {
+                if (j == k) return;
+                const double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
+                if (!(d2 < c.t_max)) return;
+                const double dist = dsqrt(d2);
+                const double w = weight(dist, c.re_p);
+                if (dist < c.re_p) nd = dadd(nd, w);
+                if (m < c.K) {
+                    const size_t e = (size_t)m * np + k;
+                    nb.slot[e] = j;
+                    nb.dist[e] = dist;
+                    nb.wp[e] = w;
+                }
+                m++;
+            });
         }
-        m++;
-    });
+        s.nd_last[k] = nd;
+    }
+    if (k < c.n) nb.cnt[k] = m < c.K ? m : c.K;
     if (m > c.K) raise_status(ds, ST_CAPACITY);
-    atomicMax(&ds->max_neighbors, m);
-    nb.cnt[k] = m < c.K ? m : c.K;
-    s.nd_last[k] = nd;
+    // one atomic per warp for the largest neighbour count
+    const int wmax = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(&ds->max_neighbors, wmax);
 }
 
 // setBoundaryCondition + setSourceTerm (classic form), src/mps.cpp:262-320.
