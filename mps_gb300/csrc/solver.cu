@@ -198,7 +198,7 @@ __device__ __forceinline__ float spmv32_sell_row(const Ppe& A, int K, int row,
 // traffic in flight (a warp issues in order: it stalls at the first use of
 // a load).  Summation order is per group (a0: entries 0, 2; a1: 1, 3), the
 // same for any kGroups.
-constexpr int kGroups = 2;
+constexpr int kGroups = 4;
 __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf, int K, int row,
                                                  const float* __restrict__ u) {
     const int sl = row >> 5;
@@ -774,9 +774,6 @@ int coop_grid(const void* fn, int device, int block, size_t smem, int max_per_sm
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (smem > 0) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    // the solvers stream their operators through L1: keep the shared-memory
-    // carve-out at what their static arrays need
-    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxL1);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, smem) != cudaSuccess) {
         cudaGetLastError();
         per = 0;
