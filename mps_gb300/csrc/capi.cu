@@ -525,7 +525,8 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         g.nlev = l;
         if ((size_t)g.lev[l].nx * g.lev[l].ny > (size_t)kMgMaxCoarsest) g.enabled = 0;
         g.ngrid = 0;
-        while (g.ngrid + 1 < g.nlev && (size_t)g.lev[g.ngrid + 1].nx * g.lev[g.ngrid + 1].ny > 4096) g.ngrid++;
+        while (g.ngrid + 1 < g.nlev && (size_t)g.lev[g.ngrid + 1].nx * g.lev[g.ngrid + 1].ny > kMgBlockCells)
+            g.ngrid++;
         if (e->alloc(&g.e0, np) || e->alloc(&g.res0, np) ||
             e->alloc(&g.dense, (size_t)kMgMaxCoarsest * kMgMaxCoarsest))
             return bail(fail(MPS_ERR_CUDA, "cudaMalloc multigrid"));

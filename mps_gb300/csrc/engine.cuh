@@ -183,6 +183,9 @@ void launch_number_density(const Consts& c, const StateBuf& s, const NbList& nb,
 // built in a fixed order (deterministic); the coarsest level (<= 96
 // unknowns) is solved with its dense inverse.
 constexpr int kMgMaxLevels = 16;
+// Levels with at most this many cells run in one block (between two grid
+// barriers); larger ones run grid-wide.
+constexpr int kMgBlockCells = 1024;
 constexpr int kMgMaxCoarsest = 96;
 struct MgLevel {
     int32_t nx, ny;

@@ -382,28 +382,48 @@ __device__ __forceinline__ float stencil_row(const MgLevel& L, int I, const floa
     return acc;
 }
 
+// Tap (dx, dy) of a 9-point stencil at (x, y): the neighbour's index,
+// clamped into the grid so that its loads are always legal (no branch, so the
+// compiler can issue every tap's loads at once), and whether it exists.
+__device__ __forceinline__ int tap(const MgLevel& L, int x, int y, int d, bool& ok) {
+    const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
+    ok = nx >= 0 && ny >= 0 && nx < L.nx && ny < L.ny;
+    return min(max(nx, 0), L.nx - 1) * L.ny + min(max(ny, 0), L.ny - 1);
+}
+
 // residual of level l restricted to level l+1 (sum over the 2x2 children).
-// The children's 4 x 9 loads are predicated, not branched around, so they
-// are all in flight together.  Callers skip coarse cells without unknowns
-// (their children have none either: the Galerkin diagonal of an aggregate
-// with an unknown is positive).
+// Every load depends only on the cell's position and is unconditional (taps
+// clamped, then masked), so a child's 20 loads are in flight together: one
+// memory round trip per child, which after a grid barrier is an L2 access,
+// often on the other die (with a branch per tap, each tap was a round trip).  Cells without unknowns hold zero stencils, residuals and
+// corrections, so they add exactly 0 and need no test.  Callers skip coarse
+// cells without unknowns (their children have none either: the Galerkin
+// diagonal of an aggregate with an unknown is positive).
 __device__ __forceinline__ float restrict_cell(const MgLevel& F, int X, int Y) {
     const int n = F.nx * F.ny;
     float res[4];
-#pragma unroll
+    // children one after another (each child's 20 loads in one batch) keeps
+    // the register footprint small enough not to spill
+#pragma unroll 1
     for (int ab = 0; ab < 4; ab++) {
         const int x = 2 * X + (ab >> 1), y = 2 * Y + (ab & 1);
         const bool in = x < F.nx && y < F.ny;
-        const int c = in ? x * F.ny + y : 0;
-        const bool act = in && ldc(F.invd, c) > 0.f;
-        float s = 0.f;
+        const int xc = min(x, F.nx - 1), yc = min(y, F.ny - 1);
+        const int c = xc * F.ny + yc;
+        float st[9], ev[9];
+        bool ok[9];
 #pragma unroll
         for (int d = 0; d < 9; d++) {
-            const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
-            if (act && nx >= 0 && ny >= 0 && nx < F.nx && ny < F.ny)
-                s = fmaf(ldc(F.st, (size_t)d * n + c), ldv(F.e, nx * F.ny + ny), s);
+            const int j = tap(F, xc, yc, d, ok[d]);
+            st[d] = ldc(F.st, (size_t)d * n + c);
+            ev[d] = ldv(F.e, j);
         }
-        res[ab] = act ? ldv(F.r, c) - s : 0.f;
+        const float rc = ldv(F.r, c);
+        float s = 0.f;
+#pragma unroll
+        for (int d = 0; d < 9; d++)
+            if (ok[d]) s = fmaf(st[d], ev[d], s);
+        res[ab] = in ? rc - s : 0.f;
     }
     // the children in the order (0,0), (0,1), (1,0), (1,1)
     float acc = 0.f;
@@ -415,20 +435,27 @@ __device__ __forceinline__ float restrict_cell(const MgLevel& F, int X, int Y) {
 // Post-smoothing of a level with the prolongation folded in: the corrected
 // value of a cell is e + s * e_parent, computed on the fly for the cell and
 // its 8 neighbours, so prolongation needs no pass or barrier of its own.
+// Taps clamped and masked like restrict_cell: all loads in one batch.
 __device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, const MgLevel& C,
                                                 int I) {
     const int n = L.nx * L.ny;
     const int x = I / L.ny, y = I - x * L.ny;
     const float ei = fmaf(mg.scale, ldv(C.e, (x / 2) * C.ny + y / 2), ldv(L.e, I));
-    float acc = 0.f;
+    float st[9], ej[9];
+    bool ok[9];
 #pragma unroll
     for (int d = 0; d < 9; d++) {
-        const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
-        if (nx < 0 || ny < 0 || nx >= L.nx || ny >= L.ny) continue;
-        const float ej = fmaf(mg.scale, ldv(C.e, (nx / 2) * C.ny + ny / 2), ldv(L.e, nx * L.ny + ny));
-        acc = fmaf(ldc(L.st, (size_t)d * n + I), ej, acc);
+        const int j = tap(L, x, y, d, ok[d]);
+        const int jx = j / L.ny, jy = j - jx * L.ny;
+        st[d] = ldc(L.st, (size_t)d * n + I);
+        ej[d] = fmaf(mg.scale, ldv(C.e, (jx / 2) * C.ny + jy / 2), ldv(L.e, j));
     }
-    return fmaf(mg.omega * ldc(L.invd, I), ldv(L.r, I) - acc, ei);
+    const float iv = ldc(L.invd, I), ri = ldv(L.r, I);
+    float acc = 0.f;
+#pragma unroll
+    for (int d = 0; d < 9; d++)
+        if (ok[d]) acc = fmaf(st[d], ej[d], acc);
+    return fmaf(mg.omega * iv, ri - acc, ei);
 }
 
 // Levels lo..nlev of the V-cycle, run by the group's first block alone (they
@@ -506,6 +533,11 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
                                           int n, GridBar& gb, DevStats* ds) {
     const int gtid = gb.rank * BS + threadIdx.x;
     const int gsz = gb.size * BS;
+    // Cells of the grid levels are dealt to blocks in interleaved 32-cell
+    // chunks (coalesced within a warp): the cells with unknowns cover only
+    // the fluid's part of the tank, and a contiguous split would hand them all
+    // to a few blocks while the rest wait at the next barrier.
+    const int gcell = ((threadIdx.x >> 5) * gb.size + gb.rank) * 32 + (threadIdx.x & 31);
     // level 0 residual of the Inner particles (coalesced, one row per thread)
     for (int i = gtid; i < n; i += gsz)
         mg.res0[i] = A.diag32[i] > 0.f ? __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0) : 0.f;
@@ -514,7 +546,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     {
         MgLevel& L1 = mg.lev[1];
         const int n1 = L1.nx * L1.ny;
-        for (int I = gtid; I < n1; I += gsz) {
+        for (int I = gcell; I < n1; I += gsz) {
             const int b = __ldg(mf.cs + I), e = __ldg(mf.cs + I + 1);
             float acc = 0.f;
             for (int i = b; i < e; i++) acc += __ldcg(mg.res0 + i);
@@ -528,7 +560,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         MgLevel& L = mg.lev[l];
         MgLevel& C = mg.lev[l + 1];
         const bool smooth = l + 1 <= mg.ngrid;
-        for (int I = gtid; I < C.nx * C.ny; I += gsz) {
+        for (int I = gcell; I < C.nx * C.ny; I += gsz) {
             const int X = I / C.ny, Y = I - X * C.ny;
             const float iv = __ldg(C.invd + I);
             const float rr = iv > 0.f ? restrict_cell(L, X, Y) : 0.f;
@@ -545,7 +577,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         MgLevel& L = mg.lev[l];
         MgLevel& C = mg.lev[l + 1];
         const int nl = L.nx * L.ny;
-        for (int I = gtid; I < nl; I += gsz) L.t[I] = __ldg(L.invd + I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
+        for (int I = gcell; I < nl; I += gsz) L.t[I] = __ldg(L.invd + I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
         if (!grid_sync(gb, ds)) return false;
         float* tmp = L.e;
         L.e = L.t;
@@ -554,9 +586,15 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     // level 1 -> 0: prolongate to the Inner particles, then post-smooth
     {
         MgLevel& L1 = mg.lev[1];
-        for (int i = gtid; i < n; i += gsz)
-            if (A.diag32[i] > 0.f)
-                mg.e0[i] = fmaf(mg.scale, __ldcg(L1.e + __ldg(mf.skey + i)), __ldcg(mg.e0 + i));
+        const int n1 = L1.nx * L1.ny;
+        for (int i = gtid; i < n; i += gsz) {
+            // loads first, test after: two round trips, not four
+            const float dg = A.diag32[i];
+            const int key = min(__ldg(mf.skey + i), n1 - 1);  // ghosts: sentinel key
+            const float e0 = __ldcg(mg.e0 + i);
+            const float ec = __ldcg(L1.e + key);
+            if (dg > 0.f) mg.e0[i] = fmaf(mg.scale, ec, e0);
+        }
     }
     if (!grid_sync(gb, ds)) return false;
     for (int i = gtid; i < n; i += gsz) {
