@@ -489,7 +489,7 @@ def run_reference(args, rank: int):
         pass
     cpu = cpu_sample(steps=max(1, args.steps // 5) + 1)
     per.append(cpu["value"])
-    return {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+    return {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"{args.workload} (CPU sample: {CPU_SAMPLE})"},

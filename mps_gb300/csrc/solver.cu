@@ -251,10 +251,87 @@ __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf
     return a0 + a1;
 }
 
+// Compact sums of two rows of different slices at once (their groups'
+// loads interleaved: twice the memory traffic in flight per thread).  Each
+// row keeps its own order (group by group, a0: entries 0, 2; a1: 1, 3), so
+// the results equal compact_row_sum's.
+__device__ __forceinline__ void compact_rows2(const Ppe& A, const MatFree& mf, int K, int ra, int rb,
+                                              const float* __restrict__ u, float& oa, float& ob) {
+    const int wa = __ldg(A.slice_w + (ra >> 5)), wb = __ldg(A.slice_w + (rb >> 5));
+    const int sa[3] = {__ldg(mf.rs + ra), __ldg(mf.rs + mf.rs_stride + ra), __ldg(mf.rs + 2 * mf.rs_stride + ra)};
+    const int sb[3] = {__ldg(mf.rs + rb), __ldg(mf.rs + mf.rs_stride + rb), __ldg(mf.rs + 2 * mf.rs_stride + rb)};
+    const float4* vpa = reinterpret_cast<const float4*>(A.val32) + (qsell_index(ra, 0, K) >> 2);
+    const float4* vpb = reinterpret_cast<const float4*>(A.val32) + (qsell_index(rb, 0, K) >> 2);
+    const uint32_t* ipa = reinterpret_cast<const uint32_t*>(mf.idx8) + (qsell_index(ra, 0, K) >> 2);
+    const uint32_t* ipb = reinterpret_cast<const uint32_t*>(mf.idx8) + (qsell_index(rb, 0, K) >> 2);
+    auto col = [](const int* st, uint32_t b4, int t) {
+        const uint32_t b = (b4 >> (8 * t)) & 255u;
+        const uint32_t r = b >> 6;
+        return (r == 0 ? st[0] : (r == 1 ? st[1] : st[2])) + (int)(b & 63u);
+    };
+    auto group = [&](const float4& v, uint32_t b4, const int* st, float& a0, float& a1) {
+        float x[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) x[t] = __ldcg(u + col(st, b4, t));
+        a0 = fmaf(v.x, x[0], a0);
+        a1 = fmaf(v.y, x[1], a1);
+        a0 = fmaf(v.z, x[2], a0);
+        a1 = fmaf(v.w, x[3], a1);
+    };
+    const int ga = (wa + 3) >> 2, gb = (wb + 3) >> 2, gm = min(ga, gb);
+    float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+    int g = 0;
+    for (; g + 2 <= gm; g += 2) {
+        const float4 va0 = __ldg(vpa + g * 32), va1 = __ldg(vpa + (g + 1) * 32);
+        const float4 vb0 = __ldg(vpb + g * 32), vb1 = __ldg(vpb + (g + 1) * 32);
+        const uint32_t ia0 = __ldg(ipa + g * 32), ia1 = __ldg(ipa + (g + 1) * 32);
+        const uint32_t ib0 = __ldg(ipb + g * 32), ib1 = __ldg(ipb + (g + 1) * 32);
+        float xa[8], xb[8];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            xa[t] = __ldcg(u + col(sa, ia0, t));
+            xa[4 + t] = __ldcg(u + col(sa, ia1, t));
+            xb[t] = __ldcg(u + col(sb, ib0, t));
+            xb[4 + t] = __ldcg(u + col(sb, ib1, t));
+        }
+        a0 = fmaf(va0.x, xa[0], a0);
+        a1 = fmaf(va0.y, xa[1], a1);
+        a0 = fmaf(va0.z, xa[2], a0);
+        a1 = fmaf(va0.w, xa[3], a1);
+        a0 = fmaf(va1.x, xa[4], a0);
+        a1 = fmaf(va1.y, xa[5], a1);
+        a0 = fmaf(va1.z, xa[6], a0);
+        a1 = fmaf(va1.w, xa[7], a1);
+        b0 = fmaf(vb0.x, xb[0], b0);
+        b1 = fmaf(vb0.y, xb[1], b1);
+        b0 = fmaf(vb0.z, xb[2], b0);
+        b1 = fmaf(vb0.w, xb[3], b1);
+        b0 = fmaf(vb1.x, xb[4], b0);
+        b1 = fmaf(vb1.y, xb[5], b1);
+        b0 = fmaf(vb1.z, xb[6], b0);
+        b1 = fmaf(vb1.w, xb[7], b1);
+    }
+    for (int h = g; h < ga; h++) group(__ldg(vpa + h * 32), __ldg(ipa + h * 32), sa, a0, a1);
+    for (int h = g; h < gb; h++) group(__ldg(vpb + h * 32), __ldg(ipb + h * 32), sb, b0, b1);
+    oa = a0 + a1;
+    ob = b0 + b1;
+}
+
 // Off-diagonal part of row i of the FP32 operator.
 __device__ __forceinline__ float off_row(const Ppe& A, const MatFree& mf, int K, int i,
                                          const float* __restrict__ v) {
     return (mf.enabled && !mf.sell_row[i]) ? compact_row_sum(A, mf, K, i, v) : spmv32_sell_row(A, K, i, v);
+}
+
+// Off-diagonal parts of rows i and i2 (i2 < 0: none), paired when both are compact.
+__device__ __forceinline__ void off_rows(const Ppe& A, const MatFree& mf, int K, int i, int i2,
+                                         const float* __restrict__ v, float& o, float& o2) {
+    if (mf.enabled && i2 >= 0 && !mf.sell_row[i] && !mf.sell_row[i2]) {
+        compact_rows2(A, mf, K, i, i2, v, o, o2);
+        return;
+    }
+    o = off_row(A, mf, K, i, v);
+    o2 = i2 >= 0 ? off_row(A, mf, K, i2, v) : 0.f;
 }
 
 // ----------------------------------------------------------------- FP64 CG
@@ -356,12 +433,6 @@ __device__ __forceinline__ void acc_prod(F2& a, float x, float y) {
     a.lo += err + e;
 }
 __device__ __forceinline__ double f2d(const F2& a) { return (double)a.hi + (double)a.lo; }
-
-// Level-0 operator row (FP32): diag_i v_i + off-diagonal sum.
-__device__ __forceinline__ float a0_row(const Ppe& A, const MatFree& mf, int K, int i,
-                                        const float* __restrict__ v) {
-    return fmaf(A.diag32[i], __ldcg(v + i), off_row(A, mf, K, i, v));
-}
 
 // Loads of multigrid data: the vectors change during the solve (L2), the
 // stencils and inverse diagonals do not (read-only cache).
@@ -539,8 +610,18 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     // to a few blocks while the rest wait at the next barrier.
     const int gcell = ((threadIdx.x >> 5) * gb.size + gb.rank) * 32 + (threadIdx.x & 31);
     // level 0 residual of the Inner particles (coalesced, one row per thread)
-    for (int i = gtid; i < n; i += gsz)
-        mg.res0[i] = A.diag32[i] > 0.f ? __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0) : 0.f;
+    for (int i = gtid; i < n; i += 2 * gsz) {
+        const int i2 = i + gsz < n ? i + gsz : -1;
+        float o, o2;
+        off_rows(A, mf, K, i, i2, mg.e0, o, o2);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int row = h == 0 ? i : i2;
+            if (row < 0) break;
+            const float dg = A.diag32[row];
+            mg.res0[row] = dg > 0.f ? __ldcg(r + row) - fmaf(dg, __ldcg(mg.e0 + row), h == 0 ? o : o2) : 0.f;
+        }
+    }
     if (!grid_sync(gb, ds)) return false;
     // level 1: sum over each cell's contiguous slots; pre-smooth
     {
@@ -597,10 +678,18 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         }
     }
     if (!grid_sync(gb, ds)) return false;
-    for (int i = gtid; i < n; i += gsz) {
-        const float dg = A.diag32[i];
-        u[i] = dg > 0.f ? fmaf(mg.omega / dg, __ldcg(r + i) - a0_row(A, mf, K, i, mg.e0), __ldcg(mg.e0 + i))
-                        : 0.f;
+    for (int i = gtid; i < n; i += 2 * gsz) {
+        const int i2 = i + gsz < n ? i + gsz : -1;
+        float o, o2;
+        off_rows(A, mf, K, i, i2, mg.e0, o, o2);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int row = h == 0 ? i : i2;
+            if (row < 0) break;
+            const float dg = A.diag32[row];
+            const float e0 = __ldcg(mg.e0 + row);
+            u[row] = dg > 0.f ? fmaf(mg.omega / dg, __ldcg(r + row) - fmaf(dg, e0, h == 0 ? o : o2), e0) : 0.f;
+        }
     }
     return true;
 }
@@ -671,17 +760,26 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
         for (;;) {
             // phase B: w = A u ; gamma = r.u, delta = w.u, rho = r.r
             F2 g = {0.f, 0.f}, dl = {0.f, 0.f}, rr = {0.f, 0.f};
-            for (int i = gtid; i < a.n; i += gsz) {
-                // rows that are not unknowns (diagonal 0: Surface, Ignored,
-                // ghosts) have only zero entries: w = +0 without the gathers
-                const float ui = __ldcg(kv.u32 + i);
-                const float dg = A.diag32[i];
-                const float w = dg > 0.f ? fmaf(dg, ui, off_row(A, mf, a.K, i, kv.u32)) : 0.f;
-                kv.w32[i] = w;
-                const float r = kv.r32[i];
-                acc_prod(g, r, ui);
-                acc_prod(dl, w, ui);
-                acc_prod(rr, r, r);
+            // rows i and i + gsz of this thread together (their operator
+            // loads interleaved); rows that are not unknowns (diagonal 0:
+            // Surface, Ignored, ghosts) get w = +0
+            for (int i = gtid; i < a.n; i += 2 * gsz) {
+                const int i2 = i + gsz < a.n ? i + gsz : -1;
+                float o, o2;
+                off_rows(A, mf, a.K, i, i2, kv.u32, o, o2);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int row = h == 0 ? i : i2;
+                    if (row < 0) break;
+                    const float ui = __ldcg(kv.u32 + row);
+                    const float dg = A.diag32[row];
+                    const float w = dg > 0.f ? fmaf(dg, ui, h == 0 ? o : o2) : 0.f;
+                    kv.w32[row] = w;
+                    const float r = kv.r32[row];
+                    acc_prod(g, r, ui);
+                    acc_prod(dl, w, ui);
+                    acc_prod(rr, r, r);
+                }
             }
             double v3[3] = {f2d(g), f2d(dl), f2d(rr)}, t3[3];
             if (!reduce_sync<3, BS>(gb, v3, t3, ds)) return;
