@@ -668,13 +668,25 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     {
         MgLevel& L1 = mg.lev[1];
         const int n1 = L1.nx * L1.ny;
-        for (int i = gtid; i < n; i += gsz) {
-            // loads first, test after: two round trips, not four
-            const float dg = A.diag32[i];
-            const int key = min(__ldg(mf.skey + i), n1 - 1);  // ghosts: sentinel key
-            const float e0 = __ldcg(mg.e0 + i);
-            const float ec = __ldcg(L1.e + key);
-            if (dg > 0.f) mg.e0[i] = fmaf(mg.scale, ec, e0);
+        // four rows per iteration, loads first and tests after: two round
+        // trips per four rows
+        for (int i0 = gtid; i0 < n; i0 += 4 * gsz) {
+            float dg[4], e0[4], ec[4];
+            int key[4];
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int i = min(i0 + h * gsz, n - 1);
+                dg[h] = A.diag32[i];
+                key[h] = min(__ldg(mf.skey + i), n1 - 1);  // ghosts: sentinel key
+                e0[h] = __ldcg(mg.e0 + i);
+            }
+#pragma unroll
+            for (int h = 0; h < 4; h++) ec[h] = __ldcg(L1.e + key[h]);
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int i = i0 + h * gsz;
+                if (i < n && dg[h] > 0.f) mg.e0[i] = fmaf(mg.scale, ec[h], e0[h]);
+            }
         }
     }
     if (!grid_sync(gb, ds)) return false;
@@ -796,19 +808,38 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
             }
             gamma_old = gamma;
             // phase A: p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; u = M r
-            for (int i = gtid; i < a.n; i += gsz) {
-                const float u = __ldcg(kv.u32 + i);
-                const float p = fmaf(beta, kv.p32[i], u);
-                const float s = fmaf(beta, kv.s32[i], kv.w32[i]);
-                kv.p32[i] = p;
-                kv.s32[i] = s;
-                kv.x32[i] = fmaf(alpha, p, kv.x32[i]);
-                const float r = fmaf(-alpha, s, kv.r32[i]);
-                kv.r32[i] = r;
-                if (mg.enabled)
-                    mg.e0[i] = mg.omega * kv.inv_diag32[i] * r;
-                else
-                    kv.u32[i] = kv.inv_diag32[i] * r;
+            // Four of this thread's rows per iteration, all loads before any
+            // store (the compiler cannot move loads above stores to arrays it
+            // cannot prove distinct): four rows' memory traffic in flight.
+            for (int i0 = gtid; i0 < a.n; i0 += 4 * gsz) {
+                float u[4], p[4], s[4], w[4], x[4], r[4], id[4];
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int i = min(i0 + h * gsz, a.n - 1);
+                    u[h] = __ldcg(kv.u32 + i);
+                    p[h] = kv.p32[i];
+                    s[h] = kv.s32[i];
+                    w[h] = kv.w32[i];
+                    x[h] = kv.x32[i];
+                    r[h] = kv.r32[i];
+                    id[h] = kv.inv_diag32[i];
+                }
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int i = i0 + h * gsz;
+                    if (i >= a.n) break;
+                    const float pn = fmaf(beta, p[h], u[h]);
+                    const float sn = fmaf(beta, s[h], w[h]);
+                    kv.p32[i] = pn;
+                    kv.s32[i] = sn;
+                    kv.x32[i] = fmaf(alpha, pn, x[h]);
+                    const float rn = fmaf(-alpha, sn, r[h]);
+                    kv.r32[i] = rn;
+                    if (mg.enabled)
+                        mg.e0[i] = mg.omega * id[h] * rn;
+                    else
+                        kv.u32[i] = id[h] * rn;
+                }
             }
             k++;
             if (!grid_sync(gb, ds)) return;
