@@ -158,3 +158,48 @@ def test_torch_autograd_function():
     assert np.all(np.isfinite(gv)) and np.abs(gv[fl]).max() > 0
     tr.close()
     eng.close()
+
+
+def test_adjoint_3d_against_finite_differences():
+    """A non-planar scene (the 3-D box of the golden set, seeded 3-D initial
+    velocities): the adjoint's z components (gravity and velocities) against
+    central finite differences."""
+    m = engine_or_skip()
+    from golden_cases import load
+
+    g = load("box3d")
+    prm = dict(g["params"])
+    pos, t = g["pos0"], g["type0"]
+    rng = np.random.default_rng(21)
+    fl = t == 0
+    vel = np.zeros_like(pos)
+    vel[fl] = rng.normal(0.0, 0.01, (fl.sum(), 3))
+    steps, every = 6, 4
+    target = pos[fl] + rng.normal(0.0, 1e-3, (fl.sum(), 3))
+    eng = m.Engine(prm, pos, vel, t, precision=m.FP64)
+    tr = m.Trajectory(eng, steps, every, np.flatnonzero(t == 1)[:8].astype(np.int32))
+    gv0 = np.array(prm["gravity"], float)
+
+    def loss(v0, gvec):
+        sp, pf, _ = tr.forward(v0, gvec)
+        return float(np.mean(sp ** 2)) + 1e6 * float(np.sum((pf[fl] - target) ** 2)), sp, pf
+
+    L, sp, pf = loss(vel, gv0)
+    d_pos = np.zeros_like(pf)
+    d_pos[fl] = 2e6 * (pf[fl] - target)
+    _, gvel, gg = tr.backward(2.0 * sp / sp.size, d_pos, None)
+    eps = 1e-6
+    for d in (1, 2):
+        gp, gm = gv0.copy(), gv0.copy()
+        gp[d] += eps
+        gm[d] -= eps
+        fd = (loss(vel, gp)[0] - loss(vel, gm)[0]) / (2 * eps)
+        assert abs(gg[d] - fd) <= REL * max(abs(fd), 1e-3 * np.abs(gg).max()), (d, gg[d], fd)
+    u = np.zeros_like(vel)
+    u[fl] = rng.normal(size=(fl.sum(), 3))
+    u /= np.linalg.norm(u)
+    fd = (loss(vel + eps * u, gv0)[0] - loss(vel - eps * u, gv0)[0]) / (2 * eps)
+    ad = float(np.sum(gvel * u))
+    assert abs(ad - fd) <= REL * max(abs(fd), 1e-3 * np.linalg.norm(gvel)), (ad, fd)
+    tr.close()
+    eng.close()

@@ -98,3 +98,37 @@ def test_graph_replay_matches_eager(precision):
     assert fa == [1, 1, 1, 0, 1, 1] and fb == [0] * 6
     for k in a:
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_fp64_step_at_config1_resolution_against_oracle():
+    """The plain FP64 step at the 2M workload's particle distance and time
+    step (l0 = 5e-4 m, dt = 5e-5 s, same tank walls and physics), on a small
+    seeded crop of that scene (a 60 x 120 column), against the CPU oracle:
+    bit-exact flags and collision pairs, pressure within the CG tolerance."""
+    m = engine_or_skip()
+    from oracle import Oracle
+
+    from mps_gb300 import scenes
+
+    l0 = 5e-4
+    prm, pos, vel, t = scenes.dam_break(l0, tank=(0.06, 0.075), column=(0.03, 0.06), dt=5e-5,
+                                        margin=0.005)
+    rng = np.random.default_rng(12)
+    fl = t == scenes.FLUID
+    vel[fl, :2] = rng.normal(0.0, 0.02, (fl.sum(), 2))
+    e = m.Engine(prm, pos, vel, t, precision=m.FP64)
+    o = Oracle(prm, pos, vel, t)
+    o.set_cg(solves=1)
+    for s in range(5):
+        st = e.step()
+        so = o.step()
+        assert st["debug_log_count"] == so["debug_log_count"], s
+        ci, cj, _ = e.collisions()
+        oi, oj, _ = o.collisions()
+        assert np.array_equal(ci, oi) and np.array_equal(cj, oj), s
+    a, b = e.state(), o.state()
+    for k in ("type", "bc", "dirichlet"):
+        assert np.array_equal(a[k], b[k]), k
+    assert rel_l2(a["pressure"], b["pressure"]) < 1e-7
+    assert np.max(np.abs(a["pos"] - b["pos"])) < 1e-12
+    e.close()
