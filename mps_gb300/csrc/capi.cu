@@ -71,11 +71,6 @@ int lattice_count(int dim, double ratio) {
     return cnt;
 }
 
-__global__ void k_from_host_order(int n, const int32_t* __restrict__ id, const double* __restrict__ src,
-                                  int comps, int comp, double* __restrict__ dst) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) dst[k] = src[(size_t)id[k] * comps + comp];
-}
 __global__ void k_type_from_host_order(int n, const int32_t* __restrict__ id,
                                        const int32_t* __restrict__ src, int8_t* __restrict__ dst) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -86,15 +81,43 @@ __global__ void k_to_host_order(int n, const int32_t* __restrict__ id, const dou
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) dst[(size_t)id[k] * comps + comp] = src[k];
 }
-__global__ void k_fill_host_order(int n, const int32_t* __restrict__ id, double v, int comps,
-                                  int comp, double* __restrict__ dst) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) dst[(size_t)id[k] * comps + comp] = v;
-}
 __global__ void k_i8_to_host_order(int n, const int32_t* __restrict__ id, const int8_t* __restrict__ src,
                                    int32_t* __restrict__ dst) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) dst[id[k]] = src[k];
+}
+// xyz-interleaved host layout <-> the slot-ordered component arrays (one
+// launch per vector; planar engines keep no z array: z is the constant zc)
+__global__ void k_vec3_to_host(int n, const int32_t* __restrict__ id, const double* __restrict__ d0,
+                               const double* __restrict__ d1, const double* __restrict__ d2,
+                               double zc, double* __restrict__ dst) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const size_t o = (size_t)id[k] * 3;
+    dst[o] = d0[k];
+    dst[o + 1] = d1[k];
+    dst[o + 2] = d2 ? d2[k] : zc;
+}
+__global__ void k_vec3_from_host(int n, const int32_t* __restrict__ id, const double* __restrict__ src,
+                                 double* __restrict__ d0, double* __restrict__ d1, double* __restrict__ d2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const size_t o = (size_t)id[k] * 3;
+    d0[k] = src[o];
+    d1[k] = src[o + 1];
+    if (d2) d2[k] = src[o + 2];
+}
+// Upload checks before anything is written: planar engines keep z = z0 and
+// v_z = 0 (bit 1), types lie in {-1, 0, 1, 2} (bit 2).
+__global__ void k_check_upload(int n, const double* __restrict__ pos, const double* __restrict__ vel,
+                               const int32_t* __restrict__ type, int planar, double z0,
+                               int32_t* __restrict__ flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t f = 0;
+    if (planar && ((pos && pos[3 * (size_t)i + 2] != z0) || (vel && vel[3 * (size_t)i + 2] != 0.0))) f |= 1;
+    if (type && (type[i] < -1 || type[i] > 2)) f |= 2;
+    if (f) atomicOr(flag, f);
 }
 __global__ void k_iota(int n, int32_t* a) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -494,8 +517,8 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         e->alloc(&e->mf.sell_row, np) || e->alloc(&e->mf.rs, 3 * np) ||
         e->alloc(&e->cand_cnt, np + 1) || e->alloc(&e->cand_base, np + 2) ||
         e->alloc(&e->parent, np) || e->alloc(&e->has_surface, np) || e->alloc(&e->ax, np) ||
-        e->alloc(&e->ay, np) || e->alloc(&e->az, np) || e->alloc(&e->stage, 3 * np) ||
-        e->alloc(&e->stage_i, np) || e->alloc(&e->ds, 1))
+        e->alloc(&e->ay, np) || e->alloc(&e->az, np) || e->alloc(&e->stage, 9 * np) ||
+        e->alloc(&e->stage_i, 3 * np) || e->alloc(&e->dflag, 1) || e->alloc(&e->ds, 1))
         return bail(fail(MPS_ERR_CUDA, "cudaMalloc failed (out of device memory?)"));
     e->pair_cap = (int32_t)std::min<size_t>(4 * np + 1024, (size_t)1 << 30);
     if (e->alloc(&e->pairs, e->pair_cap)) return bail(fail(MPS_ERR_CUDA, "cudaMalloc pairs"));
@@ -552,14 +575,10 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     cudaMemsetAsync(e->nb.cnt, 0, np * 4, e->st);
     k_iota<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id);
     // upload the initial condition (identity slot order, ids = indices)
-    for (int comp = 0; comp < 3; comp++) {
-        double* pd[3] = {s.x, s.y, s.z};
-        double* vd[3] = {s.vx, s.vy, s.vz};
-        CU(cudaMemcpyAsync(e->stage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
-        k_from_host_order<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id, e->stage, 3, comp, pd[comp]);
-        CU(cudaMemcpyAsync(e->stage, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
-        k_from_host_order<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id, e->stage, 3, comp, vd[comp]);
-    }
+    CU(cudaMemcpyAsync(e->stage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
+    CU(cudaMemcpyAsync(e->stage + 3 * np, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
+    k_vec3_from_host<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id, e->stage, s.x, s.y, s.z);
+    k_vec3_from_host<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id, e->stage + 3 * np, s.vx, s.vy, s.vz);
     CU(cudaMemcpyAsync(e->stage_i, type, sizeof(int32_t) * n, cudaMemcpyHostToDevice, e->st));
     k_type_from_host_order<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id, e->stage_i, s.type);
     e->cur = 0;
@@ -639,46 +658,36 @@ int mps_download(mps_engine* e, double* pos, double* vel, double* pressure, doub
                  double* ndr, int32_t* type, int32_t* bc, int32_t* dirichlet) {
     if (!e) return fail(MPS_ERR_ARG, "null engine");
     const int n = e->n, T = 256, G = (n + 255) / 256;
+    const size_t np = e->n_pad;
     StateBuf& s = e->S();
-    // planar engines do not store z / v_z: they are the constants z0 / 0
-    auto vec3 = [&](double* host, double* d[3], double zconst) -> int {
-        for (int comp = 0; comp < 3; comp++) {
-            if (comp == 2 && e->c.planar)
-                k_fill_host_order<<<G, T, 0, e->st>>>(n, s.id, zconst, 3, 2, e->stage);
-            else
-                k_to_host_order<<<G, T, 0, e->st>>>(n, s.id, d[comp], 3, comp, e->stage);
-        }
-        CU(cudaMemcpyAsync(host, e->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->st));
-        CU(cudaStreamSynchronize(e->st));
-        return MPS_OK;
-    };
-    int rc;
+    // every array gathers into its own staging region and is copied out; one
+    // wait at the end.  Planar engines keep no z / v_z: they are z0 / 0.
+    const bool pl = e->c.planar;
     if (pos) {
-        double* d[3] = {s.x, s.y, s.z};
-        if ((rc = vec3(pos, d, e->c.z0))) return rc;
+        k_vec3_to_host<<<G, T, 0, e->st>>>(n, s.id, s.x, s.y, pl ? nullptr : s.z, e->c.z0, e->stage);
+        CU(cudaMemcpyAsync(pos, e->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->st));
     }
     if (vel) {
-        double* d[3] = {s.vx, s.vy, s.vz};
-        if ((rc = vec3(vel, d, 0.0))) return rc;
+        k_vec3_to_host<<<G, T, 0, e->st>>>(n, s.id, s.vx, s.vy, pl ? nullptr : s.vz, 0.0, e->stage + 3 * np);
+        CU(cudaMemcpyAsync(vel, e->stage + 3 * np, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->st));
     }
-    auto scal = [&](double* host, double* d) -> int {
-        k_to_host_order<<<G, T, 0, e->st>>>(n, s.id, d, 1, 0, e->stage);
-        CU(cudaMemcpyAsync(host, e->stage, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
-        CU(cudaStreamSynchronize(e->st));
-        return MPS_OK;
-    };
-    if (pressure && (rc = scal(pressure, s.p))) return rc;
-    if (min_pressure && (rc = scal(min_pressure, s.minp))) return rc;
-    if (ndr && (rc = scal(ndr, s.ndr))) return rc;
-    auto i8 = [&](int32_t* host, int8_t* d) -> int {
-        k_i8_to_host_order<<<G, T, 0, e->st>>>(n, s.id, d, e->stage_i);
-        CU(cudaMemcpyAsync(host, e->stage_i, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, e->st));
-        CU(cudaStreamSynchronize(e->st));
-        return MPS_OK;
-    };
-    if (type && (rc = i8(type, s.type))) return rc;
-    if (bc && (rc = i8(bc, s.bc))) return rc;
-    if (dirichlet && (rc = i8(dirichlet, s.dir))) return rc;
+    double* sc[3] = {pressure, min_pressure, ndr};
+    double* sd[3] = {s.p, s.minp, s.ndr};
+    for (int q = 0; q < 3; q++) {
+        if (!sc[q]) continue;
+        double* st = e->stage + (6 + q) * np;
+        k_to_host_order<<<G, T, 0, e->st>>>(n, s.id, sd[q], 1, 0, st);
+        CU(cudaMemcpyAsync(sc[q], st, sizeof(double) * n, cudaMemcpyDeviceToHost, e->st));
+    }
+    int32_t* ic[3] = {type, bc, dirichlet};
+    int8_t* id8[3] = {s.type, s.bc, s.dir};
+    for (int q = 0; q < 3; q++) {
+        if (!ic[q]) continue;
+        int32_t* st = e->stage_i + q * np;
+        k_i8_to_host_order<<<G, T, 0, e->st>>>(n, s.id, id8[q], st);
+        CU(cudaMemcpyAsync(ic[q], st, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, e->st));
+    }
+    CU(cudaStreamSynchronize(e->st));
     CU(cudaGetLastError());
     return MPS_OK;
 }
@@ -686,34 +695,28 @@ int mps_download(mps_engine* e, double* pos, double* vel, double* pressure, doub
 int mps_upload(mps_engine* e, const double* pos, const double* vel, const int32_t* type) {
     if (!e) return fail(MPS_ERR_ARG, "null engine");
     const int n = e->n, T = 256, G = (n + 255) / 256;
+    const size_t np = e->n_pad;
     StateBuf& s = e->S();
-    if (e->c.planar) {
-        for (int i = 0; i < n; i++)
-            if ((pos && pos[3 * i + 2] != e->c.z0) || (vel && vel[3 * i + 2] != 0.0))
-                return fail(MPS_ERR_ARG, "mps_upload: a planar engine keeps z and v_z constant");
-    }
-    int comps = e->c.planar ? 2 : 3;
-    if (pos) {
-        double* d[3] = {s.x, s.y, s.z};
-        CU(cudaMemcpyAsync(e->stage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
-        for (int comp = 0; comp < comps; comp++)
-            k_from_host_order<<<G, T, 0, e->st>>>(n, s.id, e->stage, 3, comp, d[comp]);
-        CU(cudaStreamSynchronize(e->st));
-    }
-    if (vel) {
-        double* d[3] = {s.vx, s.vy, s.vz};
-        CU(cudaMemcpyAsync(e->stage, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
-        for (int comp = 0; comp < comps; comp++)
-            k_from_host_order<<<G, T, 0, e->st>>>(n, s.id, e->stage, 3, comp, d[comp]);
-        CU(cudaStreamSynchronize(e->st));
-    }
-    if (type) {
-        for (int i = 0; i < n; i++)
-            if (type[i] < -1 || type[i] > 2) return fail(MPS_ERR_ARG, "mps_upload: bad particle type");
-        CU(cudaMemcpyAsync(e->stage_i, type, sizeof(int32_t) * n, cudaMemcpyHostToDevice, e->st));
-        k_type_from_host_order<<<G, T, 0, e->st>>>(n, s.id, e->stage_i, s.type);
-        CU(cudaStreamSynchronize(e->st));
-    }
+    const bool pl = e->c.planar;
+    // copy in and check on the device; the state changes only if all is valid
+    double* ps = pos ? e->stage : nullptr;
+    double* vs = vel ? e->stage + 3 * np : nullptr;
+    int32_t* ts = type ? e->stage_i : nullptr;
+    if (pos) CU(cudaMemcpyAsync(ps, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
+    if (vel) CU(cudaMemcpyAsync(vs, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, e->st));
+    if (type) CU(cudaMemcpyAsync(ts, type, sizeof(int32_t) * n, cudaMemcpyHostToDevice, e->st));
+    CU(cudaMemsetAsync(e->dflag, 0, sizeof(int32_t), e->st));
+    k_check_upload<<<G, T, 0, e->st>>>(n, ps, vs, ts, pl ? 1 : 0, e->c.z0, e->dflag);
+    CU(cudaMemcpyAsync(&e->hs->upload_flag, e->dflag, sizeof(int32_t), cudaMemcpyDeviceToHost, e->st));
+    CU(cudaStreamSynchronize(e->st));
+    CU(cudaGetLastError());
+    const int32_t f = e->hs->upload_flag;
+    if (f & 1) return fail(MPS_ERR_ARG, "mps_upload: a planar engine keeps z and v_z constant");
+    if (f & 2) return fail(MPS_ERR_ARG, "mps_upload: bad particle type");
+    if (pos) k_vec3_from_host<<<G, T, 0, e->st>>>(n, s.id, ps, s.x, s.y, pl ? nullptr : s.z);
+    if (vel) k_vec3_from_host<<<G, T, 0, e->st>>>(n, s.id, vs, s.vx, s.vy, pl ? nullptr : s.vz);
+    if (type) k_type_from_host_order<<<G, T, 0, e->st>>>(n, s.id, ts, s.type);
+    CU(cudaStreamSynchronize(e->st));
     CU(cudaGetLastError());
     return MPS_OK;
 }

@@ -87,6 +87,8 @@ struct DevStats {
     int32_t pad;
     double cg_rel_residual;
     unsigned long long nnz_off;
+    int32_t upload_flag;  // host copy of mps_upload's device checks
+    int32_t pad2;
 };
 
 struct CollPair {

@@ -60,8 +60,9 @@ struct mps_engine {
     int32_t* parent = nullptr;
     int8_t* has_surface = nullptr;
     double *ax = nullptr, *ay = nullptr, *az = nullptr;
-    double* stage = nullptr;  // 3 n doubles for host transfers
-    int32_t* stage_i = nullptr;
+    double* stage = nullptr;   // 9 n doubles for host transfers (pos, vel, p, p_min, ndr)
+    int32_t* stage_i = nullptr;  // 3 n ints (type, bc, dirichlet)
+    int32_t* dflag = nullptr;    // device flag of the upload checks
     mpsg::DevStats* ds = nullptr;
     mpsg::DevStats* hs = nullptr;  // pinned
     int precision = MPS_PRECISION_FP64;
