@@ -105,11 +105,15 @@ int mps_destroy(mps_engine* e);
  * keep the defaults. */
 int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_iter);
 
-/* The MIXED solver's preconditioner on planar scenes: an aggregation
- * multigrid V(1,1) cycle (default on; omega = damped-Jacobi weight in (0,1),
- * scale = coarse-correction weight in [1,2)), or plain Jacobi when disabled.
- * No counterpart in the reference (its CG is Jacobi-preconditioned). */
-int mps_set_multigrid(mps_engine* e, int32_t enabled, float omega, float scale);
+/* The MIXED solver's preconditioner on planar scenes.  mode 0: Jacobi;
+ * mode 1 (default): aggregation multigrid, additive at the particle level,
+ * u = omega D^-1 r + scale P V(P^T r) with V a V(1,1) cycle over the cell
+ * grids (one operator pass per iteration); mode 2: the multiplicative
+ * V(1,1) cycle from the particle level (three operator passes per
+ * iteration, fewer iterations).  omega = damped-Jacobi weight in (0,1),
+ * scale = coarse-correction weight in [1,2) (default 0.9, 1.5).  No
+ * counterpart in the reference (its CG is Jacobi-preconditioned). */
+int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale);
 
 /* Non-export steps run as a CUDA graph replay (default on): the first step
  * at each buffer parity captures the step's kernel sequence, later steps

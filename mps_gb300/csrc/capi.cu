@@ -152,7 +152,8 @@ int alloc_state(mps_engine* e, StateBuf& s) {
 
 Mg active_mg(const mps_engine* e) {
     Mg g = e->mg;
-    g.enabled = e->mg.enabled && e->mg_requested;
+    g.enabled = e->mg.enabled && e->mg_requested != 0;
+    g.additive = e->mg_requested == 1;
     return g;
 }
 
@@ -252,17 +253,20 @@ void enqueue_step(mps_engine* e, bool do_export) {
 // the row's own entry).  Per stored off-diagonal entry and pass: FP64 12 B
 // (column + value), compact FP32 5 B (value + index byte).  Per row and
 // iteration: FP64 CG 116 B (8 vectors); MIXED inner iteration 65 B with the
-// Jacobi preconditioner, or with the multigrid V-cycle 143 B plus two more
-// level-0 operator passes and ~96 B per coarse-grid cell (two 9-point
-// stencil reads + 6 vector words).  MIXED adds per refinement the FP64
+// Jacobi preconditioner; with the multigrid V-cycle ~96 B per coarse-grid
+// cell (two 9-point stencil reads + 6 vector words) and, additive at level
+// 0, 89 B per row, multiplicative 143 B per row and two more level-0
+// operator passes.  MIXED adds per refinement the FP64
 // residual (12 B/entry + 36 B/row) and once the FP32 operator setup
 // (17 B/entry + 16 B/row written and read).
 double solve_bytes(const mps_engine* e, const DevStats& h) {
     const double nnz = (double)h.nnz_off, n = (double)e->n, it = (double)h.cg_iterations;
     if (e->precision == MPS_PRECISION_FP64) return it * (12.0 * nnz + 116.0 * n) + 36.0 * n;
-    const bool mg = e->mg.enabled && e->mg_requested;
+    const bool mg = e->mg.enabled && e->mg_requested != 0;
+    const bool additive = mg && e->mg_requested == 1;
     const double ent = e->c.planar ? 5.0 : 8.0;
-    double per_it = mg ? (3.0 * ent * nnz + 143.0 * n) : (ent * nnz + 65.0 * n);
+    double per_it = !mg ? (ent * nnz + 65.0 * n)
+                        : additive ? (ent * nnz + 89.0 * n) : (3.0 * ent * nnz + 143.0 * n);
     if (mg)
         for (int l = 1; l <= e->mg.nlev; l++) per_it += 96.0 * e->mg.lev[l].nx * e->mg.lev[l].ny;
     const double ref = (double)h.refinements + 1.0;
@@ -531,6 +535,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         g.enabled = 1;
         g.omega = 0.9f;
         g.scale = 1.5f;
+        g.additive = 1;
         int nx = c.numX, ny = c.numY, l = 1;
         for (;;) {
             g.lev[l].nx = nx;
@@ -620,14 +625,15 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
     return MPS_OK;
 }
 
-int mps_set_multigrid(mps_engine* e, int32_t enabled, float omega, float scale) {
+int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale) {
     if (!e) return fail(MPS_ERR_ARG, "null engine");
-    if (enabled && !e->mg.enabled)
+    if (mode < 0 || mode > 2) return fail(MPS_ERR_ARG, "multigrid mode must be 0, 1 or 2");
+    if (mode && !e->mg.enabled)
         return fail(MPS_ERR_ARG, "multigrid needs a planar scene (2-D, constant z)");
     if (!(omega > 0.f && omega < 1.f) || !(scale >= 1.f && scale < 2.f))
         return fail(MPS_ERR_ARG, "multigrid weights out of range (0 < omega < 1, 1 <= scale < 2)");
     drop_graphs(e);
-    e->mg_requested = enabled ? 1 : 0;
+    e->mg_requested = mode;
     e->mg.omega = omega;
     e->mg.scale = scale;
     return MPS_OK;

@@ -206,6 +206,10 @@ struct Mg {
     int32_t nc;
     float omega;    // damped-Jacobi weight
     float scale;    // coarse-correction scale
+    // 0: multiplicative V(1,1) from level 0 (Jacobi pre- and post-smoothing
+    // around the coarse correction); 1: additive at level 0, u = omega D^-1 r
+    // + scale P V1(P^T r) (no level-0 operator pass; still SPD)
+    int32_t additive;
 };
 
 // --------------------------------------------------------------- solver.cu

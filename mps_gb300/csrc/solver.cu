@@ -609,7 +609,10 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     // the fluid's part of the tank, and a contiguous split would hand them all
     // to a few blocks while the rest wait at the next barrier.
     const int gcell = ((threadIdx.x >> 5) * gb.size + gb.rank) * 32 + (threadIdx.x & 31);
-    // level 0 residual of the Inner particles (coalesced, one row per thread)
+    // level 0 residual of the Inner particles (coalesced, one row per thread);
+    // the additive form restricts r itself
+    const float* src0 = mg.additive ? r : mg.res0;
+    if (!mg.additive) {
     for (int i = gtid; i < n; i += 2 * gsz) {
         const int i2 = i + gsz < n ? i + gsz : -1;
         float o, o2;
@@ -623,6 +626,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         }
     }
     if (!grid_sync(gb, ds)) return false;
+    }
     // level 1: sum over each cell's contiguous slots; pre-smooth
     {
         MgLevel& L1 = mg.lev[1];
@@ -630,7 +634,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         for (int I = gcell; I < n1; I += gsz) {
             const int b = __ldg(mf.cs + I), e = __ldg(mf.cs + I + 1);
             float acc = 0.f;
-            for (int i = b; i < e; i++) acc += __ldcg(mg.res0 + i);
+            for (int i = b; i < e; i++) acc += __ldcg(src0 + i);
             L1.r[I] = acc;
             L1.e[I] = mg.omega * __ldg(L1.invd + I) * acc;
         }
@@ -663,6 +667,30 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         float* tmp = L.e;
         L.e = L.t;
         L.t = tmp;
+    }
+    if (mg.additive) {
+        // u = omega D^-1 r + scale * (level-1 correction of the row's cell)
+        MgLevel& L1 = mg.lev[1];
+        const int n1 = L1.nx * L1.ny;
+        for (int i0 = gtid; i0 < n; i0 += 4 * gsz) {
+            float dg[4], ri[4], ec[4];
+            int key[4];
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int i = min(i0 + h * gsz, n - 1);
+                dg[h] = A.diag32[i];
+                key[h] = min(__ldg(mf.skey + i), n1 - 1);
+                ri[h] = __ldcg(r + i);
+            }
+#pragma unroll
+            for (int h = 0; h < 4; h++) ec[h] = __ldcg(L1.e + key[h]);
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int i = i0 + h * gsz;
+                if (i < n) u[i] = dg[h] > 0.f ? fmaf(mg.scale, ec[h], (mg.omega / dg[h]) * ri[h]) : 0.f;
+            }
+        }
+        return true;
     }
     // level 1 -> 0: prolongate to the Inner particles, then post-smooth
     {

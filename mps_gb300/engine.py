@@ -218,9 +218,14 @@ class Engine:
     def set_solver(self, precision=FP64, tol=0.0, max_iter=0):
         _check(_lib.mps_set_solver(self._h, int(precision), float(tol), int(max_iter)))
 
-    def set_multigrid(self, enabled=True, omega=0.9, scale=1.5):
-        """Preconditioner of the MIXED solver: aggregation multigrid or Jacobi."""
-        _check(_lib.mps_set_multigrid(self._h, 1 if enabled else 0, float(omega), float(scale)))
+    MG_JACOBI, MG_ADDITIVE, MG_MULTIPLICATIVE = 0, 1, 2
+
+    def set_multigrid(self, mode=1, omega=0.9, scale=1.5):
+        """Preconditioner of the MIXED solver: 0 Jacobi, 1 multigrid additive at
+        the particle level (default), 2 multiplicative V(1,1) (True/False map
+        to 1/0)."""
+        mode = int(mode) if not isinstance(mode, bool) else (1 if mode else 0)
+        _check(_lib.mps_set_multigrid(self._h, mode, float(omega), float(scale)))
 
     def set_graphs(self, enabled=True):
         """Non-export steps as CUDA graph replays (default) or eager launches."""
