@@ -110,9 +110,10 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
  * u = omega D^-1 r + scale P V(P^T r) with V a V(1,1) cycle over the cell
  * grids (one operator pass per iteration); mode 2: the multiplicative
  * V(1,1) cycle from the particle level (three operator passes per
- * iteration, fewer iterations).  omega = damped-Jacobi weight in (0,1),
- * scale = coarse-correction weight in [1,2) (default 0.9, 1.5).  No
- * counterpart in the reference (its CG is Jacobi-preconditioned). */
+ * iteration, fewer iterations).  omega = Jacobi weight in (0,1],
+ * scale = coarse-correction weight in [1,2); 0 picks the mode's default
+ * (mode 1: 1.0, 1.4; mode 2: 0.9, 1.5).  No counterpart in the reference
+ * (its CG is Jacobi-preconditioned). */
 int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale);
 
 /* Non-export steps run as a CUDA graph replay (default on): the first step

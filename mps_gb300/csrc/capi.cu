@@ -253,10 +253,11 @@ void enqueue_step(mps_engine* e, bool do_export) {
 // the row's own entry).  Per stored off-diagonal entry and pass: FP64 12 B
 // (column + value), compact FP32 5 B (value + index byte).  Per row and
 // iteration: FP64 CG 116 B (8 vectors); MIXED inner iteration 65 B with the
-// Jacobi preconditioner; with the multigrid V-cycle ~96 B per coarse-grid
-// cell (two 9-point stencil reads + 6 vector words) and, additive at level
-// 0, 89 B per row, multiplicative 143 B per row and two more level-0
-// operator passes.  MIXED adds per refinement the FP64
+// Jacobi preconditioner; with the multigrid V-cycle, per cell of level 1
+// 72 B (segment bounds, the up pass's 9-point stencil and 8 vector words)
+// and of levels >= 2 132 B (the same plus the 4x4 restriction weights), and,
+// additive at level 0, 89 B per row, multiplicative 143 B per row and two
+// more level-0 operator passes.  MIXED adds per refinement the FP64
 // residual (12 B/entry + 36 B/row) and once the FP32 operator setup
 // (17 B/entry + 16 B/row written and read).
 double solve_bytes(const mps_engine* e, const DevStats& h) {
@@ -268,7 +269,8 @@ double solve_bytes(const mps_engine* e, const DevStats& h) {
     double per_it = !mg ? (ent * nnz + 65.0 * n)
                         : additive ? (ent * nnz + 89.0 * n) : (3.0 * ent * nnz + 143.0 * n);
     if (mg)
-        for (int l = 1; l <= e->mg.nlev; l++) per_it += 96.0 * e->mg.lev[l].nx * e->mg.lev[l].ny;
+        for (int l = 1; l <= e->mg.nlev; l++)
+            per_it += (l == 1 ? 72.0 : 132.0) * e->mg.lev[l].nx * e->mg.lev[l].ny;
     const double ref = (double)h.refinements + 1.0;
     return it * per_it + ref * (12.0 * nnz + 36.0 * n) + (17.0 * nnz + 16.0 * n);
 }
@@ -370,6 +372,23 @@ int run_one_step(mps_engine* e, bool do_export, mps_step_stats* stats) {
     CU(cudaGetLastError());
     fill_stats(e, stats);
     return check_status(e);
+}
+
+// Default multigrid weights per mode.  Additive (mode 1): the particle-level
+// term omega D^-1 r only has to be positive, and the cell-level V(1,1) uses
+// the same omega on Galerkin 9-point stencils, whose Jacobi spectrum
+// D^-1 A_c stays well below 2, so undamped Jacobi still smooths there;
+// omega 1, s 1.4 took the fewest CG iterations on the 1M dam break (69 vs
+// 73 at 0.9/1.5).  Multiplicative (mode 2) smooths the particle matrix
+// itself, whose D^-1 A can approach 2: there the damped 0.9 stays.
+void mg_default_weights(int mode, float* omega, float* scale) {
+    if (mode == 2) {
+        *omega = 0.9f;
+        *scale = 1.5f;
+    } else {
+        *omega = 1.0f;
+        *scale = 1.4f;
+    }
 }
 
 }  // namespace
@@ -533,8 +552,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     if (c.planar) {
         Mg& g = e->mg;
         g.enabled = 1;
-        g.omega = 0.9f;
-        g.scale = 1.5f;
+        mg_default_weights(1, &g.omega, &g.scale);
         g.additive = 1;
         int nx = c.numX, ny = c.numY, l = 1;
         for (;;) {
@@ -543,7 +561,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
             size_t cells = (size_t)nx * ny;
             if (e->alloc(&g.lev[l].st, 9 * cells) || e->alloc(&g.lev[l].invd, cells) ||
                 e->alloc(&g.lev[l].r, cells) || e->alloc(&g.lev[l].e, cells) ||
-                e->alloc(&g.lev[l].t, cells))
+                e->alloc(&g.lev[l].t, cells) || (l >= 2 && e->alloc(&g.lev[l].rw, 16 * cells)))
                 return bail(fail(MPS_ERR_CUDA, "cudaMalloc multigrid level"));
             if (cells <= (size_t)kMgMaxCoarsest || l == kMgMaxLevels - 1) break;
             nx = (nx + 1) / 2;
@@ -630,8 +648,12 @@ int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale) {
     if (mode < 0 || mode > 2) return fail(MPS_ERR_ARG, "multigrid mode must be 0, 1 or 2");
     if (mode && !e->mg.enabled)
         return fail(MPS_ERR_ARG, "multigrid needs a planar scene (2-D, constant z)");
-    if (!(omega > 0.f && omega < 1.f) || !(scale >= 1.f && scale < 2.f))
-        return fail(MPS_ERR_ARG, "multigrid weights out of range (0 < omega < 1, 1 <= scale < 2)");
+    float dw, ds;
+    mg_default_weights(mode, &dw, &ds);
+    if (omega == 0.f) omega = dw;
+    if (scale == 0.f) scale = ds;
+    if (!(omega > 0.f && omega <= 1.f) || !(scale >= 1.f && scale < 2.f))
+        return fail(MPS_ERR_ARG, "multigrid weights out of range (0 < omega <= 1, 1 <= scale < 2)");
     drop_graphs(e);
     e->mg_requested = mode;
     e->mg.omega = omega;

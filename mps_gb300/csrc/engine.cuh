@@ -194,6 +194,12 @@ struct MgLevel {
     float* st;    // 9 x (nx*ny), direction d = (dx+1)*3 + (dy+1), d = 4 is the diagonal
     float* invd;  // 1 / diagonal, 0 for cells without unknowns
     float *r, *e, *t;
+    // levels >= 2: restriction weights, 16 x (nx*ny).  Coarse cell (X, Y)
+    // gets the pre-smoothed residual of the finer level as
+    // sum_k rw[k] r_f(2X - 1 + k / 4, 2Y - 1 + k % 4): the 2x2 children's
+    // residuals after one Jacobi step from zero, folded into one 4x4 stencil
+    // on the finer residual alone
+    float* rw;
 };
 struct Mg {
     int32_t enabled;

@@ -64,30 +64,44 @@ __global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L) {
     L.invd[I] = st[4] > 0.f ? 1.f / st[4] : 0.f;
 }
 
-__global__ void k_mg_coarsen(MgLevel F, MgLevel C) {
+// Coarse level C from fine level F: the Galerkin 9-point stencil and C's
+// restriction weights (MgLevel::rw).  The residual that the V-cycle hands
+// from F to C is, for each child c of a coarse cell, r_c - sum_d st_d(c)
+// omega invd_j r_j (one Jacobi step from zero on F, then its residual);
+// summed over the 2x2 children it is a fixed 4x4 stencil on r_F, whose
+// weights depend only on the operator and omega.
+__global__ void k_mg_coarsen(MgLevel F, MgLevel C, float omega) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int nc = C.nx * C.ny;
     if (I >= nc) return;
     const int X = I / C.ny, Y = I - X * C.ny;
     const int nf = F.nx * F.ny;
-    float st[9];
+    float st[9], w[16];
 #pragma unroll
     for (int d = 0; d < 9; d++) st[d] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; k++) w[k] = 0.f;
     for (int a = 0; a < 2; a++)
         for (int bb = 0; bb < 2; bb++) {
             const int x = 2 * X + a, y = 2 * Y + bb;
             if (x >= F.nx || y >= F.ny) continue;
             const int cf = x * F.ny + y;
+            w[(a + 1) * 4 + (bb + 1)] += 1.f;
             for (int d = 0; d < 9; d++) {
                 const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
                 if (nx < 0 || ny < 0 || nx >= F.nx || ny >= F.ny) continue;
+                const float s = F.st[(size_t)d * nf + cf];
                 const int DX = nx / 2 - X, DY = ny / 2 - Y;
-                st[(DX + 1) * 3 + (DY + 1)] += F.st[(size_t)d * nf + cf];
+                st[(DX + 1) * 3 + (DY + 1)] += s;
+                // tap (nx, ny) sits at (nx - 2X + 1, ny - 2Y + 1) of the 4x4 patch
+                w[(nx - 2 * X + 1) * 4 + (ny - 2 * Y + 1)] -= omega * F.invd[nx * F.ny + ny] * s;
             }
         }
 #pragma unroll
     for (int d = 0; d < 9; d++) C.st[(size_t)d * nc + I] = st[d];
     C.invd[I] = st[4] > 0.f ? 1.f / st[4] : 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; k++) C.rw[(size_t)k * nc + I] = w[k];
 }
 
 // Dense inverse of the coarsest operator; cells without unknowns get an
@@ -141,7 +155,7 @@ void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg&
     ++g_launches;
     for (int l = 1; l < mg.nlev; l++) {
         const MgLevel& C = mg.lev[l + 1];
-        k_mg_coarsen<<<(C.nx * C.ny + T - 1) / T, T, 0, st>>>(mg.lev[l], C);
+        k_mg_coarsen<<<(C.nx * C.ny + T - 1) / T, T, 0, st>>>(mg.lev[l], C, mg.omega);
         ++g_launches;
     }
     k_mg_dense<<<1, 1024, 0, st>>>(mg.lev[mg.nlev], mg.dense);

@@ -39,6 +39,7 @@ namespace {
 // each grid barrier.  Batched solves (many scenes in one launch) run the same
 // code on groups of blocks, each group with its own barrier and partials.
 constexpr int kBlock = 1024;
+constexpr int kMixedBlock = 1024;  // k_cg_mixed: one block per SM
 constexpr long long kSpinLimit = 1ll << 25;  // ~1-2 s with the back-off below
 
 struct SolveArgs {
@@ -91,15 +92,24 @@ __device__ __forceinline__ bool grid_sync(GridBar& gb, DevStats* ds) {
         red_release_add(gb.count, 1u);
         bool ok = true;
         long long it = 0;
+        // Passing needs every block's arrival, so a block that gave up never
+        // lets the others past the next barrier: they learn of it here, on
+        // the slow path, from the status flag (no extra load when passing).
         while ((int)(ld_acquire(gb.count) - target) < 0) {
-            if (++it > kSpinLimit) {
-                atomicOr(&ds->status, ST_TIMEOUT);
-                ok = false;
-                break;
+            if (++it > 256) {
+                __nanosleep(16);
+                if ((it & 1023) == 0 && (*(volatile int*)&ds->status & ST_TIMEOUT)) {
+                    ok = false;
+                    break;
+                }
+                if (it > kSpinLimit) {
+                    atomicOr(&ds->status, ST_TIMEOUT);
+                    ok = false;
+                    break;
+                }
             }
-            if (it > 256) __nanosleep(16);
         }
-        s_ok = ok && !(*(volatile int*)&ds->status & ST_TIMEOUT);
+        s_ok = ok;
     }
     __syncthreads();
     return s_ok != 0;
@@ -252,40 +262,33 @@ __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf
 }
 
 // Compact sums of two rows of different slices at once (their groups'
-// loads interleaved: twice the memory traffic in flight per thread).  Each
-// row keeps its own order (group by group, a0: entries 0, 2; a1: 1, 3), so
-// the results equal compact_row_sum's.
-__device__ __forceinline__ void compact_rows2(const Ppe& A, const MatFree& mf, int K, int ra, int rb,
-                                              const float* __restrict__ u, float& oa, float& ob) {
-    const int wa = __ldg(A.slice_w + (ra >> 5)), wb = __ldg(A.slice_w + (rb >> 5));
-    const int sa[3] = {__ldg(mf.rs + ra), __ldg(mf.rs + mf.rs_stride + ra), __ldg(mf.rs + 2 * mf.rs_stride + ra)};
-    const int sb[3] = {__ldg(mf.rs + rb), __ldg(mf.rs + mf.rs_stride + rb), __ldg(mf.rs + 2 * mf.rs_stride + rb)};
+// loads interleaved: twice the memory traffic in flight per thread), given
+// both rows' slice widths (both > 0) and range starts.  One loop over the wider row's
+// groups, two groups of each row per pass; past a row's own groups it
+// re-reads its last group with weight 0, which adds exactly +0, so each
+// row's sum equals compact_row_sum's (group by group, a0: entries 0, 2;
+// a1: 1, 3) without a serial tail per row.
+__device__ __forceinline__ void compact_pair(const Ppe& A, const MatFree& mf, int K, int ra, int rb,
+                                             int wa, int wb, const int (&sa)[3], const int (&sb)[3],
+                                             const float* __restrict__ u, float& oa, float& ob) {
     const float4* vpa = reinterpret_cast<const float4*>(A.val32) + (qsell_index(ra, 0, K) >> 2);
     const float4* vpb = reinterpret_cast<const float4*>(A.val32) + (qsell_index(rb, 0, K) >> 2);
     const uint32_t* ipa = reinterpret_cast<const uint32_t*>(mf.idx8) + (qsell_index(ra, 0, K) >> 2);
     const uint32_t* ipb = reinterpret_cast<const uint32_t*>(mf.idx8) + (qsell_index(rb, 0, K) >> 2);
-    auto col = [](const int* st, uint32_t b4, int t) {
+    auto col = [](const int (&st)[3], uint32_t b4, int t) {
         const uint32_t b = (b4 >> (8 * t)) & 255u;
         const uint32_t r = b >> 6;
         return (r == 0 ? st[0] : (r == 1 ? st[1] : st[2])) + (int)(b & 63u);
     };
-    auto group = [&](const float4& v, uint32_t b4, const int* st, float& a0, float& a1) {
-        float x[4];
-#pragma unroll
-        for (int t = 0; t < 4; t++) x[t] = __ldcg(u + col(st, b4, t));
-        a0 = fmaf(v.x, x[0], a0);
-        a1 = fmaf(v.y, x[1], a1);
-        a0 = fmaf(v.z, x[2], a0);
-        a1 = fmaf(v.w, x[3], a1);
-    };
-    const int ga = (wa + 3) >> 2, gb = (wb + 3) >> 2, gm = min(ga, gb);
+    const int ga = (wa + 3) >> 2, gb = (wb + 3) >> 2, gmax = max(ga, gb);
     float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
-    int g = 0;
-    for (; g + 2 <= gm; g += 2) {
-        const float4 va0 = __ldg(vpa + g * 32), va1 = __ldg(vpa + (g + 1) * 32);
-        const float4 vb0 = __ldg(vpb + g * 32), vb1 = __ldg(vpb + (g + 1) * 32);
-        const uint32_t ia0 = __ldg(ipa + g * 32), ia1 = __ldg(ipa + (g + 1) * 32);
-        const uint32_t ib0 = __ldg(ipb + g * 32), ib1 = __ldg(ipb + (g + 1) * 32);
+    for (int g = 0; g < gmax; g += 2) {
+        const int ha0 = min(g, ga - 1), ha1 = min(g + 1, ga - 1);
+        const int hb0 = min(g, gb - 1), hb1 = min(g + 1, gb - 1);
+        float4 va0 = __ldg(vpa + ha0 * 32), va1 = __ldg(vpa + ha1 * 32);
+        float4 vb0 = __ldg(vpb + hb0 * 32), vb1 = __ldg(vpb + hb1 * 32);
+        const uint32_t ia0 = __ldg(ipa + ha0 * 32), ia1 = __ldg(ipa + ha1 * 32);
+        const uint32_t ib0 = __ldg(ipb + hb0 * 32), ib1 = __ldg(ipb + hb1 * 32);
         float xa[8], xb[8];
 #pragma unroll
         for (int t = 0; t < 4; t++) {
@@ -294,6 +297,11 @@ __device__ __forceinline__ void compact_rows2(const Ppe& A, const MatFree& mf, i
             xb[t] = __ldcg(u + col(sb, ib0, t));
             xb[4 + t] = __ldcg(u + col(sb, ib1, t));
         }
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (g >= ga) va0 = z;
+        if (g + 1 >= ga) va1 = z;
+        if (g >= gb) vb0 = z;
+        if (g + 1 >= gb) vb1 = z;
         a0 = fmaf(va0.x, xa[0], a0);
         a1 = fmaf(va0.y, xa[1], a1);
         a0 = fmaf(va0.z, xa[2], a0);
@@ -311,8 +319,6 @@ __device__ __forceinline__ void compact_rows2(const Ppe& A, const MatFree& mf, i
         b0 = fmaf(vb1.z, xb[6], b0);
         b1 = fmaf(vb1.w, xb[7], b1);
     }
-    for (int h = g; h < ga; h++) group(__ldg(vpa + h * 32), __ldg(ipa + h * 32), sa, a0, a1);
-    for (int h = g; h < gb; h++) group(__ldg(vpb + h * 32), __ldg(ipb + h * 32), sb, b0, b1);
     oa = a0 + a1;
     ob = b0 + b1;
 }
@@ -323,15 +329,30 @@ __device__ __forceinline__ float off_row(const Ppe& A, const MatFree& mf, int K,
     return (mf.enabled && !mf.sell_row[i]) ? compact_row_sum(A, mf, K, i, v) : spmv32_sell_row(A, K, i, v);
 }
 
-// Off-diagonal parts of rows i and i2 (i2 < 0: none), paired when both are compact.
+// Off-diagonal parts of rows i and i2 (i2 < 0: none), paired when both are
+// compact.  Both rows' format flags, slice widths and range starts are loaded
+// in one batch, before the branch that needs the flags.
 __device__ __forceinline__ void off_rows(const Ppe& A, const MatFree& mf, int K, int i, int i2,
                                          const float* __restrict__ v, float& o, float& o2) {
-    if (mf.enabled && i2 >= 0 && !mf.sell_row[i] && !mf.sell_row[i2]) {
-        compact_rows2(A, mf, K, i, i2, v, o, o2);
+    if (!mf.enabled) {
+        o = spmv32_sell_row(A, K, i, v);
+        o2 = i2 >= 0 ? spmv32_sell_row(A, K, i2, v) : 0.f;
         return;
     }
-    o = off_row(A, mf, K, i, v);
-    o2 = i2 >= 0 ? off_row(A, mf, K, i2, v) : 0.f;
+    const int j2 = i2 >= 0 ? i2 : i;  // a lone row is paired with itself
+    const int8_t fa = mf.sell_row[i], fb = mf.sell_row[j2];
+    const int wa = __ldg(A.slice_w + (i >> 5)), wb = __ldg(A.slice_w + (j2 >> 5));
+    const int sa[3] = {__ldg(mf.rs + i), __ldg(mf.rs + mf.rs_stride + i), __ldg(mf.rs + 2 * mf.rs_stride + i)};
+    const int sb[3] = {__ldg(mf.rs + j2), __ldg(mf.rs + mf.rs_stride + j2), __ldg(mf.rs + 2 * mf.rs_stride + j2)};
+    // pairs need a group in each row (a slice of rows without off-diagonals
+    // has width 0 and no stored groups at all)
+    if (!fa && !fb && wa > 0 && wb > 0) {
+        compact_pair(A, mf, K, i, j2, wa, wb, sa, sb, v, o, o2);
+        if (i2 < 0) o2 = 0.f;
+        return;
+    }
+    o = fa ? spmv32_sell_row(A, K, i, v) : compact_row_sum(A, mf, K, i, v);
+    o2 = i2 < 0 ? 0.f : (fb ? spmv32_sell_row(A, K, i2, v) : compact_row_sum(A, mf, K, i2, v));
 }
 
 // ----------------------------------------------------------------- FP64 CG
@@ -439,18 +460,9 @@ __device__ __forceinline__ double f2d(const F2& a) { return (double)a.hi + (doub
 __device__ __forceinline__ float ldv(const float* p, int i) { return __ldcg(p + i); }
 __device__ __forceinline__ float ldc(const float* p, size_t i) { return __ldg(p + i); }
 
-// 9-point stencil row of a structured level.
-__device__ __forceinline__ float stencil_row(const MgLevel& L, int I, const float* __restrict__ v) {
-    const int n = L.nx * L.ny;
-    const int x = I / L.ny, y = I - x * L.ny;
-    float acc = 0.f;
-#pragma unroll
-    for (int d = 0; d < 9; d++) {
-        const int nx = x + d / 3 - 1, ny = y + d % 3 - 1;
-        if (nx < 0 || ny < 0 || nx >= L.nx || ny >= L.ny) continue;
-        acc = fmaf(__ldg(L.st + (size_t)d * n + I), __ldcg(v + nx * L.ny + ny), acc);
-    }
-    return acc;
+constexpr bool kPrefetchStencil = true;
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
 // Tap (dx, dy) of a 9-point stencil at (x, y): the neighbour's index,
@@ -462,51 +474,49 @@ __device__ __forceinline__ int tap(const MgLevel& L, int x, int y, int d, bool& 
     return min(max(nx, 0), L.nx - 1) * L.ny + min(max(ny, 0), L.ny - 1);
 }
 
-// residual of level l restricted to level l+1 (sum over the 2x2 children).
-// Every load depends only on the cell's position and is unconditional (taps
-// clamped, then masked), so a child's 20 loads are in flight together: one
-// memory round trip per child, which after a grid barrier is an L2 access,
-// often on the other die (with a branch per tap, each tap was a round trip).  Cells without unknowns hold zero stencils, residuals and
-// corrections, so they add exactly 0 and need no test.  Callers skip coarse
-// cells without unknowns (their children have none either: the Galerkin
-// diagonal of an aggregate with an unknown is positive).
-__device__ __forceinline__ float restrict_cell(const MgLevel& F, int X, int Y) {
-    const int n = F.nx * F.ny;
-    float res[4];
-    // children one after another (each child's 20 loads in one batch) keeps
-    // the register footprint small enough not to spill
-#pragma unroll 1
-    for (int ab = 0; ab < 4; ab++) {
-        const int x = 2 * X + (ab >> 1), y = 2 * Y + (ab & 1);
-        const bool in = x < F.nx && y < F.ny;
-        const int xc = min(x, F.nx - 1), yc = min(y, F.ny - 1);
-        const int c = xc * F.ny + yc;
-        float st[9], ev[9];
-        bool ok[9];
+// Pre-smoothed residual of fine level F restricted to cell I = (X, Y) of
+// level C: the 4x4 stencil C.rw on r_F (the children's residual after one
+// Jacobi step from zero, folded at setup).  Taps are clamped into the grid
+// (their weights are 0 there), so all 32 loads are unconditional and in
+// flight together: one memory round trip per coarse cell, which after a
+// grid barrier is an L2 access, often on the other die.
+__device__ __forceinline__ float restrict_cell(const MgLevel& F, const MgLevel& C, int I, int X,
+                                               int Y) {
+    const int nc = C.nx * C.ny;
+    if (kPrefetchStencil) {
+        // the up pass reads the children's 9-point stencils: start moving
+        // them into L2 now (no register or stall cost), since nothing on the
+        // way down reads them any more
+        const size_t nf = (size_t)F.nx * F.ny;
 #pragma unroll
-        for (int d = 0; d < 9; d++) {
-            const int j = tap(F, xc, yc, d, ok[d]);
-            st[d] = ldc(F.st, (size_t)d * n + c);
-            ev[d] = ldv(F.e, j);
+        for (int a = 0; a < 2; a++) {
+            const size_t c = (size_t)min(2 * X + a, F.nx - 1) * F.ny + min(2 * Y, F.ny - 1);
+#pragma unroll
+            for (int d = 0; d < 9; d++) prefetch_l2(F.st + d * nf + c);
         }
-        const float rc = ldv(F.r, c);
-        float s = 0.f;
-#pragma unroll
-        for (int d = 0; d < 9; d++)
-            if (ok[d]) s = fmaf(st[d], ev[d], s);
-        res[ab] = in ? rc - s : 0.f;
     }
-    // the children in the order (0,0), (0,1), (1,0), (1,1)
+    int xs[4], ys[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        xs[k] = min(max(2 * X - 1 + k, 0), F.nx - 1) * F.ny;
+        ys[k] = min(max(2 * Y - 1 + k, 0), F.ny - 1);
+    }
+    float w[16], v[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        w[k] = ldc(C.rw, (size_t)k * nc + I);
+        v[k] = ldv(F.r, xs[k >> 2] + ys[k & 3]);
+    }
     float acc = 0.f;
 #pragma unroll
-    for (int ab = 0; ab < 4; ab++) acc += res[ab];
+    for (int k = 0; k < 16; k++) acc = fmaf(w[k], v[k], acc);
     return acc;
 }
 
 // Post-smoothing of a level with the prolongation folded in: the corrected
 // value of a cell is e + s * e_parent, computed on the fly for the cell and
 // its 8 neighbours, so prolongation needs no pass or barrier of its own.
-// Taps clamped and masked like restrict_cell: all loads in one batch.
+// Taps clamped and masked: all loads in one batch.
 __device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, const MgLevel& C,
                                                 int I) {
     const int n = L.nx * L.ny;
@@ -536,15 +546,17 @@ __device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, 
 // levels (their e/t roles swap after each up-smoothing).
 __device__ void mg_block_levels(const Mg& mg, int lo, MgLevel* lv) {
     const int tid = threadIdx.x, nt = blockDim.x;
+    // level lo's r and pre-smoothed e are already written (by the grid pass)
     for (int l = lo; l < mg.nlev; l++) {
-        MgLevel& L = lv[l];
-        const int n = L.nx * L.ny;
-        for (int I = tid; I < n; I += nt) L.e[I] = mg.omega * ldc(L.invd, I) * ldv(L.r, I);
-        __syncthreads();
+        const MgLevel& L = lv[l];
         MgLevel& C = lv[l + 1];
+        const bool smooth = l + 1 < mg.nlev;
         for (int I = tid; I < C.nx * C.ny; I += nt) {
             const int X = I / C.ny, Y = I - X * C.ny;
-            C.r[I] = ldc(C.invd, I) > 0.f ? restrict_cell(L, X, Y) : 0.f;
+            const float iv = ldc(C.invd, I);
+            const float rr = iv > 0.f ? restrict_cell(L, C, I, X, Y) : 0.f;
+            C.r[I] = rr;
+            if (smooth) C.e[I] = mg.omega * iv * rr;
         }
         __syncthreads();
     }
@@ -627,28 +639,59 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     }
     if (!grid_sync(gb, ds)) return false;
     }
-    // level 1: sum over each cell's contiguous slots; pre-smooth
+    // level 1: sum over each cell's contiguous slots; pre-smooth.  Four of
+    // this thread's cells at once, their slots four at a time, all loads of
+    // a round before any use (predicated: slots past a cell's end are not
+    // read, which also keeps the many empty cells off any one address):
+    // each cell still sums its slots in slot order.
     {
         MgLevel& L1 = mg.lev[1];
         const int n1 = L1.nx * L1.ny;
-        for (int I = gcell; I < n1; I += gsz) {
-            const int b = __ldg(mf.cs + I), e = __ldg(mf.cs + I + 1);
-            float acc = 0.f;
-            for (int i = b; i < e; i++) acc += __ldcg(src0 + i);
-            L1.r[I] = acc;
-            L1.e[I] = mg.omega * __ldg(L1.invd + I) * acc;
+        for (int I0 = gcell; I0 < n1; I0 += 4 * gsz) {
+            int b[4], cnt[4];
+            float iv[4], acc[4];
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int I = min(I0 + h * gsz, n1 - 1);
+                b[h] = __ldg(mf.cs + I);
+                cnt[h] = __ldg(mf.cs + I + 1) - b[h];
+                iv[h] = __ldg(L1.invd + I);
+                acc[h] = 0.f;
+            }
+            const int m = max(max(cnt[0], cnt[1]), max(cnt[2], cnt[3]));
+            for (int j = 0; j < m; j += 4) {
+                float x[4][4];
+#pragma unroll
+                for (int h = 0; h < 4; h++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) x[h][q] = j + q < cnt[h] ? __ldcg(src0 + b[h] + j + q) : 0.f;
+#pragma unroll
+                for (int h = 0; h < 4; h++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (j + q < cnt[h]) acc[h] += x[h][q];
+            }
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int I = I0 + h * gsz;
+                if (I < n1) {
+                    L1.r[I] = acc[h];
+                    L1.e[I] = mg.omega * iv[h] * acc[h];
+                }
+            }
         }
     }
     if (!grid_sync(gb, ds)) return false;
     // grid-wide levels, down: restrict level l into l+1 and pre-smooth there
+    // (every level but the coarsest, whose e comes from its dense inverse)
     for (int l = 1; l <= mg.ngrid; l++) {
         MgLevel& L = mg.lev[l];
         MgLevel& C = mg.lev[l + 1];
-        const bool smooth = l + 1 <= mg.ngrid;
+        const bool smooth = l + 1 < mg.nlev;
         for (int I = gcell; I < C.nx * C.ny; I += gsz) {
             const int X = I / C.ny, Y = I - X * C.ny;
             const float iv = __ldg(C.invd + I);
-            const float rr = iv > 0.f ? restrict_cell(L, X, Y) : 0.f;
+            const float rr = iv > 0.f ? restrict_cell(L, C, I, X, Y) : 0.f;
             C.r[I] = rr;
             if (smooth) C.e[I] = mg.omega * iv * rr;
         }
@@ -683,7 +726,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
                 ri[h] = __ldcg(r + i);
             }
 #pragma unroll
-            for (int h = 0; h < 4; h++) ec[h] = __ldcg(L1.e + key[h]);
+            for (int h = 0; h < 4; h++) ec[h] = dg[h] > 0.f ? __ldcg(L1.e + key[h]) : 0.f;
 #pragma unroll
             for (int h = 0; h < 4; h++) {
                 const int i = i0 + h * gsz;
@@ -709,7 +752,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
                 e0[h] = __ldcg(mg.e0 + i);
             }
 #pragma unroll
-            for (int h = 0; h < 4; h++) ec[h] = __ldcg(L1.e + key[h]);
+            for (int h = 0; h < 4; h++) ec[h] = dg[h] > 0.f ? __ldcg(L1.e + key[h]) : 0.f;
 #pragma unroll
             for (int h = 0; h < 4; h++) {
                 const int i = i0 + h * gsz;
@@ -805,20 +848,26 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
             // Surface, Ignored, ghosts) get w = +0
             for (int i = gtid; i < a.n; i += 2 * gsz) {
                 const int i2 = i + gsz < a.n ? i + gsz : -1;
+                // the rows' own words first: in flight with the operator's
+                float ui[2], dg[2], rv[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int row = h == 0 || i2 < 0 ? i : i2;
+                    ui[h] = __ldcg(kv.u32 + row);
+                    dg[h] = A.diag32[row];
+                    rv[h] = kv.r32[row];
+                }
                 float o, o2;
                 off_rows(A, mf, a.K, i, i2, kv.u32, o, o2);
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int row = h == 0 ? i : i2;
                     if (row < 0) break;
-                    const float ui = __ldcg(kv.u32 + row);
-                    const float dg = A.diag32[row];
-                    const float w = dg > 0.f ? fmaf(dg, ui, h == 0 ? o : o2) : 0.f;
+                    const float w = dg[h] > 0.f ? fmaf(dg[h], ui[h], h == 0 ? o : o2) : 0.f;
                     kv.w32[row] = w;
-                    const float r = kv.r32[row];
-                    acc_prod(g, r, ui);
-                    acc_prod(dl, w, ui);
-                    acc_prod(rr, r, r);
+                    acc_prod(g, rv[h], ui[h]);
+                    acc_prod(dl, w, ui[h]);
+                    acc_prod(rr, rv[h], rv[h]);
                 }
             }
             double v3[3] = {f2d(g), f2d(dl), f2d(rr)}, t3[3];
@@ -889,10 +938,10 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
     }
 }
 
-__global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg, Krylov kv,
-                                                        SolveArgs a, DevStats* ds) {
+__global__ void __launch_bounds__(kMixedBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg, Krylov kv,
+                                                             SolveArgs a, DevStats* ds) {
     GridBar gb = whole_grid(kv);
-    solve_mixed<kBlock>(A, mf, mg, kv, a, ds, gb);
+    solve_mixed<kMixedBlock>(A, mf, mg, kv, a, ds, gb);
 }
 
 // Many scenes in one persistent launch: block b belongs to group bmap[b].x
@@ -992,7 +1041,7 @@ SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
 
 void solver_setup(Krylov& k, int32_t /*n_pad*/, int device) {
     int g1 = coop_grid((const void*)k_cg64, device, kBlock, 0, 1);
-    int g2 = coop_grid((const void*)k_cg_mixed, device, kBlock, 0, 1);
+    int g2 = coop_grid((const void*)k_cg_mixed, device, kMixedBlock, 0, 1);
     k.grid = g1 < g2 ? g1 : g2;
     k.block = kBlock;
 }
@@ -1128,7 +1177,7 @@ void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const 
     Krylov kk = k;
     void* args[] = {&AA, &mm, &gg, &kk, &a, &ds};
     cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
-    cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kBlock), args, 0, st);
+    cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kMixedBlock), args, 0, st);
     ++g_launches;
 }
 

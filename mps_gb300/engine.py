@@ -220,10 +220,10 @@ class Engine:
 
     MG_JACOBI, MG_ADDITIVE, MG_MULTIPLICATIVE = 0, 1, 2
 
-    def set_multigrid(self, mode=1, omega=0.9, scale=1.5):
+    def set_multigrid(self, mode=1, omega=0.0, scale=0.0):
         """Preconditioner of the MIXED solver: 0 Jacobi, 1 multigrid additive at
         the particle level (default), 2 multiplicative V(1,1) (True/False map
-        to 1/0)."""
+        to 1/0).  omega/scale 0 take the mode's default weights."""
         mode = int(mode) if not isinstance(mode, bool) else (1 if mode else 0)
         _check(_lib.mps_set_multigrid(self._h, mode, float(omega), float(scale)))
 
