@@ -380,7 +380,7 @@ def run_ours(args, rank: int, world: int, dist):
     sb = [s["solve_bytes"] for s in stats]  # the engine's algorithmic-bytes model
     achieved = sum(sb) / (sum(solve_ms) / 1e3) / 1e9
     row_iters = sum(s["cg_iterations"] for s in stats) * n / len(stats)
-    tpr = traffic_per_row_iter("cg_mixed" if prec == MIXED else "cg64")
+    tpr = traffic_per_row_iter("k_cg_mixed" if prec == MIXED else "k_cg64")
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                 "frac": round(achieved / hbm_peak, 4),
                 "traffic": (tpr * row_iters) if tpr else None,
