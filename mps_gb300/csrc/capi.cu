@@ -539,7 +539,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         e->alloc(&e->kv.totals, 8) || e->alloc(&e->mf.idx8, np * K) ||
         e->alloc(&e->mf.sell_row, np) || e->alloc(&e->mf.rs, 3 * np) ||
         e->alloc(&e->cand_cnt, np + 1) || e->alloc(&e->cand_base, np + 2) ||
-        e->alloc(&e->parent, np) || e->alloc(&e->has_surface, np) || e->alloc(&e->ax, np) ||
+        e->alloc(&e->parent, np + 1) || e->alloc(&e->has_surface, np) || e->alloc(&e->ax, np) ||
         e->alloc(&e->ay, np) || e->alloc(&e->az, np) || e->alloc(&e->stage, 9 * np) ||
         e->alloc(&e->stage_i, 3 * np) || e->alloc(&e->dflag, 1) || e->alloc(&e->ds, 1))
         return bail(fail(MPS_ERR_CUDA, "cudaMalloc failed (out of device memory?)"));

@@ -17,6 +17,14 @@ namespace mpsg {
 
 namespace {
 
+// Adds v to stencil entry d, the nine entries kept in registers (an
+// indexed local array would live in local memory); the other entries add
+// +0, which leaves them unchanged, so the sums equal one indexed add.
+__device__ __forceinline__ void add_tap(float (&st)[9], int d, float v) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) st[q] += q == d ? v : 0.f;
+}
+
 __global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= L.nx * L.ny) return;
@@ -36,26 +44,46 @@ __global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L) {
         const float dg = A.diag32[k];
         if (!(dg > 0.f)) continue;  // not an unknown (not Inner)
         st[4] += dg;
-        const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
         const int cnt = A.offcnt[k];
-        const bool compact = mf.enabled && !mf.sell_row[k];
-        for (int m = 0; m < cnt; m++) {
-            const float v = A.val32[qsell_index(k, m, c.K)];
-            int dx, dy;
-            if (compact) {
-                const int bt = mf.idx8[qsell_index(k, m, c.K)];
-                const int r = bt >> 6;
-                const int j = rs[r][0] + (bt & 63);
-                dx = r - 1;
-                dy = (j >= rs[r][1]) + (j >= rs[r][2]) - 1;
-            } else {
+        if (mf.enabled && !mf.sell_row[k]) {
+            // compact row: four groups of four entries per round of loads,
+            // entries added in order
+            const size_t q0 = qsell_index(k, 0, c.K) >> 2;
+            const float4* vp = reinterpret_cast<const float4*>(A.val32) + q0;
+            const uint32_t* ip = reinterpret_cast<const uint32_t*>(mf.idx8) + q0;
+            const int ng = (cnt + 3) >> 2;
+            for (int g0 = 0; g0 < ng; g0 += 4) {
+                float4 v[4];
+                uint32_t b4[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int gi = min(g0 + q, ng - 1);
+                    v[q] = __ldg(vp + gi * 32);
+                    b4[q] = __ldg(ip + gi * 32);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float vv[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
+#pragma unroll
+                    for (int t = 0; t < 4; t++) {
+                        if ((g0 + q) * 4 + t >= cnt) break;
+                        const int bt = (b4[q] >> (8 * t)) & 255;
+                        const int r = bt >> 6;
+                        const int j = rs[r][0] + (bt & 63);
+                        const int dy = (j >= rs[r][1]) + (j >= rs[r][2]) - 1;
+                        add_tap(st, r * 3 + (dy + 1), vv[t]);
+                    }
+                }
+            }
+        } else {
+            const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
+            for (int m = 0; m < cnt; m++) {
+                const float v = A.val32[qsell_index(k, m, c.K)];
                 const int j = A.col[base + (size_t)m * 32];
                 const int kj = mf.skey[j];
                 const int jx = kj / c.numY, jy = kj - jx * c.numY;
-                dx = jx - cx;
-                dy = jy - cy;
+                add_tap(st, (jx - cx + 1) * 3 + (jy - cy + 1), v);
             }
-            st[(dx + 1) * 3 + (dy + 1)] += v;
         }
     }
     const int n = L.nx * L.ny;

@@ -471,14 +471,72 @@ __global__ void k_cc_init(int n, int* par) {
     if (k < n) par[k] = k;
 }
 
-__global__ void __launch_bounds__(kThreads) k_cc_hook(Consts c, StateBuf s, NbList nb, int* par,
+// Sampled linking (the Afforest scheme of Sutton et al., 2018): almost every
+// particle of a scene belongs to one large component, and its edges need not
+// all be processed.  Pass 1 joins each particle to the components of its first
+// kCcLinks neighbours within re_p; after full compression, the most frequent
+// root of a fixed sample of particles names the large component; pass 2 runs
+// every edge of each particle outside it.  Every edge with an endpoint outside
+// the large component is then processed from that endpoint (the pressure
+// phase's lists are symmetric and hold no ghost: ghosts are in no cell), so
+// the components, and every flag derived from them, are those of processing
+// all edges.
+constexpr int kCcLinks = 2;
+constexpr int kCcSamples = 1024;
+
+__global__ void __launch_bounds__(kThreads) k_cc_link(Consts c, StateBuf s, NbList nb, int* par,
                                                       DevStats* ds) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.n || s.type[k] == T_GHOST) return;
     const int np = nb.n_pad, m = nb.cnt[k];
+    int links = 0;
+    for (int q = 0; q < m && links < kCcLinks; q++) {
+        const size_t o = (size_t)q * np + k;
+        if (nb.dist[o] < c.re_p) {
+            uf_union(par, k, nb.slot[o], ds);
+            links++;
+        }
+    }
+}
+
+// No unions run here, so every find returns the final root.
+__global__ void k_cc_compress(int n, int* par, DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) par[k] = uf_find(par, k, ds);
+}
+
+// One block: the most frequent root among kCcSamples evenly spaced
+// particles (ties: the smaller root).
+__global__ void k_cc_giant(int n, const int* __restrict__ par, int* giant) {
+    __shared__ int roots[kCcSamples];
+    __shared__ unsigned long long best;
+    const int tid = threadIdx.x;
+    if (tid == 0) best = 0ull;
+    for (int i = tid; i < kCcSamples; i += blockDim.x)
+        roots[i] = par[(int)(((long long)i * n) / kCcSamples)];
+    __syncthreads();
+    for (int i = tid; i < kCcSamples; i += blockDim.x) {
+        int cnt = 0;
+        for (int j = 0; j < kCcSamples; j++) cnt += roots[j] == roots[i];
+        // larger count first, then smaller root
+        const unsigned long long key =
+            ((unsigned long long)cnt << 32) | (unsigned int)(0x7fffffff - roots[i]);
+        atomicMax(&best, key);
+    }
+    __syncthreads();
+    if (tid == 0) *giant = 0x7fffffff - (int)(unsigned int)(best & 0xffffffffull);
+}
+
+__global__ void __launch_bounds__(kThreads) k_cc_hook(Consts c, StateBuf s, NbList nb, int* par,
+                                                      const int* giant, DevStats* ds) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.n || s.type[k] == T_GHOST) return;
+    // after compression par[k] is k's root, unless a find moved it higher since
+    if (((volatile int*)par)[k] == *giant) return;
+    const int np = nb.n_pad, m = nb.cnt[k];
     for (int q = 0; q < m; q++) {
-        int j = nb.slot[(size_t)q * np + k];
-        if (j < k && nb.dist[(size_t)q * np + k] < c.re_p) uf_union(par, k, j, ds);
+        const size_t o = (size_t)q * np + k;
+        if (nb.dist[o] < c.re_p) uf_union(par, k, nb.slot[o], ds);
     }
 }
 
@@ -718,9 +776,16 @@ void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, cons
                       int32_t* parent, int8_t* has_surface, DevStats* ds, cudaStream_t st) {
     int g = blocks_for(c.n);
     cudaMemsetAsync(has_surface, 0, c.n, st);
+    int* giant = parent + c.n;  // the parent array has one spare element
     k_cc_init<<<g, kThreads, 0, st>>>(c.n, parent);
     ++g_launches;
-    k_cc_hook<<<g, kThreads, 0, st>>>(c, s, nb, parent, ds);
+    k_cc_link<<<g, kThreads, 0, st>>>(c, s, nb, parent, ds);
+    ++g_launches;
+    k_cc_compress<<<g, kThreads, 0, st>>>(c.n, parent, ds);
+    ++g_launches;
+    k_cc_giant<<<1, 1024, 0, st>>>(c.n, parent, giant);
+    ++g_launches;
+    k_cc_hook<<<g, kThreads, 0, st>>>(c, s, nb, parent, giant, ds);
     ++g_launches;
     k_cc_mark<<<g, kThreads, 0, st>>>(c, s, parent, has_surface, ds);
     ++g_launches;

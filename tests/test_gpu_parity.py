@@ -132,3 +132,56 @@ def test_fp64_step_at_config1_resolution_against_oracle():
     assert rel_l2(a["pressure"], b["pressure"]) < 1e-7
     assert np.max(np.abs(a["pos"] - b["pos"])) < 1e-12
     e.close()
+
+
+def _sealed_box(l0, nf, origin, wall_layers=2, dummy_layers=2):
+    """A fully packed nf x nf fluid block closed by walls and dummies on all
+    four sides: none of its particles is Surface, so its component has no
+    Dirichlet connection (src/mps.cpp:362-415 doubles its Inner diagonals)."""
+    from mps_gb300 import scenes
+
+    L = wall_layers + dummy_layers
+    ix, iy = np.meshgrid(np.arange(-L, nf + L), np.arange(-L, nf + L), indexing="ij")
+    ix, iy = ix.ravel(), iy.ravel()
+    ring = np.maximum(np.maximum(-ix, ix - (nf - 1)), np.maximum(-iy, iy - (nf - 1)))
+    t = np.where(ring <= 0, scenes.FLUID,
+                 np.where(ring <= wall_layers, scenes.WALL, scenes.DUMMY)).astype(np.int32)
+    pos = np.zeros((len(t), 3))
+    pos[:, 0] = origin[0] + (ix + 0.5) * l0
+    pos[:, 1] = origin[1] + (iy + 0.5) * l0
+    return pos, np.zeros_like(pos), t
+
+
+@pytest.mark.parametrize("box_n", [10, 60])
+def test_unconnected_component_against_oracle(box_n):
+    """A dam break beside a sealed, fully packed box (no Surface particle):
+    the box's particles are unconnected.  At box_n = 10 the dam break is the
+    largest component, at 60 the box is, so both sides of the sampled
+    component search are covered.  Dirichlet flags, boundary flags and the
+    unconnected count bit-exact, pressure within the CG tolerance."""
+    m = engine_or_skip()
+    from oracle import Oracle
+
+    from mps_gb300 import scenes
+
+    l0 = 0.01
+    prm, pos, vel, t = scenes.dam_break(l0, tank=(0.3, 0.25), column=(0.1, 0.2), dt=1e-3,
+                                        margin=0.05)
+    bp, bv, bt = _sealed_box(l0, box_n, (0.5, 0.05))
+    prm["domain_max"] = [0.5 + (box_n + 10) * l0, max(prm["domain_max"][1], 0.05 + (box_n + 10) * l0),
+                         0.0]
+    pos, vel, t = np.vstack([pos, bp]), np.vstack([vel, bv]), np.concatenate([t, bt])
+    e = m.Engine(prm, pos, vel, t, precision=m.FP64)
+    o = Oracle(prm, pos, vel, t)
+    o.set_cg(solves=1)
+    in_box = pos[:, 0] > 0.45
+    for s in range(3):
+        st = e.step()
+        so = o.step()
+        assert st["debug_log_count"] == so["debug_log_count"], s
+        a, b = e.state(), o.state()
+        for k in ("type", "bc", "dirichlet"):
+            assert np.array_equal(a[k], b[k]), (s, k)
+        assert not a["dirichlet"][in_box].any() and a["dirichlet"][~in_box & (t == scenes.FLUID)].all()
+        assert rel_l2(a["pressure"], b["pressure"]) < 1e-7, s
+    e.close()
