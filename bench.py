@@ -315,6 +315,65 @@ def run_fp64_2m(steps: int) -> dict:
     return out
 
 
+def run_export(steps: int = 30, every: int = 10) -> dict:
+    """The 1M step with the reference's export every `every` steps (CSV + VTU
+    of every particle), three ways: no export; synchronous (the export step,
+    then snapshot and write before the next step, as the reference does);
+    asynchronous (snapshot, then the writer thread formats and writes while
+    the next steps run).  Wall time on the stepping thread."""
+    import shutil
+
+    from mps_gb300 import MIXED, Engine
+
+    prm, pos, vel, t = workload("dambreak_1m")
+    nf = int((t == 0).sum())
+    e = Engine(prm, pos, vel, t, precision=MIXED)
+    for _ in range(2):
+        e.step()
+    shm = "/dev/shm" if os.path.isdir("/dev/shm") and os.access("/dev/shm", os.W_OK) else None
+    d = tempfile.mkdtemp(dir=shm)
+    try:
+        def loop(mode):
+            writer = None
+            t0 = time.perf_counter()
+            for s in range(steps):
+                ex = mode != "none" and s % every == every - 1
+                e.step(export=ex)
+                if not ex:
+                    continue
+                csv, vtu = os.path.join(d, f"o{s}.csv"), os.path.join(d, f"o{s}.vtu")
+                if writer is not None:
+                    writer.join()
+                e.export_begin()
+                if mode == "sync":
+                    e.export_write(csv, vtu, s * prm["dt"])
+                else:
+                    writer = threading.Thread(target=e.export_write, args=(csv, vtu, s * prm["dt"]))
+                    writer.start()
+            if writer is not None:
+                writer.join()
+            return time.perf_counter() - t0
+
+        base, sync, asyn = loop("none"), loop("sync"), loop("async")
+        t0 = time.perf_counter()
+        e.export_begin()
+        e.export_write(os.path.join(d, "w.csv"), os.path.join(d, "w.vtu"), 0.0)
+        write_s = time.perf_counter() - t0
+        size = os.path.getsize(os.path.join(d, "w.csv")) + os.path.getsize(os.path.join(d, "w.vtu"))
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    e.close()
+    n_ex = steps // every
+    return {"workload": f"dambreak_1m: {nf} fluid / {len(t)} particles, mixed solver, {steps} steps, "
+                        f"export every {every} (CSV + VTU, {n_ex} exports)",
+            "target": "tmpfs (/dev/shm)" if shm else "temporary directory",
+            "ms_per_step": {"no_export": 1e3 * base / steps, "sync_export": 1e3 * sync / steps,
+                            "async_export": 1e3 * asyn / steps},
+            "export_cost_ms": {"sync": 1e3 * (sync - base) / n_ex, "async": 1e3 * (asyn - base) / n_ex},
+            "one_export_write_ms": 1e3 * write_s, "bytes_per_export": int(size),
+            "d2h_bytes_per_export": int(len(t) * 72)}
+
+
 def run_small_case() -> dict:
     """The reference's own CPU-sized case (1,250 fluid particles, dt 1e-3 s,
     1,000 steps), FP64 on the GPU (graph replays) and on the CPU oracle."""
@@ -449,6 +508,7 @@ def run_ours(args, rank: int, world: int, dist):
         others["adjoint"] = run_adjoint()
         others["fp64_2m"] = run_fp64_2m(steps=3)
         others["small_case"] = run_small_case()
+        others["export"] = run_export()
 
     if rank != 0:
         return None

@@ -129,6 +129,31 @@ int mps_step(mps_engine* e, int32_t is_time_to_export, mps_step_stats* stats);
 /* n_steps consecutive non-export steps; stats of the last step. */
 int mps_run(mps_engine* e, int32_t n_steps, mps_step_stats* stats);
 
+/* Asynchronous export (the reference's Simulation::exportParticles,
+ * src/simulation.cpp:231-245, and Exporter, src/exporter.cpp:10-167).
+ * mps_export_begin snapshots the current state in id order: gathers on the
+ * engine's stream, then a copy into engine-owned pinned host memory on a
+ * second stream, so that mps_step may go on at once.  mps_export_view waits
+ * for the copy and returns pointers into the snapshot (valid until the next
+ * mps_export_begin); mps_export_write waits and writes the reference's CSV
+ * (Ghost particles skipped, six decimals) and ASCII VTU files (either path
+ * may be NULL).  view/write may run on another thread while mps_step runs
+ * on the same handle; mps_export_begin must not overlap a view or write. */
+typedef struct {
+    int32_t n;
+    const double* pos;       /* 3n, x y z per particle */
+    const double* vel;       /* 3n */
+    const double* pressure;  /* n */
+    const double* ndr;       /* n, number density ratio */
+    const int32_t* type;     /* n, ParticleType (-1 Ghost) */
+    const int32_t* bc;       /* n, BoundaryCondition */
+} mps_snapshot;
+int mps_export_begin(mps_engine* e);
+int mps_export_view(mps_engine* e, mps_snapshot* out);
+int mps_export_write(mps_engine* e, const char* csv_path, const char* vtu_path, double time);
+/* The same writers on caller arrays (no engine, no device). */
+int mps_write_snapshot(const mps_snapshot* s, const char* csv_path, const char* vtu_path, double time);
+
 /* Particle state in id order (host pointers; any may be NULL). */
 int mps_download(mps_engine* e, double* pos, double* vel, double* pressure,
                  double* min_pressure, double* ndr, int32_t* type, int32_t* bc,

@@ -27,7 +27,8 @@ HOST_EXE = os.path.join(LIB, "mps")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--extended-lambda", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(REPO, "include")]
-ENGINE_SRCS = ["sort.cu", "sweeps.cu", "solver.cu", "mg.cu", "capi.cu", "adjoint.cu", "batch.cu", "noalloc.cu"]
+ENGINE_SRCS = ["sort.cu", "sweeps.cu", "solver.cu", "mg.cu", "capi.cu", "adjoint.cu", "batch.cu", "noalloc.cu",
+               "export.cu"]
 
 
 def nvcc() -> str:
@@ -71,7 +72,7 @@ def build_engine(verbose: bool = False) -> str:
             if verbose:
                 sys.stderr.write(r.stderr)
     if _newer(ENGINE_SO, objs):
-        _run([nvcc()] + ARCH + ["-shared", "-o", ENGINE_SO] + objs)
+        _run([nvcc()] + ARCH + ["-shared", "-o", ENGINE_SO] + objs + ["-lpthread"])
     return ENGINE_SO
 
 
@@ -86,7 +87,7 @@ def build_host() -> str:
     deps = srcs + hdrs + [ENGINE_SO, os.path.join(REPO, "include", "mps_gb300.h")]
     if _newer(HOST_EXE, deps):
         cxx = os.environ.get("CXX", "g++")
-        _run([cxx, "-std=c++20", "-O2", "-ffp-contract=off", "-I", os.path.join(REPO, "include"),
+        _run([cxx, "-std=c++20", "-O2", "-pthread", "-ffp-contract=off", "-I", os.path.join(REPO, "include"),
               "-o", HOST_EXE] + srcs + ["-L", LIB, "-lmps_gb300", f"-Wl,-rpath,{LIB}",
                                          "-Wl,-rpath,$ORIGIN"])
     return HOST_EXE

@@ -626,6 +626,12 @@ int mps_destroy(mps_engine* e) {
     if (e->hs) cudaFreeHost(e->hs);
     for (auto& ev : e->ev)
         if (ev) cudaEventDestroy(ev);
+    if (e->xst) cudaStreamSynchronize(e->xst);
+    if (e->xhost) cudaFreeHost(e->xhost);
+    if (e->xhost_i) cudaFreeHost(e->xhost_i);
+    if (e->xev_ready) cudaEventDestroy(e->xev_ready);
+    if (e->xev_done) cudaEventDestroy(e->xev_done);
+    if (e->xst) cudaStreamDestroy(e->xst);
     if (e->st) cudaStreamDestroy(e->st);
     delete e;
     return MPS_OK;

@@ -81,6 +81,15 @@ struct mps_engine {
     // Set while a trajectory records a step for its adjoint (eager launches).
     const mpsg::TapeStep* tape = nullptr;
     cudaEvent_t ev[4]{};
+    // asynchronous export (export.cu): device gather buffer, pinned host
+    // snapshot, side stream; allocated on first use
+    double* xdev = nullptr;   // 8 x n_pad: pos 3, vel 3, pressure, ndr
+    int32_t* xdev_i = nullptr;  // 2 x n_pad: type, bc
+    double* xhost = nullptr;
+    int32_t* xhost_i = nullptr;
+    cudaStream_t xst = nullptr;
+    cudaEvent_t xev_ready = nullptr, xev_done = nullptr;
+    int32_t x_pending = 0;
     std::vector<void*> allocs;
 
     template <typename T>

@@ -1,0 +1,283 @@
+// Asynchronous export: the reference's Simulation::exportParticles
+// (src/simulation.cpp:231-245) and Exporter (src/exporter.cpp:10-167).
+//
+// The reference copies every particle to its host vector each export step and
+// formats the CSV and VTU files on the stepping thread.  Here an export is a
+// snapshot: one gather kernel on the engine's stream puts the state into id
+// order in a device buffer, a copy on a second stream moves it to pinned
+// host memory, and the steps that follow run meanwhile.  The writers format
+// the snapshot with std::to_chars on several threads (the same text as the
+// reference's printf("%.6f") CSV fields and default-precision ostream VTU
+// fields) and write each file with a few large writes.
+#include <algorithm>
+#include <charconv>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "engine_impl.cuh"
+
+using namespace mpsg;
+
+namespace {
+
+// slot k -> id order: pos/vel xyz-interleaved (planar engines: z = z0, v_z = 0)
+__global__ void k_export_gather(int n, const int32_t* __restrict__ id, const double* __restrict__ x,
+                                const double* __restrict__ y, const double* __restrict__ z, double z0,
+                                const double* __restrict__ vx, const double* __restrict__ vy,
+                                const double* __restrict__ vz, const double* __restrict__ p,
+                                const double* __restrict__ ndr, const int8_t* __restrict__ type,
+                                const int8_t* __restrict__ bc, size_t np, double* __restrict__ out,
+                                int32_t* __restrict__ out_i) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const size_t o = (size_t)id[k];
+    out[3 * o] = x[k];
+    out[3 * o + 1] = y[k];
+    out[3 * o + 2] = z ? z[k] : z0;
+    out[3 * np + 3 * o] = vx[k];
+    out[3 * np + 3 * o + 1] = vy[k];
+    out[3 * np + 3 * o + 2] = vz ? vz[k] : 0.0;
+    out[6 * np + o] = p[k];
+    out[7 * np + o] = ndr[k];
+    out_i[o] = type[k];
+    out_i[np + o] = bc[k];
+}
+
+int err(int code, const std::string& m) {
+    set_last_error(m);
+    return code;
+}
+
+#define XCU(call)                                                                            \
+    do {                                                                                     \
+        cudaError_t err_ = (call);                                                           \
+        if (err_ != cudaSuccess)                                                             \
+            return err(MPS_ERR_CUDA, std::string(#call " failed: ") + cudaGetErrorString(err_)); \
+    } while (0)
+
+// ---------------------------------------------------------------- writers
+// printf("%.6f") and ostream's default (printf "%g", 6 significant digits)
+// are both defined as correctly rounded; std::to_chars with the same format
+// and precision produces the same characters.
+inline void put_fixed6(std::string& s, double v) {
+    char b[400];
+    const auto r = std::to_chars(b, b + sizeof b, v, std::chars_format::fixed, 6);
+    s.append(b, r.ptr);
+}
+inline void put_general6(std::string& s, double v) {
+    char b[64];
+    const auto r = std::to_chars(b, b + sizeof b, v, std::chars_format::general, 6);
+    s.append(b, r.ptr);
+}
+inline void put_int(std::string& s, long long v) {
+    char b[24];
+    const auto r = std::to_chars(b, b + sizeof b, v);
+    s.append(b, r.ptr);
+}
+
+// Formats [0, n) in chunks on up to 16 threads and writes them in order.
+template <typename F>
+bool write_rows(std::FILE* f, int n, F&& row) {
+    const int hw = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const int T = n >= 65536 ? hw : 1;
+    std::vector<std::string> part(T);
+    auto work = [&](int t) {
+        const int b = (int)((long long)n * t / T), e = (int)((long long)n * (t + 1) / T);
+        std::string& s = part[t];
+        s.reserve((size_t)(e - b) * 96);
+        for (int i = b; i < e; i++) row(s, i);
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; t++) th.emplace_back(work, t);
+    work(0);
+    for (auto& x : th) x.join();
+    for (auto& s : part)
+        if (!s.empty() && std::fwrite(s.data(), 1, s.size(), f) != s.size()) return false;
+    return true;
+}
+
+bool put(std::FILE* f, const std::string& s) { return std::fwrite(s.data(), 1, s.size(), f) == s.size(); }
+
+// Exporter::toCsv (src/exporter.cpp:10-55): Ghost particles skipped, the
+// count line holds every particle.
+int write_csv(const mps_snapshot& s, const char* path, double time) {
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return err(MPS_ERR_ARG, std::string("Could not open target csv file: ") + path);
+    std::string h = "Time (s),";
+    put_fixed6(h, time);
+    h += "\nNumber of Particles,";
+    put_int(h, s.n);
+    h += "\nID,Type,Position.x (m),Position.y (m),Position.z (m),Velocity.x (m/s),Velocity.y (m/s),"
+         "Velocity.z (m/s),Pressure (Pa),Number Density Ratio\n";
+    bool ok = put(f, h) && write_rows(f, s.n, [&](std::string& o, int i) {
+        if (s.type[i] == -1) return;
+        put_int(o, i);
+        o += ',';
+        put_int(o, s.type[i]);
+        for (int c = 0; c < 3; c++) {
+            o += ',';
+            put_fixed6(o, s.pos[3 * (size_t)i + c]);
+        }
+        for (int c = 0; c < 3; c++) {
+            o += ',';
+            put_fixed6(o, s.vel[3 * (size_t)i + c]);
+        }
+        o += ',';
+        put_fixed6(o, s.pressure[i]);
+        o += ',';
+        put_fixed6(o, s.ndr[i]);
+        o += '\n';
+    });
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? MPS_OK : err(MPS_ERR_ARG, std::string("write failed: ") + path);
+}
+
+// Exporter::toVtu (src/exporter.cpp:57-167): every particle, one vertex cell
+// each; the velocity's z is written as 0.
+int write_vtu(const mps_snapshot& s, const char* path, double time) {
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return err(MPS_ERR_ARG, std::string("Could not open target vtu file: ") + path);
+    const int n = s.n;
+    auto begin_array = [](const char* comps, const char* type, const char* name) {
+        return std::string("<DataArray NumberOfComponents='") + comps + "' type='" + type + "' Name='" +
+               name + "' format='ascii'>\n";
+    };
+    const std::string end_array = "</DataArray>\n";
+    std::string h = "<?xml version='1.0' encoding='UTF-8'?>\n"
+                    "<VTKFile byte_order='LittleEndian' version='0.1' type = 'UnstructuredGrid'>\n"
+                    "<UnstructuredGrid>\n<FieldData>\n"
+                    "<DataArray type='Float64' Name='Time' NumberOfComponents='1' NumberOfTuples='1' "
+                    "format='ascii'>\n";
+    put_general6(h, time);
+    h += "\n</DataArray>\n</FieldData>\n<Piece NumberOfCells='";
+    put_int(h, n);
+    h += "' NumberOfPoints='";
+    put_int(h, n);
+    h += "'>\n<Points>\n<DataArray NumberOfComponents='3' type='Float64' Name='position' format='ascii'>\n";
+    bool ok = put(f, h);
+    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+        for (int c = 0; c < 3; c++) {
+            put_general6(o, s.pos[3 * (size_t)i + c]);
+            o += c < 2 ? ' ' : '\n';
+        }
+    });
+    ok = ok && put(f, end_array + "</Points>\n<PointData>\n" + begin_array("1", "Int32", "Type"));
+    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+        put_int(o, s.type[i]);
+        o += '\n';
+    });
+    ok = ok && put(f, end_array + begin_array("3", "Float64", "Velocity"));
+    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+        put_general6(o, s.vel[3 * (size_t)i]);
+        o += ' ';
+        put_general6(o, s.vel[3 * (size_t)i + 1]);
+        o += " 0\n";
+    });
+    ok = ok && put(f, end_array + begin_array("1", "Float64", "Pressure"));
+    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+        put_general6(o, s.pressure[i]);
+        o += '\n';
+    });
+    ok = ok && put(f, end_array + begin_array("1", "Float64", "Number Density Ratio"));
+    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+        put_general6(o, s.ndr[i]);
+        o += '\n';
+    });
+    ok = ok && put(f, end_array + begin_array("1", "Int32", "Boundary Condition"));
+    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+        put_int(o, s.bc[i]);
+        o += '\n';
+    });
+    ok = ok && put(f, end_array + "</PointData>\n<Cells>\n<DataArray type='Int32' Name='connectivity' "
+                                  "format='ascii'>\n");
+    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+        put_int(o, i);
+        o += '\n';
+    });
+    ok = ok && put(f, end_array + "<DataArray type='Int32' Name='offsets' format='ascii'>\n");
+    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+        put_int(o, (long long)i + 1);
+        o += '\n';
+    });
+    ok = ok && put(f, end_array + "<DataArray type='UInt8' Name='types' format='ascii'>\n");
+    ok = ok && write_rows(f, n, [&](std::string& o, int) { o += "1\n"; });
+    ok = ok && put(f, end_array + "</Cells>\n</Piece>\n</UnstructuredGrid>\n</VTKFile>\n");
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? MPS_OK : err(MPS_ERR_ARG, std::string("write failed: ") + path);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mps_write_snapshot(const mps_snapshot* s, const char* csv_path, const char* vtu_path, double time) {
+    if (!s || s->n < 0 || (s->n > 0 && (!s->pos || !s->vel || !s->pressure || !s->ndr || !s->type || !s->bc)))
+        return err(MPS_ERR_ARG, "mps_write_snapshot: incomplete snapshot");
+    if (csv_path) {
+        const int rc = write_csv(*s, csv_path, time);
+        if (rc) return rc;
+    }
+    if (vtu_path) {
+        const int rc = write_vtu(*s, vtu_path, time);
+        if (rc) return rc;
+    }
+    return MPS_OK;
+}
+
+int mps_export_begin(mps_engine* e) {
+    if (!e) return err(MPS_ERR_ARG, "null engine");
+    const size_t np = e->n_pad;
+    if (!e->xdev) {
+        XCU(cudaStreamCreateWithFlags(&e->xst, cudaStreamNonBlocking));
+        XCU(cudaEventCreateWithFlags(&e->xev_ready, cudaEventDisableTiming));
+        XCU(cudaEventCreateWithFlags(&e->xev_done, cudaEventDisableTiming));
+        XCU(cudaMallocHost(&e->xhost, sizeof(double) * 8 * np));
+        XCU(cudaMallocHost(&e->xhost_i, sizeof(int32_t) * 2 * np));
+        if (e->alloc(&e->xdev, 8 * np) || e->alloc(&e->xdev_i, 2 * np))
+            return err(MPS_ERR_CUDA, "cudaMalloc export buffers");
+    }
+    // the device buffer is rewritten only after the last snapshot left it
+    if (e->x_pending) XCU(cudaStreamWaitEvent(e->st, e->xev_done, 0));
+    const StateBuf& s = e->S();
+    const int n = e->n;
+    const bool pl = e->c.planar;
+    k_export_gather<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id, s.x, s.y, pl ? nullptr : s.z, e->c.z0,
+                                                        s.vx, s.vy, pl ? nullptr : s.vz, s.p, s.ndr, s.type,
+                                                        s.bc, np, e->xdev, e->xdev_i);
+    ++g_launches;
+    XCU(cudaGetLastError());
+    XCU(cudaEventRecord(e->xev_ready, e->st));
+    XCU(cudaStreamWaitEvent(e->xst, e->xev_ready, 0));
+    XCU(cudaMemcpyAsync(e->xhost, e->xdev, sizeof(double) * 8 * np, cudaMemcpyDeviceToHost, e->xst));
+    XCU(cudaMemcpyAsync(e->xhost_i, e->xdev_i, sizeof(int32_t) * 2 * np, cudaMemcpyDeviceToHost, e->xst));
+    XCU(cudaEventRecord(e->xev_done, e->xst));
+    e->x_pending = 1;
+    return MPS_OK;
+}
+
+int mps_export_view(mps_engine* e, mps_snapshot* out) {
+    if (!e || !out) return err(MPS_ERR_ARG, "mps_export_view: null argument");
+    if (!e->x_pending) return err(MPS_ERR_ARG, "mps_export_view: no snapshot (call mps_export_begin)");
+    XCU(cudaEventSynchronize(e->xev_done));
+    const size_t np = e->n_pad;
+    out->n = e->n;
+    out->pos = e->xhost;
+    out->vel = e->xhost + 3 * np;
+    out->pressure = e->xhost + 6 * np;
+    out->ndr = e->xhost + 7 * np;
+    out->type = e->xhost_i;
+    out->bc = e->xhost_i + np;
+    return MPS_OK;
+}
+
+int mps_export_write(mps_engine* e, const char* csv_path, const char* vtu_path, double time) {
+    mps_snapshot s;
+    const int rc = mps_export_view(e, &s);
+    if (rc) return rc;
+    return mps_write_snapshot(&s, csv_path, vtu_path, time);
+}
+
+}  // extern "C"

@@ -68,6 +68,19 @@ class MpsStepStats(C.Structure):
     ]
 
 
+class MpsSnapshot(C.Structure):
+    """mps_snapshot (include/mps_gb300.h): an export snapshot in id order."""
+    _fields_ = [
+        ("n", C.c_int32),
+        ("pos", C.POINTER(C.c_double)),
+        ("vel", C.POINTER(C.c_double)),
+        ("pressure", C.POINTER(C.c_double)),
+        ("ndr", C.POINTER(C.c_double)),
+        ("type", C.POINTER(C.c_int32)),
+        ("bc", C.POINTER(C.c_int32)),
+    ]
+
+
 class MpsError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"mps error {code}: {msg}")
@@ -140,6 +153,12 @@ def load(build_if_missing: bool = False):
                  "mps_batch_set_launch", "mps_batch_launch_info", "mps_batch_group_blocks",
                  "mps_batch_step"):
         getattr(L, name).restype = C.c_int
+    L.mps_export_begin.argtypes = [vp]
+    L.mps_export_view.argtypes = [vp, P(MpsSnapshot)]
+    L.mps_export_write.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_double]
+    L.mps_write_snapshot.argtypes = [P(MpsSnapshot), C.c_char_p, C.c_char_p, C.c_double]
+    for name in ("mps_export_begin", "mps_export_view", "mps_export_write", "mps_write_snapshot"):
+        getattr(L, name).restype = C.c_int
     L.mps_last_error.restype = C.c_char_p
     for name in ("mps_create", "mps_destroy", "mps_set_solver", "mps_step", "mps_run",
                  "mps_download", "mps_upload", "mps_neighbors", "mps_system", "mps_collisions"):
@@ -151,6 +170,20 @@ def load(build_if_missing: bool = False):
 def _check(rc):
     if rc != MPS_OK:
         raise MpsError(rc, _lib.mps_last_error().decode())
+
+
+def write_snapshot(snap: dict, csv_path=None, vtu_path=None, time=0.0):
+    """The engine's CSV / VTU writers on host arrays (pos, vel: n x 3; pressure,
+    ndr: n; type, bc: n int32), without an engine or a device."""
+    L = load()
+    n = len(snap["type"])
+    keep = [np.ascontiguousarray(snap[k], dtype=np.float64) for k in ("pos", "vel", "pressure", "ndr")]
+    keep += [np.ascontiguousarray(snap[k], dtype=np.int32) for k in ("type", "bc")]
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+    s = MpsSnapshot(n, dp(keep[0]), dp(keep[1]), dp(keep[2]), dp(keep[3]), ip(keep[4]), ip(keep[5]))
+    enc = lambda q: None if q is None else os.fsencode(q)
+    _check(L.mps_write_snapshot(C.byref(s), enc(csv_path), enc(vtu_path), float(time)))
 
 
 def make_params(p: dict) -> MpsParams:
@@ -257,6 +290,26 @@ class Engine:
     def download_into(self, pos=None, vel=None, pressure=None, ndr=None, types=None, bc=None):
         _check(_lib.mps_download(self._h, _p(pos), _p(vel), _p(pressure), None, _p(ndr),
                                  _p(types), _p(bc), None))
+
+    def export_begin(self):
+        """Snapshot the state for export; the following steps may run at once."""
+        _check(_lib.mps_export_begin(self._h))
+
+    def export_snapshot(self) -> dict:
+        """Waits for the snapshot of the last export_begin; copies of its arrays."""
+        s = MpsSnapshot()
+        _check(_lib.mps_export_view(self._h, C.byref(s)))
+        n = s.n
+        arr = lambda p, k: np.ctypeslib.as_array(p, shape=(k,)).copy()
+        return dict(pos=arr(s.pos, 3 * n).reshape(n, 3), vel=arr(s.vel, 3 * n).reshape(n, 3),
+                    pressure=arr(s.pressure, n), ndr=arr(s.ndr, n), type=arr(s.type, n),
+                    bc=arr(s.bc, n))
+
+    def export_write(self, csv_path=None, vtu_path=None, time=0.0):
+        """Waits for the snapshot and writes the reference's CSV / VTU files
+        (releases the GIL: may run on a writer thread while steps go on)."""
+        enc = lambda p: None if p is None else os.fsencode(p)
+        _check(_lib.mps_export_write(self._h, enc(csv_path), enc(vtu_path), float(time)))
 
     def upload(self, pos=None, vel=None, types=None):
         _check(_lib.mps_upload(self._h, _p(pos), _p(vel), _p(types)))

@@ -172,6 +172,17 @@ double MPS::stepForward(const bool isTimeToExport) {
         mpslog::debug("Courant number is larger than CFL condition. Courant=" + std::to_string(stats.courant));
     if (stats.courant > 1.0) mpslog::error("Courant number is larger than 1.0. Exiting Simulation.");
     debugLogCount = stats.debug_log_count;
-    if (isTimeToExport) syncParticles();
+    if (isTimeToExport && syncOnExport) syncParticles();
     return stats.courant;
+}
+
+void MPS::beginExport() {
+    if (!engine) throw std::runtime_error("MPS::beginExport before loadInitialState");
+    check(mps_export_begin(engine.get()));
+}
+
+// Safe on another thread while stepForward runs (see include/mps_gb300.h).
+void MPS::writeExport(const std::filesystem::path& csv, const std::filesystem::path& vtu, double time) {
+    const int rc = mps_export_write(engine.get(), csv.string().c_str(), vtu.string().c_str(), time);
+    if (rc != MPS_OK) throw std::runtime_error(std::string("export failed: ") + mps_last_error());
 }

@@ -40,6 +40,13 @@ public:
     void setSolver(int precision, double tol = 0.0, long long maxIter = 0);
     void syncParticles();
     const mps_step_stats& lastStepStats() const { return stats; }
+    // Export steps refresh `particles` (the reference's behaviour) unless a
+    // driver that exports from engine snapshots turns this off.
+    bool syncOnExport = true;
+    // Snapshot of the current state for export (mps_export_begin); the
+    // following steps may run while writeExport() waits for it and writes.
+    void beginExport();
+    void writeExport(const std::filesystem::path& csv, const std::filesystem::path& vtu, double time);
 
 private:
     struct EngineDeleter {

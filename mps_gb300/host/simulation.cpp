@@ -21,7 +21,8 @@ void Simulation::run(const fs::path& inputYamlPath, int precision) {
     mps = MPS(inputYamlPath);
     mps.setSolver(precision);
     time = mps.loadInitialState();
-    exportParticles(mps.particles);
+    mps.syncOnExport = false;  // exports are written from engine snapshots
+    exportSnapshot();
 
     mpslog::info("START SIMULATION");
     simulationStartTime = system_clock::now();
@@ -30,10 +31,11 @@ void Simulation::run(const fs::path& inputYamlPath, int precision) {
         int before = mps.debugLogCount;
         time += mps.settings.dt;
         double courant = mps.stepForward(isTimeToExport());
-        if (isTimeToExport()) exportParticles(mps.particles);
+        if (isTimeToExport()) exportSnapshot();
         timeStepReport(t0, system_clock::now(), courant, mps.debugLogCount > before);
         timeStep++;
     }
+    finishExport();
     simulationEndTime = system_clock::now();
     endSimulation();
 }
@@ -108,7 +110,35 @@ bool Simulation::isTimeToExport() {
     return rem < mps.settings.dt / 10.0;
 }
 
-// src/simulation.cpp:231-245
+// src/simulation.cpp:231-245, asynchronously: the state is snapshotted on
+// the device and copied to pinned memory while the next steps run, and a
+// writer thread formats and writes the same two files.
+void Simulation::exportSnapshot() {
+    finishExport();
+    mps.beginExport();
+    const auto csv = resultDirectory / std::format("csv/output_{:04}.csv", outFileNum);
+    const auto vtu = resultDirectory / std::format("vtu/output_{:04}.vtu", outFileNum);
+    const double t = time;
+    exportWriter = std::thread([this, csv, vtu, t] {
+        try {
+            mps.writeExport(csv, vtu, t);
+        } catch (...) {
+            exportError = std::current_exception();
+        }
+    });
+    outFileNum++;
+}
+
+void Simulation::finishExport() {
+    if (exportWriter.joinable()) exportWriter.join();
+    if (exportError) {
+        auto e = exportError;
+        exportError = nullptr;
+        std::rethrow_exception(e);
+    }
+}
+
+// The reference's synchronous form, from the host particle vector.
 void Simulation::exportParticles(const std::vector<Particle>& particles) {
     Exporter exporter;
     exporter.toCsv(resultDirectory / std::format("csv/output_{:04}.csv", outFileNum), particles, time);

@@ -2,7 +2,9 @@
 #pragma once
 #include <chrono>
 #include <filesystem>
+#include <exception>
 #include <fstream>
+#include <thread>
 #include <vector>
 
 #include "mps.hpp"
@@ -20,6 +22,10 @@ private:
     std::chrono::system_clock::time_point simulationStartTime, simulationEndTime;
 
     int outFileNum = 0;
+    // Files of an export are written on this thread from an engine snapshot
+    // while the next steps run; one export in flight at a time.
+    std::thread exportWriter;
+    std::exception_ptr exportError;
     std::ofstream timeStepReportFile;
     std::filesystem::path resultDirectory;
 
@@ -30,5 +36,7 @@ private:
                         const double& courantNumber, const bool& isDebugLogAdded);
     bool isTimeToExport();
     void exportParticles(const std::vector<Particle>& particles);
+    void exportSnapshot();
+    void finishExport();
     void endSimulation();
 };

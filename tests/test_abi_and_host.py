@@ -146,3 +146,68 @@ def test_wall_taps_sit_under_the_fluid():
     assert np.all(t[taps] == scenes.WALL)
     assert np.allclose(pos[taps, 1], pos[t == scenes.FLUID, 1].min() - l0)
     assert np.all(np.diff(pos[taps, 0]) > 0)
+
+
+def _reference_csv(s, time):
+    """src/exporter.cpp:10-55 in Python: printf("%.6f") fields, Ghosts skipped."""
+    out = [f"Time (s),{time:.6f}\n", f"Number of Particles,{len(s['type'])}\n",
+           "ID,Type,Position.x (m),Position.y (m),Position.z (m),Velocity.x (m/s),Velocity.y (m/s),"
+           "Velocity.z (m/s),Pressure (Pa),Number Density Ratio\n"]
+    for i, t in enumerate(s["type"]):
+        if t == -1:
+            continue
+        vals = list(s["pos"][i]) + list(s["vel"][i]) + [s["pressure"][i], s["ndr"][i]]
+        out.append(f"{i},{t}," + ",".join("%.6f" % v for v in vals) + "\n")
+    return "".join(out)
+
+
+def _reference_vtu(s, time):
+    """src/exporter.cpp:57-167 in Python: ostream default (printf "%g") fields."""
+    g = lambda v: "%g" % v
+    n = len(s["type"])
+    arr = lambda c, ty, name: f"<DataArray NumberOfComponents='{c}' type='{ty}' Name='{name}' format='ascii'>\n"
+    out = ["<?xml version='1.0' encoding='UTF-8'?>\n",
+           "<VTKFile byte_order='LittleEndian' version='0.1' type = 'UnstructuredGrid'>\n",
+           "<UnstructuredGrid>\n", "<FieldData>\n",
+           "<DataArray type='Float64' Name='Time' NumberOfComponents='1' NumberOfTuples='1' format='ascii'>\n",
+           g(time) + "\n", "</DataArray>\n", "</FieldData>\n",
+           f"<Piece NumberOfCells='{n}' NumberOfPoints='{n}'>\n", "<Points>\n",
+           "<DataArray NumberOfComponents='3' type='Float64' Name='position' format='ascii'>\n"]
+    out += [" ".join(g(v) for v in p) + "\n" for p in s["pos"]]
+    out += ["</DataArray>\n", "</Points>\n", "<PointData>\n", arr(1, "Int32", "Type")]
+    out += [f"{t}\n" for t in s["type"]] + ["</DataArray>\n", arr(3, "Float64", "Velocity")]
+    out += [f"{g(v[0])} {g(v[1])} 0\n" for v in s["vel"]] + ["</DataArray>\n", arr(1, "Float64", "Pressure")]
+    out += [g(v) + "\n" for v in s["pressure"]] + ["</DataArray>\n", arr(1, "Float64", "Number Density Ratio")]
+    out += [g(v) + "\n" for v in s["ndr"]] + ["</DataArray>\n", arr(1, "Int32", "Boundary Condition")]
+    out += [f"{b}\n" for b in s["bc"]] + ["</DataArray>\n", "</PointData>\n", "<Cells>\n",
+                                          "<DataArray type='Int32' Name='connectivity' format='ascii'>\n"]
+    out += [f"{i}\n" for i in range(n)] + ["</DataArray>\n", "<DataArray type='Int32' Name='offsets' format='ascii'>\n"]
+    out += [f"{i + 1}\n" for i in range(n)] + ["</DataArray>\n", "<DataArray type='UInt8' Name='types' format='ascii'>\n"]
+    out += ["1\n"] * n + ["</DataArray>\n", "</Cells>\n", "</Piece>\n", "</UnstructuredGrid>\n", "</VTKFile>\n"]
+    return "".join(out)
+
+
+@pytest.mark.parametrize("n", [7, 70000])
+def test_export_writers_match_reference_formats(built, tmp_path, n):
+    """The engine's multithreaded CSV / VTU writers (to_chars) against the
+    reference's printf / ostream formats, byte for byte, including negative
+    zero, values that round to -0.000000, large and tiny magnitudes; 70,000
+    particles take the multithreaded path."""
+    from mps_gb300 import write_snapshot
+
+    rng = np.random.default_rng(3)
+    pos = rng.normal(0.0, 0.7, (n, 3))
+    vel = rng.normal(0.0, 1e-3, (n, 3))
+    pressure = rng.random(n) * 2e4
+    ndr = rng.random(n) * 1.2
+    edge = np.array([0.0, -0.0, -1e-9, 5e-7, -4.9999999e-7, 123456.789012345, 1e-5, 2.5, -0.125, 1e15])
+    m = min(n, len(edge))
+    pos[:m, 0] = edge[:m]
+    vel[:m, 1] = edge[::-1][:m]
+    pressure[:m] = edge[:m]
+    types = rng.integers(-1, 3, n).astype(np.int32)
+    bc = rng.integers(0, 3, n).astype(np.int32)
+    s = dict(pos=pos, vel=vel, pressure=pressure, ndr=ndr, type=types, bc=bc)
+    write_snapshot(s, tmp_path / "o.csv", tmp_path / "o.vtu", 0.0125)
+    assert (tmp_path / "o.csv").read_text() == _reference_csv(s, 0.0125)
+    assert (tmp_path / "o.vtu").read_text() == _reference_vtu(s, 0.0125)
