@@ -29,7 +29,7 @@ enum {
     MPS_OK = 0,
     MPS_ERR_ARG = 1,         /* invalid argument (null pointer, bad size, bad setting) */
     MPS_ERR_CUDA = 2,        /* a CUDA call failed; the engine should be destroyed */
-    MPS_ERR_CAPACITY = 3,    /* a particle had more neighbours than the engine's list capacity */
+    MPS_ERR_CAPACITY = 3,    /* a capacity was exceeded: neighbour list, or mps_read_csv arrays */
     MPS_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up (kernel returned early) */
     MPS_ERR_NO_DEVICE = 5,   /* no CUDA device, or not an sm_103 part */
     MPS_ERR_NONFINITE = 6    /* a particle position became NaN/inf; it was made a ghost */
@@ -153,6 +153,15 @@ int mps_export_view(mps_engine* e, mps_snapshot* out);
 int mps_export_write(mps_engine* e, const char* csv_path, const char* vtu_path, double time);
 /* The same writers on caller arrays (no engine, no device). */
 int mps_write_snapshot(const mps_snapshot* s, const char* csv_path, const char* vtu_path, double time);
+
+/* The reference's particle CSV import (MPS::importInitialCondition,
+ * src/mps.cpp:38-94): "Time (s),t", a count line, a header line, then one
+ * row per particle whose ID equals its row index (empty lines skipped);
+ * columns found by name.  Host only.  Fills up to `capacity` particles
+ * (pos/vel xyz-interleaved; any array may be NULL) and sets *n to the row
+ * count; returns MPS_ERR_CAPACITY with *n set when capacity is too small. */
+int mps_read_csv(const char* path, int32_t capacity, int32_t* n, double* time, double* pos,
+                 double* vel, int32_t* type);
 
 /* Particle state in id order (host pointers; any may be NULL). */
 int mps_download(mps_engine* e, double* pos, double* vel, double* pressure,

@@ -6,4 +6,4 @@ the scene generator and CSV format (scenes.py) and the settings reader
 (settings.py).  The C++ front end that mirrors the reference's
 Simulation/MPS/Particle/Bucket classes lives in host/.
 """
-from .engine import FP64, MIXED, Batch, Engine, MpsError, Trajectory, load, write_snapshot  # noqa: F401
+from .engine import FP64, MIXED, Batch, Engine, MpsError, Trajectory, load, read_particles_csv, write_snapshot  # noqa: F401

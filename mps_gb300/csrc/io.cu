@@ -1,5 +1,7 @@
-// Asynchronous export: the reference's Simulation::exportParticles
-// (src/simulation.cpp:231-245) and Exporter (src/exporter.cpp:10-167).
+// Particle file IO.  Asynchronous export: the reference's
+// Simulation::exportParticles (src/simulation.cpp:231-245) and Exporter
+// (src/exporter.cpp:10-167).  CSV import: MPS::importInitialCondition
+// (src/mps.cpp:38-94).
 //
 // The reference copies every particle to its host vector each export step and
 // formats the CSV and VTU files on the stepping thread.  Here an export is a
@@ -209,6 +211,69 @@ int write_vtu(const mps_snapshot& s, const char* path, double time) {
     return ok ? MPS_OK : err(MPS_ERR_ARG, std::string("write failed: ") + path);
 }
 
+// ------------------------------------------------------------- CSV import
+// The file is read once; line starts are indexed in one pass; rows are parsed
+// on up to 16 threads with std::from_chars (correctly rounded, so the values
+// equal strtod's).
+struct CsvFile {
+    std::string text;
+    std::vector<std::pair<size_t, size_t>> lines;  // [begin, end) without '\r'
+};
+
+bool read_all(const char* path, std::string& out) {
+    std::FILE* f = std::fopen(path, "rb");
+    if (!f) return false;
+    std::fseek(f, 0, SEEK_END);
+    const long len = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    if (len < 0) {
+        std::fclose(f);
+        return false;
+    }
+    out.resize((size_t)len);
+    const bool ok = std::fread(out.data(), 1, out.size(), f) == out.size();
+    std::fclose(f);
+    return ok;
+}
+
+void index_lines(CsvFile& c) {
+    const char* s = c.text.data();
+    const size_t n = c.text.size();
+    size_t b = 0;
+    while (b < n) {
+        const void* q = std::memchr(s + b, '\n', n - b);
+        size_t e = q ? (size_t)((const char*)q - s) : n;
+        const size_t next = q ? e + 1 : n;
+        if (e > b && s[e - 1] == '\r') e--;
+        c.lines.emplace_back(b, e);
+        b = next;
+    }
+}
+
+// fields of one line, split at commas
+int split_fields(const char* b, const char* e, const char** fb, const char** fe, int cap) {
+    int k = 0;
+    const char* p = b;
+    while (k < cap) {
+        const char* q = (const char*)std::memchr(p, ',', (size_t)(e - p));
+        fb[k] = p;
+        fe[k] = q ? q : e;
+        k++;
+        if (!q) break;
+        p = q + 1;
+    }
+    return k;
+}
+
+template <typename T>
+bool parse_num(const char* b, const char* e, T& v) {
+    while (b < e && *b == ' ') b++;
+    while (e > b && e[-1] == ' ') e--;
+    if (b < e && *b == '+') b++;
+    const auto r = std::from_chars(b, e, v);
+    return r.ec == std::errc() && r.ptr == e;
+}
+
 }  // namespace
 
 extern "C" {
@@ -278,6 +343,77 @@ int mps_export_write(mps_engine* e, const char* csv_path, const char* vtu_path, 
     const int rc = mps_export_view(e, &s);
     if (rc) return rc;
     return mps_write_snapshot(&s, csv_path, vtu_path, time);
+}
+
+int mps_read_csv(const char* path, int32_t capacity, int32_t* n, double* time, double* pos,
+                 double* vel, int32_t* type) {
+    if (!path || !n) return err(MPS_ERR_ARG, "mps_read_csv: null argument");
+    CsvFile c;
+    if (!read_all(path, c.text))
+        return err(MPS_ERR_ARG, std::string("Input file does not exist in the specified path: ") + path);
+    index_lines(c);
+    if (c.lines.size() < 3) return err(MPS_ERR_ARG, std::string("particle CSV too short: ") + path);
+    const char* s = c.text.data();
+    const char *fb[64], *fe[64];
+    auto line_fields = [&](size_t r) {
+        return split_fields(s + c.lines[r].first, s + c.lines[r].second, fb, fe, 64);
+    };
+    if (line_fields(0) < 2 || (time && !parse_num(fb[1], fe[1], *time)))
+        return err(MPS_ERR_ARG, "particle CSV: bad time line");
+    const int nh = line_fields(2);
+    const char* need[8] = {"ID", "Type", "Position.x (m)", "Position.y (m)", "Position.z (m)",
+                           "Velocity.x (m/s)", "Velocity.y (m/s)", "Velocity.z (m/s)"};
+    int col[8];
+    for (int k = 0; k < 8; k++) {
+        col[k] = -1;
+        for (int h = 0; h < nh; h++)
+            if ((size_t)(fe[h] - fb[h]) == std::strlen(need[k]) && std::memcmp(fb[h], need[k], fe[h] - fb[h]) == 0)
+                col[k] = h;
+        if (col[k] < 0) return err(MPS_ERR_ARG, std::string("particle CSV lacks column ") + need[k]);
+    }
+    // data rows: non-empty lines after the header, in order
+    std::vector<size_t> rows;
+    rows.reserve(c.lines.size());
+    for (size_t r = 3; r < c.lines.size(); r++)
+        if (c.lines[r].second > c.lines[r].first) rows.push_back(r);
+    if (rows.size() > (size_t)INT32_MAX) return err(MPS_ERR_ARG, "particle CSV: too many rows");
+    *n = (int32_t)rows.size();
+    if (rows.size() > (size_t)std::max(capacity, 0)) return MPS_ERR_CAPACITY;
+    const int R = (int)rows.size();
+    const int hw = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const int T = R >= 65536 ? hw : 1;
+    std::vector<long long> bad(T, -1);  // first bad row per thread
+    auto work = [&](int t) {
+        const char *b[64], *e[64];
+        const int r0 = (int)((long long)R * t / T), r1 = (int)((long long)R * (t + 1) / T);
+        for (int i = r0; i < r1; i++) {
+            const auto& L = c.lines[rows[i]];
+            const int nf = split_fields(s + L.first, s + L.second, b, e, 64);
+            int id = -1, ty = 0;
+            double v[6];
+            bool ok = nf >= nh && parse_num(b[col[0]], e[col[0]], id) && id == i &&
+                      parse_num(b[col[1]], e[col[1]], ty);
+            for (int k = 0; ok && k < 6; k++) ok = parse_num(b[col[2 + k]], e[col[2 + k]], v[k]);
+            if (!ok) {
+                bad[t] = (long long)rows[i];
+                return;
+            }
+            if (type) type[i] = ty;
+            if (pos)
+                for (int k = 0; k < 3; k++) pos[3 * (size_t)i + k] = v[k];
+            if (vel)
+                for (int k = 0; k < 3; k++) vel[3 * (size_t)i + k] = v[3 + k];
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; t++) th.emplace_back(work, t);
+    work(0);
+    for (auto& x : th) x.join();
+    for (int t = 0; t < T; t++)
+        if (bad[t] >= 0)
+            return err(MPS_ERR_ARG, "particle CSV: bad row " + std::to_string(bad[t] + 1) +
+                                        " (fields, numbers, or an ID that is not its row index)");
+    return MPS_OK;
 }
 
 }  // extern "C"

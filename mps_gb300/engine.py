@@ -159,6 +159,8 @@ def load(build_if_missing: bool = False):
     L.mps_write_snapshot.argtypes = [P(MpsSnapshot), C.c_char_p, C.c_char_p, C.c_double]
     for name in ("mps_export_begin", "mps_export_view", "mps_export_write", "mps_write_snapshot"):
         getattr(L, name).restype = C.c_int
+    L.mps_read_csv.argtypes = [C.c_char_p, C.c_int32, P(C.c_int32), P(C.c_double), vp, vp, vp]
+    L.mps_read_csv.restype = C.c_int
     L.mps_last_error.restype = C.c_char_p
     for name in ("mps_create", "mps_destroy", "mps_set_solver", "mps_step", "mps_run",
                  "mps_download", "mps_upload", "mps_neighbors", "mps_system", "mps_collisions"):
@@ -184,6 +186,23 @@ def write_snapshot(snap: dict, csv_path=None, vtu_path=None, time=0.0):
     s = MpsSnapshot(n, dp(keep[0]), dp(keep[1]), dp(keep[2]), dp(keep[3]), ip(keep[4]), ip(keep[5]))
     enc = lambda q: None if q is None else os.fsencode(q)
     _check(L.mps_write_snapshot(C.byref(s), enc(csv_path), enc(vtu_path), float(time)))
+
+
+def read_particles_csv(path):
+    """The engine's particle CSV reader (the reference's importInitialCondition
+    format): (time, pos n x 3, vel n x 3, type n int32).  Host only."""
+    L = load()
+    n = C.c_int32(0)
+    tm = C.c_double(0.0)
+    enc = os.fsencode(path)
+    rc = L.mps_read_csv(enc, 0, C.byref(n), C.byref(tm), None, None, None)
+    if rc not in (0, 3):
+        _check(rc)
+    pos = np.zeros((n.value, 3))
+    vel = np.zeros((n.value, 3))
+    typ = np.zeros(n.value, np.int32)
+    _check(L.mps_read_csv(enc, n.value, C.byref(n), C.byref(tm), _p(pos), _p(vel), _p(typ)))
+    return tm.value, pos, vel, typ
 
 
 def make_params(p: dict) -> MpsParams:

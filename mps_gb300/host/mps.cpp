@@ -1,10 +1,9 @@
 #include "mps.hpp"
 
 #include <cmath>
-#include <fstream>
-#include <map>
-#include <sstream>
 #include <stdexcept>
+#include <string>
+#include <vector>
 
 #include "logger.hpp"
 
@@ -42,45 +41,21 @@ MPS::MPS(const std::filesystem::path& inputYamlPath) {
 // src/mps.cpp:38-94: the CSV written by Exporter::toCsv; ids must be the row
 // indices (the reference indexes particles by id).
 double MPS::importInitialCondition() {
-    std::ifstream in(settings.inputCsvPath);
-    if (!in.is_open())
-        throw std::runtime_error("Input file does not exist in the specified path: " + settings.inputCsvPath.string());
-    std::string line;
-    std::vector<std::string> rows;
-    while (std::getline(in, line)) {
-        if (!line.empty() && line.back() == '\r') line.pop_back();
-        rows.push_back(line);
-    }
-    if (rows.size() < 3) throw std::runtime_error("particle CSV too short: " + settings.inputCsvPath.string());
-    auto split = [](const std::string& s) {
-        std::vector<std::string> f;
-        std::stringstream ss(s);
-        std::string c;
-        while (std::getline(ss, c, ',')) f.push_back(c);
-        return f;
-    };
-    double t0 = std::stod(split(rows[0]).at(1));
-    auto head = split(rows[2]);
-    std::map<std::string, size_t> col;
-    for (size_t k = 0; k < head.size(); k++) col[head[k]] = k;
-    const char* need[] = {"ID", "Type", "Position.x (m)", "Position.y (m)", "Position.z (m)",
-                          "Velocity.x (m/s)", "Velocity.y (m/s)", "Velocity.z (m/s)"};
-    for (const char* k : need)
-        if (!col.count(k)) throw std::runtime_error(std::string("particle CSV lacks column ") + k);
+    // the engine's reader (one read, rows parsed on several threads)
+    const std::string path = settings.inputCsvPath.string();
+    int32_t n = 0;
+    double t0 = 0.0;
+    int rc = mps_read_csv(path.c_str(), 0, &n, &t0, nullptr, nullptr, nullptr);
+    if (rc != MPS_OK && rc != MPS_ERR_CAPACITY) throw std::runtime_error(mps_last_error());
+    std::vector<double> pos(3 * (size_t)n), vel(3 * (size_t)n);
+    std::vector<int32_t> type(n);
+    rc = mps_read_csv(path.c_str(), n, &n, &t0, pos.data(), vel.data(), type.data());
+    if (rc != MPS_OK) throw std::runtime_error(mps_last_error());
     particles.clear();
-    for (size_t r = 3; r < rows.size(); r++) {
-        if (rows[r].empty()) continue;
-        auto f = split(rows[r]);
-        int id = std::stoi(f.at(col["ID"]));
-        if (id != (int)particles.size())
-            throw std::runtime_error("particle ids must equal their row index (row " + std::to_string(r) + ")");
-        int type = std::stoi(f.at(col["Type"]));
-        Vec3 x(std::stod(f.at(col["Position.x (m)"])), std::stod(f.at(col["Position.y (m)"])),
-               std::stod(f.at(col["Position.z (m)"])));
-        Vec3 v(std::stod(f.at(col["Velocity.x (m/s)"])), std::stod(f.at(col["Velocity.y (m/s)"])),
-               std::stod(f.at(col["Velocity.z (m/s)"])));
-        particles.emplace_back(id, static_cast<ParticleType>(type), x, v, settings.density);
-    }
+    particles.reserve(n);
+    for (int32_t i = 0; i < n; i++)
+        particles.emplace_back(i, static_cast<ParticleType>(type[i]), Vec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]),
+                               Vec3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]), settings.density);
     return t0;
 }
 

@@ -211,3 +211,30 @@ def test_export_writers_match_reference_formats(built, tmp_path, n):
     write_snapshot(s, tmp_path / "o.csv", tmp_path / "o.vtu", 0.0125)
     assert (tmp_path / "o.csv").read_text() == _reference_csv(s, 0.0125)
     assert (tmp_path / "o.vtu").read_text() == _reference_vtu(s, 0.0125)
+
+
+def test_csv_reader_matches_python_parser(built, tmp_path):
+    """mps_read_csv (parallel, from_chars) against the Python reader on a
+    scene written in the reference's CSV format, with CRLF line ends and an
+    empty line; a bad ID is reported."""
+    from mps_gb300 import read_particles_csv, scenes
+
+    prm, pos, vel, t = scenes.dam_break(1 / 640, tank=(1.0, 0.6), column=(0.5, 0.5))
+    rng = np.random.default_rng(5)
+    vel[:, :2] = rng.normal(0.0, 0.3, (len(t), 2))
+    path = tmp_path / "in.csv"
+    scenes.write_csv(path, pos, vel, t, time=0.25)
+    assert len(t) > 65536  # the multithreaded path
+    tm, p2, v2, t2 = read_particles_csv(path)
+    tm0, p0, v0, t0 = scenes.read_csv(path)
+    assert tm == tm0 == 0.25
+    assert np.array_equal(p2, p0) and np.array_equal(v2, v0) and np.array_equal(t2, t0)
+    lines = path.read_text().splitlines()
+    crlf = tmp_path / "crlf.csv"
+    crlf.write_bytes(("\r\n".join(lines[:10] + [""] + lines[10:]) + "\r\n").encode())
+    tm, p3, v3, t3 = read_particles_csv(crlf)
+    assert np.array_equal(p3, p0) and np.array_equal(t3, t0)
+    bad = tmp_path / "bad.csv"
+    bad.write_text("\n".join(lines[:5] + [lines[6]] + lines[6:]) + "\n")
+    with pytest.raises(Exception, match="bad row"):
+        read_particles_csv(bad)
