@@ -208,8 +208,7 @@ struct Mg {
     MgLevel lev[kMgMaxLevels];
     float* e0;      // level-0 correction (per slot)
     float* res0;    // level-0 residual (per slot)
-    float* dense;   // inverse of the coarsest operator (nc x nc)
-    int32_t nc;
+    float* dense;   // inverse of the coarsest operator (cells x cells of level nlev)
     float omega;    // damped-Jacobi weight
     float scale;    // coarse-correction scale
     // 0: multiplicative V(1,1) from level 0 (Jacobi pre- and post-smoothing
