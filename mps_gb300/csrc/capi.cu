@@ -256,7 +256,7 @@ void enqueue_step(mps_engine* e, bool do_export) {
 // Jacobi preconditioner; with the multigrid V-cycle, per cell of level 1
 // 72 B (segment bounds, the up pass's 9-point stencil and 8 vector words)
 // and of levels >= 2 132 B (the same plus the 4x4 restriction weights), and,
-// additive at level 0, 89 B per row, multiplicative 143 B per row and two
+// additive at level 0, 81 B per row, multiplicative 143 B per row and two
 // more level-0 operator passes.  MIXED adds per refinement the FP64
 // residual (12 B/entry + 36 B/row) and once the FP32 operator setup
 // (17 B/entry + 16 B/row written and read).
@@ -267,7 +267,7 @@ double solve_bytes(const mps_engine* e, const DevStats& h) {
     const bool additive = mg && e->mg_requested == 1;
     const double ent = e->c.planar ? 5.0 : 8.0;
     double per_it = !mg ? (ent * nnz + 65.0 * n)
-                        : additive ? (ent * nnz + 89.0 * n) : (3.0 * ent * nnz + 143.0 * n);
+                        : additive ? (ent * nnz + 81.0 * n) : (3.0 * ent * nnz + 143.0 * n);
     if (mg)
         for (int l = 1; l <= e->mg.nlev; l++)
             per_it += (l == 1 ? 72.0 : 132.0) * e->mg.lev[l].nx * e->mg.lev[l].ny;

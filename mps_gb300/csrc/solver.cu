@@ -885,6 +885,8 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
             }
             gamma_old = gamma;
             // phase A: p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; u = M r
+            // (the additive cycle starts from r alone: no level-0 pre-smoothing here)
+            const bool need_id = !mg.enabled || !mg.additive;
             // Four of this thread's rows per iteration, all loads before any
             // store (the compiler cannot move loads above stores to arrays it
             // cannot prove distinct): four rows' memory traffic in flight.
@@ -899,7 +901,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
                     w[h] = kv.w32[i];
                     x[h] = kv.x32[i];
                     r[h] = kv.r32[i];
-                    id[h] = kv.inv_diag32[i];
+                    id[h] = need_id ? kv.inv_diag32[i] : 0.f;
                 }
 #pragma unroll
                 for (int h = 0; h < 4; h++) {
@@ -912,10 +914,10 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
                     kv.x32[i] = fmaf(alpha, pn, x[h]);
                     const float rn = fmaf(-alpha, sn, r[h]);
                     kv.r32[i] = rn;
-                    if (mg.enabled)
-                        mg.e0[i] = mg.omega * id[h] * rn;
-                    else
+                    if (!mg.enabled)
                         kv.u32[i] = id[h] * rn;
+                    else if (!mg.additive)
+                        mg.e0[i] = mg.omega * id[h] * rn;
                 }
             }
             k++;
