@@ -296,13 +296,17 @@ int mps_export_begin(mps_engine* e) {
     if (!e) return err(MPS_ERR_ARG, "null engine");
     const size_t np = e->n_pad;
     if (!e->xdev) {
-        XCU(cudaStreamCreateWithFlags(&e->xst, cudaStreamNonBlocking));
-        XCU(cudaEventCreateWithFlags(&e->xev_ready, cudaEventDisableTiming));
-        XCU(cudaEventCreateWithFlags(&e->xev_done, cudaEventDisableTiming));
-        XCU(cudaMallocHost(&e->xhost, sizeof(double) * 8 * np));
-        XCU(cudaMallocHost(&e->xhost_i, sizeof(int32_t) * 2 * np));
-        if (e->alloc(&e->xdev, 8 * np) || e->alloc(&e->xdev_i, 2 * np))
-            return err(MPS_ERR_CUDA, "cudaMalloc export buffers");
+        // all or nothing: each resource is created once (mps_destroy frees
+        // what exists), and the buffers count as ready only when all are
+        if (!e->xst) XCU(cudaStreamCreateWithFlags(&e->xst, cudaStreamNonBlocking));
+        if (!e->xev_ready) XCU(cudaEventCreateWithFlags(&e->xev_ready, cudaEventDisableTiming));
+        if (!e->xev_done) XCU(cudaEventCreateWithFlags(&e->xev_done, cudaEventDisableTiming));
+        if (!e->xhost) XCU(cudaMallocHost(&e->xhost, sizeof(double) * 8 * np));
+        if (!e->xhost_i) XCU(cudaMallocHost(&e->xhost_i, sizeof(int32_t) * 2 * np));
+        double* d = nullptr;
+        if (!e->xdev_i && e->alloc(&e->xdev_i, 2 * np)) return err(MPS_ERR_CUDA, "cudaMalloc export buffers");
+        if (e->alloc(&d, 8 * np)) return err(MPS_ERR_CUDA, "cudaMalloc export buffers");
+        e->xdev = d;
     }
     // the device buffer is rewritten only after the last snapshot left it
     if (e->x_pending) XCU(cudaStreamWaitEvent(e->st, e->xev_done, 0));
