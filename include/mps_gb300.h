@@ -116,6 +116,15 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
  * (its CG is Jacobi-preconditioned). */
 int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale);
 
+/* Self-test of the device-side wait limits (no counterpart in the
+ * reference): runs the solver's grid barrier on 8 blocks in a group that
+ * counts 9, so no block can pass; every block must give up with the timeout
+ * status (its own spin limit, 2^16 polls here against the solver's 2^23,
+ * ~2.4 s; or the flag of the first block that gave up) and the kernel ends
+ * normally, leaving the context usable.
+ * MPS_OK when all 8 gave up with that status. */
+int mps_selftest_wait_limit(int32_t* blocks_gave_up, double* seconds);
+
 /* Non-export steps run as a CUDA graph replay (default on): the first step
  * at each buffer parity captures the step's kernel sequence, later steps
  * replay it.  Changing the solver or the multigrid settings drops the

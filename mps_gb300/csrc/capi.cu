@@ -667,6 +667,19 @@ int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale) {
     return MPS_OK;
 }
 
+int mps_selftest_wait_limit(int32_t* blocks_gave_up, double* seconds) {
+    int gave = 0, status = 0;
+    float ms = 0.f;
+    constexpr int kBlocks = 8;
+    if (selftest_wait_limit(kBlocks, &gave, &status, &ms) != 0)
+        return fail(MPS_ERR_CUDA, "mps_selftest_wait_limit: CUDA call failed");
+    if (blocks_gave_up) *blocks_gave_up = gave;
+    if (seconds) *seconds = ms * 1e-3;
+    if (gave != kBlocks || !(status & ST_TIMEOUT))
+        return fail(MPS_ERR_TIMEOUT, "mps_selftest_wait_limit: not every block gave up with the timeout status");
+    return MPS_OK;
+}
+
 int mps_set_graphs(mps_engine* e, int32_t enabled) {
     if (!e) return fail(MPS_ERR_ARG, "null engine");
     e->use_graph = enabled ? 1 : 0;

@@ -228,6 +228,9 @@ struct Krylov {
     int32_t block;
 };
 void solver_setup(Krylov& k, int32_t n_pad, int device);
+// Runs the grid barrier with one block that never arrives on `blocks`
+// blocks; reports how many gave up, the status word and the kernel time.
+int selftest_wait_limit(int blocks, int* gave_up, int* status, float* ms);
 // Solves A x = b; returns through DevStats (iterations, residual, status).
 void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double tol,
                        int64_t max_iter, DevStats* ds, cudaStream_t st);

@@ -40,7 +40,10 @@ namespace {
 // code on groups of blocks, each group with its own barrier and partials.
 constexpr int kBlock = 1024;
 constexpr int kMixedBlock = 1024;  // k_cg_mixed: one block per SM
-constexpr long long kSpinLimit = 1ll << 25;  // ~1-2 s with the back-off below
+// Polls before a barrier wait gives up: one poll (an acquire load plus the
+// back-off) takes ~0.28 us on GB300 (measured by mps_selftest_wait_limit),
+// so ~2.4 s, far above any legitimate wait (tens of microseconds).
+constexpr long long kSpinLimit = 1ll << 23;
 
 struct SolveArgs {
     int32_t n;          // rows (slots)
@@ -67,6 +70,7 @@ struct GridBar {
     int rank;            // this block's index within its group
     int size;            // blocks in the group (the whole grid for a single scene)
     double* partials;    // 2 x size x 8 per-block partial sums of the group
+    long long spin_limit = kSpinLimit;  // polls before a barrier wait gives up
 };
 
 __device__ __forceinline__ GridBar whole_grid(const Krylov& kv) {
@@ -102,7 +106,7 @@ __device__ __forceinline__ bool grid_sync(GridBar& gb, DevStats* ds) {
                     ok = false;
                     break;
                 }
-                if (it > kSpinLimit) {
+                if (it > gb.spin_limit) {
                     atomicOr(&ds->status, ST_TIMEOUT);
                     ok = false;
                     break;
@@ -321,12 +325,6 @@ __device__ __forceinline__ void compact_pair(const Ppe& A, const MatFree& mf, in
     }
     oa = a0 + a1;
     ob = b0 + b1;
-}
-
-// Off-diagonal part of row i of the FP32 operator.
-__device__ __forceinline__ float off_row(const Ppe& A, const MatFree& mf, int K, int i,
-                                         const float* __restrict__ v) {
-    return (mf.enabled && !mf.sell_row[i]) ? compact_row_sum(A, mf, K, i, v) : spmv32_sell_row(A, K, i, v);
 }
 
 // Off-diagonal parts of rows i and i2 (i2 < 0: none), paired when both are
@@ -1067,6 +1065,53 @@ void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double to
     cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
     cudaLaunchCooperativeKernel((const void*)k_cg64, dim3(k.grid), dim3(kBlock), args, 0, st);
     ++g_launches;
+}
+
+// Self-test of the bounded waits: the solver's grid barrier in a group that
+// counts one block more than the launch has, so no block can pass.  Every
+// block gives up (at its spin limit, here 2^16 polls instead of the solver's
+// 2^23, or on the flag of the first that did), records it and ends; nothing
+// faults and nothing is left waiting.
+namespace {
+__global__ void k_selftest_barrier(unsigned int* words, DevStats* ds) {
+    GridBar gb{words, 0u, 0, (int)blockIdx.x, (int)gridDim.x + 1, nullptr, 1ll << 16};
+    const bool ok = grid_sync(gb, ds);
+    if (threadIdx.x == 0 && !ok) atomicAdd(words + 1, 1u);
+}
+}  // namespace
+
+int selftest_wait_limit(int blocks, int* gave_up, int* status, float* ms) {
+    unsigned int* words = nullptr;
+    DevStats* ds = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = 0;
+    if (cudaMalloc(&words, 2 * sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc(&ds, sizeof(DevStats)) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess) {
+        rc = -1;
+    } else {
+        cudaMemset(words, 0, 2 * sizeof(unsigned int));
+        cudaMemset(ds, 0, sizeof(DevStats));
+        cudaEventRecord(e0);
+        k_selftest_barrier<<<blocks, 64>>>(words, ds);
+        cudaEventRecord(e1);
+        unsigned int h[2] = {0, 0};
+        DevStats hs{};
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(h, words, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(&hs, ds, sizeof hs, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            rc = -1;
+        } else {
+            *gave_up = (int)h[1];
+            *status = hs.status;
+            cudaEventElapsedTime(ms, e0, e1);
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(words);
+    cudaFree(ds);
+    return rc;
 }
 
 // ----------------------------------------------------------- batched solve

@@ -161,6 +161,8 @@ def load(build_if_missing: bool = False):
         getattr(L, name).restype = C.c_int
     L.mps_read_csv.argtypes = [C.c_char_p, C.c_int32, P(C.c_int32), P(C.c_double), vp, vp, vp]
     L.mps_read_csv.restype = C.c_int
+    L.mps_selftest_wait_limit.argtypes = [P(C.c_int32), P(C.c_double)]
+    L.mps_selftest_wait_limit.restype = C.c_int
     L.mps_last_error.restype = C.c_char_p
     for name in ("mps_create", "mps_destroy", "mps_set_solver", "mps_step", "mps_run",
                  "mps_download", "mps_upload", "mps_neighbors", "mps_system", "mps_collisions"):
@@ -203,6 +205,16 @@ def read_particles_csv(path):
     typ = np.zeros(n.value, np.int32)
     _check(L.mps_read_csv(enc, n.value, C.byref(n), C.byref(tm), _p(pos), _p(vel), _p(typ)))
     return tm.value, pos, vel, typ
+
+
+def selftest_wait_limit():
+    """Runs the device-side wait-limit self-test (include/mps_gb300.h):
+    (return code, blocks that gave up, seconds)."""
+    L = load()
+    g = C.c_int32(0)
+    sec = C.c_double(0.0)
+    rc = L.mps_selftest_wait_limit(C.byref(g), C.byref(sec))
+    return rc, g.value, sec.value
 
 
 def make_params(p: dict) -> MpsParams:
