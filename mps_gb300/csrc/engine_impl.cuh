@@ -81,7 +81,7 @@ struct mps_engine {
     // Set while a trajectory records a step for its adjoint (eager launches).
     const mpsg::TapeStep* tape = nullptr;
     cudaEvent_t ev[4]{};
-    // asynchronous export (export.cu): device gather buffer, pinned host
+    // asynchronous export (io.cu): device gather buffer, pinned host
     // snapshot, side stream; allocated on first use
     double* xdev = nullptr;   // 8 x n_pad: pos 3, vel 3, pressure, ndr
     int32_t* xdev_i = nullptr;  // 2 x n_pad: type, bc
