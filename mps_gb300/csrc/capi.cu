@@ -153,7 +153,8 @@ int alloc_state(mps_engine* e, StateBuf& s) {
 Mg active_mg(const mps_engine* e) {
     Mg g = e->mg;
     g.enabled = e->mg.enabled && e->mg_requested != 0;
-    g.additive = e->mg_requested == 1;
+    g.additive = e->mg_requested == 1 || e->mg_requested == 3;
+    g.smooth = e->mg_requested == 3;
     return g;
 }
 
@@ -256,18 +257,20 @@ void enqueue_step(mps_engine* e, bool do_export) {
 // Jacobi preconditioner; with the multigrid V-cycle, per cell of level 1
 // 72 B (segment bounds, the up pass's 9-point stencil and 8 vector words)
 // and of levels >= 2 132 B (the same plus the 4x4 restriction weights), and,
-// additive at level 0, 81 B per row, multiplicative 143 B per row and two
-// more level-0 operator passes.  MIXED adds per refinement the FP64
+// additive at level 0, 81 B per row (161 B with the smoothed transfer: the
+// 9 row-to-cell sums read twice and the neighbourhood's residuals),
+// multiplicative 143 B per row and two more level-0 operator passes.  MIXED adds per refinement the FP64
 // residual (12 B/entry + 36 B/row) and once the FP32 operator setup
 // (17 B/entry + 16 B/row written and read).
 double solve_bytes(const mps_engine* e, const DevStats& h) {
     const double nnz = (double)h.nnz_off, n = (double)e->n, it = (double)h.cg_iterations;
     if (e->precision == MPS_PRECISION_FP64) return it * (12.0 * nnz + 116.0 * n) + 36.0 * n;
     const bool mg = e->mg.enabled && e->mg_requested != 0;
-    const bool additive = mg && e->mg_requested == 1;
+    const bool additive = mg && (e->mg_requested == 1 || e->mg_requested == 3);
+    const bool smooth = mg && e->mg_requested == 3;
     const double ent = e->c.planar ? 5.0 : 8.0;
     double per_it = !mg ? (ent * nnz + 65.0 * n)
-                        : additive ? (ent * nnz + 81.0 * n) : (3.0 * ent * nnz + 143.0 * n);
+                        : additive ? (ent * nnz + (smooth ? 161.0 : 81.0) * n) : (3.0 * ent * nnz + 143.0 * n);
     if (mg)
         for (int l = 1; l <= e->mg.nlev; l++)
             per_it += (l == 1 ? 72.0 : 132.0) * e->mg.lev[l].nx * e->mg.lev[l].ny;
@@ -574,8 +577,9 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         while (g.ngrid + 1 < g.nlev && (size_t)g.lev[g.ngrid + 1].nx * g.lev[g.ngrid + 1].ny > kMgBlockCells)
             g.ngrid++;
         if (e->alloc(&g.e0, np) || e->alloc(&g.res0, np) ||
-            e->alloc(&g.dense, (size_t)kMgMaxCoarsest * kMgMaxCoarsest))
+            e->alloc(&g.dense, (size_t)kMgMaxCoarsest * kMgMaxCoarsest) || e->alloc(&g.rowcell, 9 * np))
             return bail(fail(MPS_ERR_CUDA, "cudaMalloc multigrid"));
+        g.n_pad = (int32_t)np;
     }
     if (e->alloc(&e->kv.partials, (size_t)e->kv.grid * 16))
         return bail(fail(MPS_ERR_CUDA, "cudaMalloc partials"));
@@ -651,7 +655,7 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
 
 int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale) {
     if (!e) return fail(MPS_ERR_ARG, "null engine");
-    if (mode < 0 || mode > 2) return fail(MPS_ERR_ARG, "multigrid mode must be 0, 1 or 2");
+    if (mode < 0 || mode > 3) return fail(MPS_ERR_ARG, "multigrid mode must be 0, 1, 2 or 3");
     if (mode && !e->mg.enabled)
         return fail(MPS_ERR_ARG, "multigrid needs a planar scene (2-D, constant z)");
     float dw, ds;

@@ -215,6 +215,13 @@ struct Mg {
     // around the coarse correction); 1: additive at level 0, u = omega D^-1 r
     // + scale P V1(P^T r) (no level-0 operator pass; still SPD)
     int32_t additive;
+    // additive with a smoothed particle-to-cell transfer: P = P1 - omega D^-1 A P1
+    // in place of P1 (the cell levels keep the operators of plain aggregation)
+    int32_t smooth;
+    // B = A P1 per slot: the operator row's sums over the 3x3 cells around the
+    // slot's own, entry d = (dx+1)*3 + (dy+1), diagonal included (9 x n_pad)
+    float* rowcell;
+    int32_t n_pad;
 };
 
 // --------------------------------------------------------------- solver.cu

@@ -53,7 +53,9 @@ struct mps_engine {
     mpsg::Krylov kv{};
     mpsg::MatFree mf{};
     mpsg::Mg mg{};
-    int32_t mg_requested = 1;  // 0 Jacobi, 1 multigrid additive at level 0, 2 multiplicative
+    // 0 Jacobi, 1 multigrid additive at level 0, 2 multiplicative, 3 additive
+    // with the smoothed particle-to-cell transfer
+    int32_t mg_requested = 1;
     int32_t *cand_cnt = nullptr, *cand_base = nullptr;
     mpsg::CollPair* pairs = nullptr;
     int32_t pair_cap = 0;

@@ -92,6 +92,70 @@ __global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L) {
     L.invd[I] = st[4] > 0.f ? 1.f / st[4] : 0.f;
 }
 
+// Smoothed transfer: B = A P1 per slot (the row's sums over the 3x3 cells
+// around its own, diagonal included), in the entry order of k_mg_level1.
+// Slots that are not unknowns get 0.
+__global__ void k_mg_rowcell(Consts c, Ppe A, MatFree mf, size_t np, float* __restrict__ B) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    float st[9];
+#pragma unroll
+    for (int d = 0; d < 9; d++) st[d] = 0.f;
+    const float dg = A.diag32[i];
+    if (dg > 0.f) {
+        st[4] = dg;
+        // an unknown is Inner, so its cell is an interior cell of the grid
+        const int key = mf.skey[i];
+        const int cx = key / c.numY, cy = key - cx * c.numY;
+        const int cnt = A.offcnt[i];
+        if (mf.enabled && !mf.sell_row[i]) {
+            int rs[3][4];
+            for (int r = 0; r < 3; r++) {
+                const int kk = (cx - 1 + r) * c.numY + cy - 1;
+                for (int q = 0; q < 4; q++) rs[r][q] = mf.cs[kk + q];
+            }
+            const size_t q0 = qsell_index(i, 0, c.K) >> 2;
+            const float4* vp = reinterpret_cast<const float4*>(A.val32) + q0;
+            const uint32_t* ip = reinterpret_cast<const uint32_t*>(mf.idx8) + q0;
+            const int ng = (cnt + 3) >> 2;
+            for (int g0 = 0; g0 < ng; g0 += 4) {
+                float4 v[4];
+                uint32_t b4[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int gi = min(g0 + q, ng - 1);
+                    v[q] = __ldg(vp + gi * 32);
+                    b4[q] = __ldg(ip + gi * 32);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float vv[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
+#pragma unroll
+                    for (int t = 0; t < 4; t++) {
+                        if ((g0 + q) * 4 + t >= cnt) break;
+                        const int bt = (b4[q] >> (8 * t)) & 255;
+                        const int r = bt >> 6;
+                        const int j = rs[r][0] + (bt & 63);
+                        const int dy = (j >= rs[r][1]) + (j >= rs[r][2]) - 1;
+                        add_tap(st, r * 3 + (dy + 1), vv[t]);
+                    }
+                }
+            }
+        } else {
+            const size_t base = (size_t)(i >> 5) * c.K * 32 + (i & 31);
+            for (int m = 0; m < cnt; m++) {
+                const float v = A.val32[qsell_index(i, m, c.K)];
+                const int j = A.col[base + (size_t)m * 32];
+                const int kj = mf.skey[j];
+                const int jx = kj / c.numY, jy = kj - jx * c.numY;
+                add_tap(st, (jx - cx + 1) * 3 + (jy - cy + 1), v);
+            }
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 9; d++) B[(size_t)d * np + i] = st[d];
+}
+
 // Coarse level C from fine level F: the Galerkin 9-point stencil and C's
 // restriction weights (MgLevel::rw).  The residual that the V-cycle hands
 // from F to C is, for each child c of a coarse cell, r_c - sum_d st_d(c)
@@ -178,6 +242,10 @@ void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg&
                      cudaStream_t st) {
     if (!mg.enabled) return;
     const int T = 256;
+    if (mg.smooth) {
+        k_mg_rowcell<<<(c.n + T - 1) / T, T, 0, st>>>(c, A, mf, (size_t)mg.n_pad, mg.rowcell);
+        ++g_launches;
+    }
     const MgLevel& L1 = mg.lev[1];
     k_mg_level1<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(c, A, mf, L1);
     ++g_launches;

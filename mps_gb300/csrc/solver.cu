@@ -611,7 +611,8 @@ __device__ void mg_block_cycle(Mg& mg, int lo) {
 template <int BS>
 __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& mf, int K,
                                           const float* __restrict__ r, float* __restrict__ u,
-                                          int n, GridBar& gb, DevStats* ds) {
+                                          const float* __restrict__ invd0, int n, GridBar& gb,
+                                          DevStats* ds) {
     const int gtid = gb.rank * BS + threadIdx.x;
     const int gsz = gb.size * BS;
     // Cells of the grid levels are dealt to blocks in interleaved 32-cell
@@ -642,7 +643,40 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     // a round before any use (predicated: slots past a cell's end are not
     // read, which also keeps the many empty cells off any one address):
     // each cell still sums its slots in slot order.
-    {
+    if (mg.smooth) {
+        // smoothed transfer: r1 = P^T r = P1^T r - omega B^T D^-1 r, where row i
+        // of the 3x3 cells around cell I adds B[d][i] r_i / d_i with d the
+        // offset from its cell to I.  A column of three cells is one slot
+        // range (rows in cell order), split by the cell starts.
+        MgLevel& L1 = mg.lev[1];
+        const int n1 = L1.nx * L1.ny, NY = L1.ny;
+        const size_t np = (size_t)mg.n_pad;
+        for (int I = gcell; I < n1; I += gsz) {
+            const float iv = __ldg(L1.invd + I);
+            float rr = 0.f;
+            if (iv > 0.f) {  // a cell with an unknown: an interior cell of the grid
+                const int cx = I / NY, cy = I - cx * NY;
+                const int b = __ldg(mf.cs + I), e = __ldg(mf.cs + I + 1);
+                float acc = 0.f;
+                for (int i = b; i < e; i++) acc += __ldcg(src0 + i);
+                float corr = 0.f;
+#pragma unroll 1
+                for (int dxn = -1; dxn <= 1; dxn++) {
+                    const int k0 = (cx + dxn) * NY + cy - 1;
+                    const int c1 = __ldg(mf.cs + k0 + 1), c2 = __ldg(mf.cs + k0 + 2);
+                    const int c0 = __ldg(mf.cs + k0), c3 = __ldg(mf.cs + k0 + 3);
+                    for (int i = c0; i < c3; i++) {
+                        const int q = (i >= c1) + (i >= c2);
+                        const int d = (1 - dxn) * 3 + (2 - q);
+                        corr = fmaf(__ldg(mg.rowcell + (size_t)d * np + i), __ldcg(src0 + i) * __ldg(invd0 + i), corr);
+                    }
+                }
+                rr = acc - mg.omega * corr;
+            }
+            L1.r[I] = rr;
+            L1.e[I] = mg.omega * iv * rr;
+        }
+    } else {
         MgLevel& L1 = mg.lev[1];
         const int n1 = L1.nx * L1.ny;
         for (int I0 = gcell; I0 < n1; I0 += 4 * gsz) {
@@ -708,6 +742,46 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         float* tmp = L.e;
         L.e = L.t;
         L.t = tmp;
+    }
+    if (mg.additive && mg.smooth) {
+        // u = omega D^-1 r + scale * P e1, P e1 = e1[cell(i)] - omega / d_i sum_d B[d][i] e1[cell(i) + d]
+        MgLevel& L1 = mg.lev[1];
+        const int n1 = L1.nx * L1.ny, NY = L1.ny;
+        const size_t np = (size_t)mg.n_pad;
+        for (int i0 = gtid; i0 < n; i0 += 2 * gsz) {
+            float dg[2], ri[2];
+            int key[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int i = min(i0 + h * gsz, n - 1);
+                dg[h] = A.diag32[i];
+                key[h] = min(__ldg(mf.skey + i), n1 - 1);
+                ri[h] = __ldcg(r + i);
+            }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int i = i0 + h * gsz;
+                if (i >= n) break;
+                float v = 0.f;
+                if (dg[h] > 0.f) {  // an unknown: its cell is interior
+                    const int k = key[h];
+                    const float ec = __ldcg(L1.e + k);
+                    float bt[9], en[9];
+#pragma unroll
+                    for (int d = 0; d < 9; d++) {
+                        bt[d] = __ldg(mg.rowcell + (size_t)d * np + i);
+                        en[d] = __ldcg(L1.e + k + (d / 3 - 1) * NY + (d % 3 - 1));
+                    }
+                    float corr = 0.f;
+#pragma unroll
+                    for (int d = 0; d < 9; d++) corr = fmaf(bt[d], en[d], corr);
+                    const float w = mg.omega / dg[h];
+                    v = fmaf(mg.scale, ec - w * corr, w * ri[h]);
+                }
+                u[i] = v;
+            }
+        }
+        return true;
     }
     if (mg.additive) {
         // u = omega D^-1 r + scale * (level-1 correction of the row's cell)
@@ -833,7 +907,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
         }
         if (!grid_sync(gb, ds)) return;
         if (mg.enabled) {
-            if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds)) return;
+            if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, kv.inv_diag32, a.n, gb, ds)) return;
             if (!grid_sync(gb, ds)) return;
         }
         float alpha = 0.f, beta = 0.f, gamma_old = 1.f;
@@ -921,7 +995,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
             k++;
             if (!grid_sync(gb, ds)) return;
             if (mg.enabled) {
-                if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, a.n, gb, ds)) return;
+                if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, kv.inv_diag32, a.n, gb, ds)) return;
                 if (!grid_sync(gb, ds)) return;
             }
         }

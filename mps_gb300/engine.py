@@ -282,12 +282,13 @@ class Engine:
     def set_solver(self, precision=FP64, tol=0.0, max_iter=0):
         _check(_lib.mps_set_solver(self._h, int(precision), float(tol), int(max_iter)))
 
-    MG_JACOBI, MG_ADDITIVE, MG_MULTIPLICATIVE = 0, 1, 2
+    MG_JACOBI, MG_ADDITIVE, MG_MULTIPLICATIVE, MG_SMOOTHED = 0, 1, 2, 3
 
     def set_multigrid(self, mode=1, omega=0.0, scale=0.0):
         """Preconditioner of the MIXED solver: 0 Jacobi, 1 multigrid additive at
-        the particle level (default), 2 multiplicative V(1,1) (True/False map
-        to 1/0).  omega/scale 0 take the mode's default weights."""
+        the particle level (default), 2 multiplicative V(1,1), 3 additive with
+        the smoothed particle-to-cell transfer (True/False map to 1/0).
+        omega/scale 0 take the mode's default weights."""
         mode = int(mode) if not isinstance(mode, bool) else (1 if mode else 0)
         _check(_lib.mps_set_multigrid(self._h, mode, float(omega), float(scale)))
 

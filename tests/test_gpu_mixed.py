@@ -1,8 +1,8 @@
 """The mixed-precision solver against the FP64 one, from the same state, for
 each preconditioner of the mixed solver (Jacobi, multigrid additive at the
-particle level, multiplicative V(1,1)): the pressure agrees within relative
-L2 1e-6 (the solver stops at relative residual 1e-10), surface flags
-exactly."""
+particle level, multiplicative V(1,1), additive with the smoothed transfer):
+the pressure agrees within relative L2 1e-6 (the solver stops at relative
+residual 1e-10), surface flags exactly."""
 import numpy as np
 import pytest
 
@@ -11,7 +11,7 @@ from gpu_util import engine_or_skip, rel_l2
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
 def test_mixed_matches_fp64(mode):
     m = engine_or_skip()
     from mps_gb300 import scenes
