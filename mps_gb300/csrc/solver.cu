@@ -656,19 +656,40 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
             float rr = 0.f;
             if (iv > 0.f) {  // a cell with an unknown: an interior cell of the grid
                 const int cx = I / NY, cy = I - cx * NY;
-                const int b = __ldg(mf.cs + I), e = __ldg(mf.cs + I + 1);
+                // the 12 cell starts of the three columns in one batch
+                int cb[3][4];
+#pragma unroll
+                for (int x = 0; x < 3; x++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) cb[x][q] = __ldg(mf.cs + (cx - 1 + x) * NY + cy - 1 + q);
+                // own cell (column x = 1, cell q = 1), eight slots per batch of
+                // predicated loads; sums in slot order
                 float acc = 0.f;
-                for (int i = b; i < e; i++) acc += __ldcg(src0 + i);
+                for (int i0 = cb[1][1]; i0 < cb[1][2]; i0 += 8) {
+                    float v[8];
+#pragma unroll
+                    for (int h = 0; h < 8; h++) v[h] = i0 + h < cb[1][2] ? __ldcg(src0 + i0 + h) : 0.f;
+#pragma unroll
+                    for (int h = 0; h < 8; h++)
+                        if (i0 + h < cb[1][2]) acc += v[h];
+                }
                 float corr = 0.f;
 #pragma unroll 1
-                for (int dxn = -1; dxn <= 1; dxn++) {
-                    const int k0 = (cx + dxn) * NY + cy - 1;
-                    const int c1 = __ldg(mf.cs + k0 + 1), c2 = __ldg(mf.cs + k0 + 2);
-                    const int c0 = __ldg(mf.cs + k0), c3 = __ldg(mf.cs + k0 + 3);
-                    for (int i = c0; i < c3; i++) {
-                        const int q = (i >= c1) + (i >= c2);
-                        const int d = (1 - dxn) * 3 + (2 - q);
-                        corr = fmaf(__ldg(mg.rowcell + (size_t)d * np + i), __ldcg(src0 + i) * __ldg(invd0 + i), corr);
+                for (int x = 0; x < 3; x++) {
+                    const int c0 = cb[x][0], c1 = cb[x][1], c2 = cb[x][2], c3 = cb[x][3];
+                    for (int i0 = c0; i0 < c3; i0 += 8) {
+                        float bv[8], yv[8];
+#pragma unroll
+                        for (int h = 0; h < 8; h++) {
+                            const int i = i0 + h;
+                            const int q = (i >= c1) + (i >= c2);
+                            const int d = (2 - x) * 3 + (2 - q);  // offset from the row's cell to I
+                            const bool in = i < c3;
+                            bv[h] = in ? __ldg(mg.rowcell + (size_t)d * np + i) : 0.f;
+                            yv[h] = in ? __ldcg(src0 + i) * __ldg(invd0 + i) : 0.f;
+                        }
+#pragma unroll
+                        for (int h = 0; h < 8; h++) corr = fmaf(bv[h], yv[h], corr);
                     }
                 }
                 rr = acc - mg.omega * corr;
