@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -80,21 +81,27 @@ inline void put_int(std::string& s, long long v) {
     s.append(b, r.ptr);
 }
 
-// Formats [0, n) in chunks on up to 16 threads and writes them in order.
+// Formats [0, n) in chunks on up to 16 threads (about row_bytes each) and
+// writes them in order; chunks whose thread could not start run here.
 template <typename F>
-bool write_rows(std::FILE* f, int n, F&& row) {
+bool write_rows(std::FILE* f, int n, size_t row_bytes, F&& row) {
     const int hw = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     const int T = n >= 65536 ? hw : 1;
     std::vector<std::string> part(T);
     auto work = [&](int t) {
         const int b = (int)((long long)n * t / T), e = (int)((long long)n * (t + 1) / T);
         std::string& s = part[t];
-        s.reserve((size_t)(e - b) * 96);
+        s.reserve((size_t)(e - b) * row_bytes);
         for (int i = b; i < e; i++) row(s, i);
     };
     std::vector<std::thread> th;
-    for (int t = 1; t < T; t++) th.emplace_back(work, t);
+    int started = 1;
+    try {
+        for (int t = 1; t < T; t++, started++) th.emplace_back(work, t);
+    } catch (const std::system_error&) {
+    }
     work(0);
+    for (int t = started; t < T; t++) work(t);
     for (auto& x : th) x.join();
     for (auto& s : part)
         if (!s.empty() && std::fwrite(s.data(), 1, s.size(), f) != s.size()) return false;
@@ -114,7 +121,7 @@ int write_csv(const mps_snapshot& s, const char* path, double time) {
     put_int(h, s.n);
     h += "\nID,Type,Position.x (m),Position.y (m),Position.z (m),Velocity.x (m/s),Velocity.y (m/s),"
          "Velocity.z (m/s),Pressure (Pa),Number Density Ratio\n";
-    bool ok = put(f, h) && write_rows(f, s.n, [&](std::string& o, int i) {
+    bool ok = put(f, h) && write_rows(f, s.n, 96, [&](std::string& o, int i) {
         if (s.type[i] == -1) return;
         put_int(o, i);
         o += ',';
@@ -160,52 +167,52 @@ int write_vtu(const mps_snapshot& s, const char* path, double time) {
     put_int(h, n);
     h += "'>\n<Points>\n<DataArray NumberOfComponents='3' type='Float64' Name='position' format='ascii'>\n";
     bool ok = put(f, h);
-    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+    ok = ok && write_rows(f, n, 36, [&](std::string& o, int i) {
         for (int c = 0; c < 3; c++) {
             put_general6(o, s.pos[3 * (size_t)i + c]);
             o += c < 2 ? ' ' : '\n';
         }
     });
     ok = ok && put(f, end_array + "</Points>\n<PointData>\n" + begin_array("1", "Int32", "Type"));
-    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+    ok = ok && write_rows(f, n, 3, [&](std::string& o, int i) {
         put_int(o, s.type[i]);
         o += '\n';
     });
     ok = ok && put(f, end_array + begin_array("3", "Float64", "Velocity"));
-    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+    ok = ok && write_rows(f, n, 28, [&](std::string& o, int i) {
         put_general6(o, s.vel[3 * (size_t)i]);
         o += ' ';
         put_general6(o, s.vel[3 * (size_t)i + 1]);
         o += " 0\n";
     });
     ok = ok && put(f, end_array + begin_array("1", "Float64", "Pressure"));
-    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+    ok = ok && write_rows(f, n, 12, [&](std::string& o, int i) {
         put_general6(o, s.pressure[i]);
         o += '\n';
     });
     ok = ok && put(f, end_array + begin_array("1", "Float64", "Number Density Ratio"));
-    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+    ok = ok && write_rows(f, n, 12, [&](std::string& o, int i) {
         put_general6(o, s.ndr[i]);
         o += '\n';
     });
     ok = ok && put(f, end_array + begin_array("1", "Int32", "Boundary Condition"));
-    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+    ok = ok && write_rows(f, n, 2, [&](std::string& o, int i) {
         put_int(o, s.bc[i]);
         o += '\n';
     });
     ok = ok && put(f, end_array + "</PointData>\n<Cells>\n<DataArray type='Int32' Name='connectivity' "
                                   "format='ascii'>\n");
-    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+    ok = ok && write_rows(f, n, 8, [&](std::string& o, int i) {
         put_int(o, i);
         o += '\n';
     });
     ok = ok && put(f, end_array + "<DataArray type='Int32' Name='offsets' format='ascii'>\n");
-    ok = ok && write_rows(f, n, [&](std::string& o, int i) {
+    ok = ok && write_rows(f, n, 8, [&](std::string& o, int i) {
         put_int(o, (long long)i + 1);
         o += '\n';
     });
     ok = ok && put(f, end_array + "<DataArray type='UInt8' Name='types' format='ascii'>\n");
-    ok = ok && write_rows(f, n, [&](std::string& o, int) { o += "1\n"; });
+    ok = ok && write_rows(f, n, 2, [&](std::string& o, int) { o += "1\n"; });
     ok = ok && put(f, end_array + "</Cells>\n</Piece>\n</UnstructuredGrid>\n</VTKFile>\n");
     ok = (std::fclose(f) == 0) && ok;
     return ok ? MPS_OK : err(MPS_ERR_ARG, std::string("write failed: ") + path);
@@ -281,13 +288,17 @@ extern "C" {
 int mps_write_snapshot(const mps_snapshot* s, const char* csv_path, const char* vtu_path, double time) {
     if (!s || s->n < 0 || (s->n > 0 && (!s->pos || !s->vel || !s->pressure || !s->ndr || !s->type || !s->bc)))
         return err(MPS_ERR_ARG, "mps_write_snapshot: incomplete snapshot");
-    if (csv_path) {
-        const int rc = write_csv(*s, csv_path, time);
-        if (rc) return rc;
-    }
-    if (vtu_path) {
-        const int rc = write_vtu(*s, vtu_path, time);
-        if (rc) return rc;
+    try {  // no C++ exception crosses the C ABI
+        if (csv_path) {
+            const int rc = write_csv(*s, csv_path, time);
+            if (rc) return rc;
+        }
+        if (vtu_path) {
+            const int rc = write_vtu(*s, vtu_path, time);
+            if (rc) return rc;
+        }
+    } catch (const std::exception& ex) {
+        return err(MPS_ERR_ARG, std::string("mps_write_snapshot: ") + ex.what());
     }
     return MPS_OK;
 }
@@ -349,9 +360,21 @@ int mps_export_write(mps_engine* e, const char* csv_path, const char* vtu_path, 
     return mps_write_snapshot(&s, csv_path, vtu_path, time);
 }
 
+static int read_csv_impl(const char* path, int32_t capacity, int32_t* n, double* time, double* pos,
+                         double* vel, int32_t* type);
+
 int mps_read_csv(const char* path, int32_t capacity, int32_t* n, double* time, double* pos,
                  double* vel, int32_t* type) {
     if (!path || !n) return err(MPS_ERR_ARG, "mps_read_csv: null argument");
+    try {  // no C++ exception crosses the C ABI
+        return read_csv_impl(path, capacity, n, time, pos, vel, type);
+    } catch (const std::exception& ex) {
+        return err(MPS_ERR_ARG, std::string("mps_read_csv: ") + ex.what());
+    }
+}
+
+static int read_csv_impl(const char* path, int32_t capacity, int32_t* n, double* time, double* pos,
+                         double* vel, int32_t* type) {
     CsvFile c;
     if (!read_all(path, c.text))
         return err(MPS_ERR_ARG, std::string("Input file does not exist in the specified path: ") + path);
@@ -410,8 +433,13 @@ int mps_read_csv(const char* path, int32_t capacity, int32_t* n, double* time, d
         }
     };
     std::vector<std::thread> th;
-    for (int t = 1; t < T; t++) th.emplace_back(work, t);
+    int started = 1;
+    try {
+        for (int t = 1; t < T; t++, started++) th.emplace_back(work, t);
+    } catch (const std::system_error&) {
+    }
     work(0);
+    for (int t = started; t < T; t++) work(t);
     for (auto& x : th) x.join();
     for (int t = 0; t < T; t++)
         if (bad[t] >= 0)
