@@ -32,7 +32,14 @@ enum {
     MPS_ERR_CAPACITY = 3,    /* a capacity was exceeded: neighbour list, or mps_read_csv arrays */
     MPS_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up (kernel returned early) */
     MPS_ERR_NO_DEVICE = 5,   /* no CUDA device, or not an sm_103 part */
-    MPS_ERR_NONFINITE = 6    /* a particle position became NaN/inf; it was made a ghost */
+    MPS_ERR_NONFINITE = 6,   /* a particle position became NaN/inf; it was made a ghost */
+    MPS_ERR_NOT_CONVERGED = 7, /* the pressure solve reached its iteration cap before its
+                                  tolerance; the step completed with that pressure, as the
+                                  reference's does (its solver.info() check, src/mps.cpp:462-464,
+                                  only logs): a warning, not a failure of the engine */
+    MPS_ERR_ASYMMETRIC = 8   /* the assembled PPE matrix is not symmetric: the step skipped the
+                                solve (the reference exits, src/mps.cpp:418-442); the message
+                                names the first pair as the reference prints it */
 };
 
 enum { MPS_PRECISION_FP64 = 0, MPS_PRECISION_MIXED = 1 };
@@ -138,8 +145,23 @@ int mps_set_graphs(mps_engine* e, int32_t enabled);
 /* MPS::stepForward (src/mps.cpp:111-130). */
 int mps_step(mps_engine* e, int32_t is_time_to_export, mps_step_stats* stats);
 
-/* n_steps consecutive non-export steps; stats of the last step. */
+/* n_steps consecutive non-export steps; stats of the last step.  Stops at
+ * the first step that returns a status other than MPS_OK. */
 int mps_run(mps_engine* e, int32_t n_steps, mps_step_stats* stats);
+
+/* The symmetry test of solvePoissonEquation (src/mps.cpp:418-442) on a host
+ * CSR matrix (n rows, row_ptr n+1, col/val row_ptr[n]; columns need not be
+ * sorted), run by the same device kernels every step runs on the engine's
+ * own matrix: MPS_OK, or MPS_ERR_ASYMMETRIC with the reference's first pair
+ * i < j (row-major) whose entries differ by more than 1e-10, else the first
+ * pair that differs at all, in *pair_i, *pair_j (-1 when symmetric) and the
+ * reference's message in mps_last_error().  The engine's matrices are
+ * bitwise symmetric by construction, so the engine treats any difference as
+ * an error (the reference tolerates differences up to 1e-10).  The CSR is
+ * checked on the host (MPS_ERR_ARG for bad row_ptr or column indices)
+ * before it is copied to the device. */
+int mps_check_symmetry(int32_t n, const int64_t* row_ptr, const int32_t* col, const double* val,
+                       int32_t* pair_i, int32_t* pair_j);
 
 /* Asynchronous export (the reference's Simulation::exportParticles,
  * src/simulation.cpp:231-245, and Exporter, src/exporter.cpp:10-167).
@@ -253,10 +275,12 @@ int mps_trajectory_backward(mps_trajectory* t, const double* d_sensor_pressure,
  * ints) and d_ndr (n doubles, output) are device pointers the caller owns,
  * and the scratch is a fixed ~5 MB static device array inside this library
  * (held on every GPU that loads it until the process exits).  Limits: at most
- * 65,536 particles and 262,144 bucket cells; larger requests return
- * MPS_ERR_ARG.  The first call on a device looks up the scratch address
- * (make it before any stream capture).  Calls share the scratch, so calls
- * whose GPU work overlaps race: issue them on one stream.  Work is enqueued
+ * 65,536 particles and 262,144 bucket cells; larger requests and a
+ * non-finite or inverted domain return MPS_ERR_ARG.  The first call on a
+ * device looks up the scratch address (make it before any stream capture)
+ * and keeps it for the process; it is not valid after cudaDeviceReset.
+ * Calls share the scratch, so calls whose GPU work overlaps race: issue
+ * them on one stream.  Work is enqueued
  * on `stream` (a cudaStream_t; NULL = the legacy default stream) and the
  * call returns without waiting. */
 int mps_number_density_static(const mps_params* prm, int32_t n, const double* d_pos,

@@ -16,21 +16,7 @@
 
 using namespace mpsg;
 
-namespace {
-
-thread_local std::string g_last_error;
-
-int fail(int code, const std::string& msg) {
-    g_last_error = msg;
-    return code;
-}
-
-#define CU(call)                                                                          \
-    do {                                                                                  \
-        cudaError_t err_ = (call);                                                        \
-        if (err_ != cudaSuccess)                                                          \
-            return fail(MPS_ERR_CUDA, std::string(#call " failed: ") + cudaGetErrorString(err_)); \
-    } while (0)
+namespace mpsg {
 
 // RefValues::RefValues, src/mps.cpp:132-163 (host, same operation order).
 void ref_values(int dim, double l0, double re, double* n0o, double* lamo) {
@@ -48,7 +34,7 @@ void ref_values(int dim, double l0, double re, double* n0o, double* lamo) {
             }
     lam /= n0;
     *n0o = n0;
-    *lamo = lam;
+    if (lamo) *lamo = lam;
 }
 
 // Smallest t with sqrt_rn(t) >= re, so that sqrt_rn(d2) < re <=> d2 < t.
@@ -59,6 +45,52 @@ double sq_threshold(double re) {
     while (std::sqrt(t) < re) t = std::nextafter(t, std::numeric_limits<double>::infinity());
     return t;
 }
+
+// Bucket::Bucket's grid (src/bucket.cpp:10-22): int(extent / len) + 3 cells
+// per axis.  The reference trusts its settings; here the domain must be
+// finite with max >= min on every axis and each axis at most 2^30 cells, so
+// that every axis has at least the 3 cells the clamped cell coordinate
+// [1, cells - 2] and the 3x3(x3) sweep need.
+bool bucket_grid(const mps_params& P, double len, int32_t dims[3], std::string* why) {
+    static const char* ax = "xyz";
+    if (!(len > 0.0) || !std::isfinite(len)) {
+        if (why) *why = "bucket length (the largest effective radius) must be finite and positive";
+        return false;
+    }
+    for (int d = 0; d < 3; d++) {
+        const double lo = P.domain_min[d], hi = P.domain_max[d];
+        if (!std::isfinite(lo) || !std::isfinite(hi) || !(hi >= lo)) {
+            if (why)
+                *why = std::string("domain ") + ax[d] + " range must be finite with max >= min";
+            return false;
+        }
+        const double q = (hi - lo) / len;
+        if (!(q < 1073741824.0)) {
+            if (why) *why = std::string("domain ") + ax[d] + " extent is too many bucket cells";
+            return false;
+        }
+        dims[d] = (int32_t)q + 3;
+    }
+    return true;
+}
+
+}  // namespace mpsg
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CU(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t err_ = (call);                                                        \
+        if (err_ != cudaSuccess)                                                          \
+            return fail(MPS_ERR_CUDA, std::string(#call " failed: ") + cudaGetErrorString(err_)); \
+    } while (0)
 
 int lattice_count(int dim, double ratio) {
     int r = (int)std::ceil(ratio) + 1, cnt = 0;
@@ -167,6 +199,11 @@ int check_status(mps_engine* e) {
         return fail(MPS_ERR_CAPACITY, "neighbour or collision list capacity exceeded (max neighbours " +
                                           std::to_string(e->hs->max_neighbors) + ", capacity " +
                                           std::to_string(e->c.K) + ")");
+    if (s & ST_ASYMMETRIC) return fail(MPS_ERR_ASYMMETRIC, symmetry_message(e));
+    if (s & ST_NOT_CONVERGED)
+        return fail(MPS_ERR_NOT_CONVERGED,
+                    "the pressure solve stopped at its iteration cap with relative residual " +
+                        std::to_string(e->hs->cg_rel_residual) + " (the step completed with that pressure)");
     return MPS_OK;
 }
 
@@ -202,6 +239,8 @@ void enqueue_pre_solve(mps_engine* e) {
     launch_bc_source(c, e->S(), e->nb, e->A, e->ds, st);
     launch_assemble(c, e->S(), e->nb, e->A, e->ds, st);
     launch_dirichlet(c, e->S(), e->nb, e->A, e->parent, e->has_surface, e->ds, st);
+    // solvePoissonEquation's symmetry test (src/mps.cpp:418-442)
+    launch_symmetry_check(c, e->S(), e->A, e->ds, st);
 }
 
 // Mixed solver only: FP32 operator and multigrid hierarchy of this step.
@@ -417,6 +456,12 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     for (int32_t i = 0; i < n; i++)
         if (type[i] < -1 || type[i] > 2)
             return fail(MPS_ERR_ARG, "mps_create: particle type outside {-1,0,1,2}");
+    int32_t grid[3];
+    {
+        std::string why;
+        const double len = std::max({P.re_pressure, P.re_viscosity, P.re_surface});
+        if (!bucket_grid(P, len, grid, &why)) return fail(MPS_ERR_ARG, "mps_create: " + why);
+    }
     int dev = 0, ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(MPS_ERR_NO_DEVICE, "no CUDA device");
@@ -455,9 +500,9 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     c.cd = P.collision_distance;
     c.len = c.re_max;
     // Bucket::Bucket, src/bucket.cpp:10-22
-    c.numX = (int)((P.domain_max[0] - P.domain_min[0]) / c.len) + 3;
-    c.numY = (int)((P.domain_max[1] - P.domain_min[1]) / c.len) + 3;
-    c.numZ = (int)((P.domain_max[2] - P.domain_min[2]) / c.len) + 3;
+    c.numX = grid[0];
+    c.numY = grid[1];
+    c.numZ = grid[2];
     bool planar = P.gravity[2] == 0.0;
     for (int32_t i = 0; i < n && planar; i++)
         planar = pos[3 * i + 2] == pos[2] && vel[3 * i + 2] == 0.0;

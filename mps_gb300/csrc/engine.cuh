@@ -22,9 +22,11 @@ enum : int8_t { BC_IGNORED = 0, BC_SURFACE = 1, BC_INNER = 2 };
 
 // Status bits raised on the device, reported through mps_step_stats.status.
 enum : int32_t {
-    ST_CAPACITY = 1,  // neighbour list overflow
-    ST_TIMEOUT = 2,   // a bounded wait gave up
-    ST_NONFINITE = 4, // a particle position became NaN or infinite
+    ST_CAPACITY = 1,       // neighbour list overflow
+    ST_TIMEOUT = 2,        // a bounded wait gave up
+    ST_NONFINITE = 4,      // a particle position became NaN or infinite
+    ST_NOT_CONVERGED = 8,  // the pressure solve stopped at its iteration cap
+    ST_ASYMMETRIC = 16,    // the assembled PPE matrix is not symmetric (solve skipped)
 };
 
 // Constants of one scene, computed on the host with the reference's
@@ -89,6 +91,14 @@ struct DevStats {
     unsigned long long nnz_off;
     int32_t upload_flag;  // host copy of mps_upload's device checks
     int32_t pad2;
+    // symmetry check of the assembled matrix (symcheck.cu): the sum over
+    // stored off-diagonal entries of +-hash(pair) * bits(value) mod 2^64 (0 for
+    // a bitwise symmetric matrix), and, only when it is not 0, the first
+    // asymmetric pair in id order stored as ~(i << 32 | j) (0: none), once for
+    // pairs whose values differ by more than 1e-10 and once for any difference
+    unsigned long long sym_fp;
+    unsigned long long asym_big;
+    unsigned long long asym_any;
 };
 
 struct CollPair {
@@ -170,6 +180,12 @@ void launch_assemble(const Consts& c, const StateBuf& s, const NbList& nb, const
                      DevStats* ds, cudaStream_t st);
 void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
                       int32_t* parent, int8_t* has_surface, DevStats* ds, cudaStream_t st);
+// --------------------------------------------------------------- symcheck.cu
+// The symmetry test of solvePoissonEquation (src/mps.cpp:418-442) on the
+// assembled matrix: a one-pass fingerprint, and the first asymmetric pair
+// when it is not zero; raises ST_ASYMMETRIC, which makes the solvers skip.
+void launch_symmetry_check(const Consts& c, const StateBuf& s, const Ppe& A, DevStats* ds,
+                           cudaStream_t st);
 void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb,
                           const double* x, double* ax, double* ay, double* az, int mixed,
                           DevStats* ds, cudaStream_t st);

@@ -114,6 +114,15 @@ namespace mpsg {
 
 // mps_last_error() message of this thread.
 MPSG_HIDDEN void set_last_error(const std::string& m);
+// RefValues::RefValues (src/mps.cpp:132-163): n0 and lambda (lam may be NULL)
+// of the 9x9(x9) lattice for radius re, in the reference's operation order.
+MPSG_HIDDEN void ref_values(int dim, double l0, double re, double* n0, double* lam);
+// Smallest t with sqrt_rn(t) >= re (0 for re <= 0): sqrt_rn(d2) < re <=> d2 < t.
+MPSG_HIDDEN double sq_threshold(double re);
+// Bucket::Bucket's cells per axis (src/bucket.cpp:10-22) for bucket length
+// len; false (with the reason) unless the domain is finite with max >= min and
+// fits, so that every axis has at least 3 cells.
+MPSG_HIDDEN bool bucket_grid(const mps_params& P, double len, int32_t dims[3], std::string* why);
 // One MPS::stepForward on the engine's stream, waits for it, fills stats and
 // returns the step's status (graph replay unless exporting or taping).
 MPSG_HIDDEN int engine_step(mps_engine* e, bool do_export, mps_step_stats* stats);
@@ -130,5 +139,8 @@ MPSG_HIDDEN Mg engine_active_mg(const mps_engine* e);
 MPSG_HIDDEN int engine_collect(mps_engine* e, mps_step_stats* stats);
 // Records a phase of the running step into e->tape (adjoint.cu).
 MPSG_HIDDEN void tape_phase(mps_engine* e, TapePhase ph);
+// The reference's message for the first asymmetric pair of the last step's
+// matrix (symcheck.cu; after a step that raised ST_ASYMMETRIC).
+MPSG_HIDDEN std::string symmetry_message(const mps_engine* e);
 
 }  // namespace mpsg

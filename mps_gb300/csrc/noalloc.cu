@@ -13,13 +13,17 @@
 //
 // Limits and behaviour:
 //  * at most kMaxParticles particles and kMaxCells bucket cells
-//    (numX * numY * numZ of the reference's Bucket); larger requests return
+//    (numX * numY * numZ of the reference's Bucket); larger requests, and a
+//    non-finite or inverted domain (max < min on an axis), return
 //    MPS_ERR_ARG without touching the GPU;
 //  * the scratch array is resident on every GPU that loads the library, for
 //    the life of the process (about 5 MB);
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make
-//    that first call before any stream capture;
+//    cudaGetSymbolAddress (with that device current) and caches it for the
+//    life of the process; make that first call before any stream capture.
+//    The cached address belongs to the device's primary context: after
+//    cudaDeviceReset (or anything else that destroys that context) it is
+//    stale, so this entry point must not be called again in that process;
 //  * every call reuses the same scratch and keeps nothing between calls (the
 //    cell counters are cleared on each call); calls whose work overlaps on
 //    the GPU race on the scratch, so issue them on one stream or order them;
@@ -38,13 +42,9 @@
 #include "../../include/mps_gb300.h"
 #include "devutil.cuh"
 #include "engine.cuh"
+#include "engine_impl.cuh"
 
 using namespace mpsg;
-
-namespace mpsg {
-// the message mps_last_error() returns (capi.cu)
-__attribute__((visibility("hidden"))) void set_last_error(const std::string& m);
-}  // namespace mpsg
 
 namespace {
 
@@ -76,29 +76,6 @@ unsigned char* g_scratch_ptr[kMaxDevices] = {};
 int na_fail(int code, const std::string& m) {
     set_last_error(m);
     return code;
-}
-
-// RefValues::RefValues (src/mps.cpp:132-163), host, same operation order.
-void na_ref_values(int dim, double l0, double re, double* n0o) {
-    double n0 = 0.0;
-    int zb = dim == 2 ? 0 : -4, ze = dim == 2 ? 1 : 5;
-    for (int ix = -4; ix < 5; ix++)
-        for (int iy = -4; iy < 5; iy++)
-            for (int iz = zb; iz < ze; iz++) {
-                if (ix == 0 && iy == 0 && iz == 0) continue;
-                double x = l0 * (double)ix, y = l0 * (double)iy, z = l0 * (double)iz;
-                double dist = std::sqrt((x * x + y * y) + z * z);
-                n0 += dist < re ? (re / dist) - 1.0 : 0.0;
-            }
-    *n0o = n0;
-}
-
-// Smallest t with sqrt_rn(t) >= re.
-double na_threshold(double re) {
-    double t = re * re;
-    while (t > 0.0 && std::sqrt(t) >= re) t = std::nextafter(t, 0.0);
-    while (std::sqrt(t) < re) t = std::nextafter(t, std::numeric_limits<double>::infinity());
-    return t;
 }
 
 struct NaView {
@@ -198,18 +175,26 @@ extern "C" int mps_number_density_static(const mps_params* prm, int32_t n, const
     c.re_p = P.re_pressure;
     c.re_max = std::max({P.re_pressure, P.re_viscosity, P.re_surface});  // src/settings.cpp:138
     c.len = c.re_max;
-    c.numX = (int)((P.domain_max[0] - P.domain_min[0]) / c.len) + 3;  // src/bucket.cpp:14-16
-    c.numY = (int)((P.domain_max[1] - P.domain_min[1]) / c.len) + 3;
-    c.numZ = (int)((P.domain_max[2] - P.domain_min[2]) / c.len) + 3;
+    {
+        // src/bucket.cpp:14-16; a non-finite or inverted domain is refused
+        // here, before the GPU is touched (every axis then has >= 3 cells)
+        int32_t dims[3];
+        std::string why;
+        if (!bucket_grid(P, c.len, dims, &why))
+            return na_fail(MPS_ERR_ARG, "mps_number_density_static: " + why);
+        c.numX = dims[0];
+        c.numY = dims[1];
+        c.numZ = dims[2];
+    }
     const double nk = (double)c.numX * c.numY * c.numZ;
     if (!(nk <= (double)kMaxCells))
         return na_fail(MPS_ERR_ARG, "mps_number_density_static: the bucket grid has " +
                                         std::to_string((long long)nk) + " cells, above the static scratch limit of " +
                                         std::to_string(kMaxCells));
     c.nkeys = (int32_t)nk;
-    c.t_p = na_threshold(c.re_p);
-    c.t_max = na_threshold(c.re_max);
-    na_ref_values(P.dim, P.particle_distance, c.re_p, &c.n0_p);
+    c.t_p = sq_threshold(c.re_p);
+    c.t_max = sq_threshold(c.re_max);
+    ref_values(P.dim, P.particle_distance, c.re_p, &c.n0_p, nullptr);
 
     int dev = 0;
     cudaError_t ce = cudaGetDevice(&dev);

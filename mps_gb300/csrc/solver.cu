@@ -354,7 +354,20 @@ __device__ __forceinline__ void off_rows(const Ppe& A, const MatFree& mf, int K,
 }
 
 // ----------------------------------------------------------------- FP64 CG
+// A step whose matrix failed the symmetry test skips its solve (the
+// reference exits there); every block reads the flag, set before the launch.
+__device__ __forceinline__ bool solve_skipped(DevStats* ds) {
+    if (!(*(volatile int32_t*)&ds->status & ST_ASYMMETRIC)) return false;
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        ds->cg_iterations = 0;
+        ds->refinements = 0;
+        ds->cg_rel_residual = -1.0;
+    }
+    return true;
+}
+
 __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs a, DevStats* ds) {
+    if (solve_skipped(ds)) return;
     GridBar gb = whole_grid(kv);
     const int lane = threadIdx.x & 31;
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -375,6 +388,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs 
     const double rhs2 = tot[0];
     int64_t it = 0;
     double rn2 = rhs2;
+    bool conv = true;
     if (rhs2 > 0.0) {
         const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
         if (!(rn2 < thr)) {
@@ -427,6 +441,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs 
                 if (!grid_sync(gb, ds)) return;
             }
         }
+        conv = rn2 < thr;
     } else {
         rn2 = 0.0;
     }
@@ -434,6 +449,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs 
         ds->cg_iterations = it;
         ds->refinements = 0;
         ds->cg_rel_residual = rhs2 > 0.0 ? sqrt(rn2 / rhs2) : 0.0;
+        if (!conv) atomicOr(&ds->status, ST_NOT_CONVERGED);
     }
 }
 
@@ -876,6 +892,14 @@ template <int BS>
 __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg& mg,
                                             const Krylov& kv, const SolveArgs& a, DevStats* ds,
                                             GridBar& gb) {
+    if (*(volatile int32_t*)&ds->status & ST_ASYMMETRIC) {  // the reference exits here
+        if (gb.rank == 0 && threadIdx.x == 0) {
+            ds->cg_iterations = 0;
+            ds->refinements = 0;
+            ds->cg_rel_residual = -1.0;
+        }
+        return;
+    }
     const int gtid = gb.rank * BS + threadIdx.x;
     const int gsz = gb.size * BS;
     const int lane = threadIdx.x & 31;
@@ -1030,6 +1054,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
         ds->cg_iterations = inner_total;
         ds->refinements = refine;
         ds->cg_rel_residual = rhs2 > 0.0 ? sqrt(rn2 / rhs2) : 0.0;
+        if (rhs2 > 0.0 && !(rn2 < thr)) atomicOr(&ds->status, ST_NOT_CONVERGED);
     }
 }
 

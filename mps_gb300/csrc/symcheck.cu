@@ -1,0 +1,272 @@
+// Symmetry test of the PPE matrix, the check solvePoissonEquation runs
+// before every solve (src/mps.cpp:418-442): Eigen's isApprox(A, A^T), and if
+// that fails, the first pair i < j (row-major, id order) with
+// |A(i,j) - A(j,i)| > 1e-10, which the reference prints before exit(1).
+//
+// The engine assembles a_ij and a_ji from the same FP64 distance, weight and
+// density (src/mps.cpp:343), so its matrices are bitwise symmetric; the test
+// is kept to catch what should never happen, at the cost of one pass over
+// the stored entries:
+//  * fingerprint: F = sum over stored off-diagonal entries (i, j) of
+//    sgn(j - i) * H(min, max) * bits(a_ij) mod 2^64, with H an odd 64-bit hash
+//    of the unordered pair and bits() the value's IEEE pattern (zeros
+//    canonical).  Integer sums are exact and order-free: F = 0 for a bitwise
+//    symmetric matrix, and F != 0 for any other with probability 1 - 2^-64;
+//  * only when F != 0: every stored entry looks up its transpose (absent =
+//    0) and the first asymmetric pair in id order is recorded, separately for
+//    pairs that differ by more than 1e-10 (the reference's exit condition)
+//    and for any difference.
+// The step then skips the solve and returns MPS_ERR_ASYMMETRIC (the
+// reference exits).  This is stricter than the reference, which continues
+// when isApprox holds (relative Frobenius difference <= 1e-12) or no pair
+// differs by more than 1e-10; a difference that small cannot come from this
+// engine's assembly either.
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "devutil.cuh"
+#include "engine.cuh"
+#include "engine_impl.cuh"
+
+namespace mpsg {
+
+namespace {
+
+constexpr int kSymThreads = 256;
+
+__host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    // SplitMix64 finaliser (Steele, Lea and Flood, 2014)
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ unsigned long long entry_term(int ri, int ci, double v) {
+    const unsigned lo = (unsigned)min(ri, ci), hi = (unsigned)max(ri, ci);
+    const unsigned long long h = mix64(((unsigned long long)lo << 32) | hi) | 1ull;
+    const unsigned long long b = v == 0.0 ? 0ull : (unsigned long long)__double_as_longlong(v);
+    const unsigned long long t = h * b;
+    return ri < ci ? t : 0ull - t;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Rows of the engine's SELL-32 matrix (rows and columns are slots; ids map
+// them to particle ids), and of a plain CSR matrix (ids = rows).
+struct SellRows {
+    const int32_t* offcnt;
+    const int32_t* col;
+    const double* val;
+    const int32_t* id;
+    int K, n;
+    __device__ int len(int r) const { return offcnt[r]; }
+    __device__ size_t at(int r, int m) const { return ((size_t)(r >> 5) * K + m) * 32 + (r & 31); }
+    __device__ int col_of(int r, int m) const { return col[at(r, m)]; }
+    __device__ double val_of(int r, int m) const { return val[at(r, m)]; }
+    __device__ int rid(int r) const { return id[r]; }
+};
+struct CsrRows {
+    const int64_t* rp;
+    const int32_t* col;
+    const double* val;
+    int n;
+    __device__ int len(int r) const { return (int)(rp[r + 1] - rp[r]); }
+    __device__ int col_of(int r, int m) const { return col[rp[r] + m]; }
+    __device__ double val_of(int r, int m) const { return val[rp[r] + m]; }
+    __device__ int rid(int r) const { return r; }
+};
+
+template <class R>
+__global__ void __launch_bounds__(kSymThreads) k_sym_fingerprint(R rows, unsigned long long* fp) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long acc = 0;
+    if (r < rows.n) {
+        const int m = rows.len(r), ri = rows.rid(r);
+        for (int q = 0; q < m; q++) {
+            const int c = rows.col_of(r, q);
+            const int ci = rows.rid(c);
+            if (ci != ri) acc += entry_term(ri, ci, rows.val_of(r, q));
+        }
+    }
+    acc = warp_sum64(acc);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(fp, acc);
+}
+
+// Runs only when the fingerprint is not 0 (the kernel is always launched so
+// that a captured step needs no host decision).
+template <class R>
+__global__ void __launch_bounds__(kSymThreads) k_sym_locate(R rows, const unsigned long long* fp,
+                                                            unsigned long long* big,
+                                                            unsigned long long* any, int32_t* status) {
+    if (*fp == 0ull) return;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) atomicOr(status, ST_ASYMMETRIC);
+    if (r >= rows.n) return;
+    const int m = rows.len(r), ri = rows.rid(r);
+    for (int q = 0; q < m; q++) {
+        const int c = rows.col_of(r, q);
+        const int ci = rows.rid(c);
+        if (ci == ri) continue;
+        const double v = rows.val_of(r, q);
+        double t = 0.0;  // the transpose entry, 0 where it is not stored
+        const int mc = rows.len(c);
+        for (int u = 0; u < mc; u++)
+            if (rows.col_of(c, u) == r) {
+                t = rows.val_of(c, u);
+                break;
+            }
+        const bool differ = !(v == t);
+        if (!differ) continue;
+        const unsigned lo = (unsigned)min(ri, ci), hi = (unsigned)max(ri, ci);
+        const unsigned long long key = ~(((unsigned long long)lo << 32) | hi);
+        atomicMax(any, key);
+        if (fabs(v - t) > 1e-10) atomicMax(big, key);
+    }
+}
+
+// Values A(i, j), A(j, i) of one pair (ids), for the error message.
+template <class R>
+__global__ void k_sym_values(R rows, int i, int j, double* out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows.n) return;
+    const int ri = rows.rid(r);
+    if (ri != i && ri != j) return;
+    const int other = ri == i ? j : i;
+    const int m = rows.len(r);
+    for (int q = 0; q < m; q++)
+        if (rows.rid(rows.col_of(r, q)) == other) out[ri == i ? 0 : 1] = rows.val_of(r, q);
+}
+
+int grid_for(int n) { return (n + kSymThreads - 1) / kSymThreads; }
+
+}  // namespace
+
+void launch_symmetry_check(const Consts& c, const StateBuf& s, const Ppe& A, DevStats* ds,
+                           cudaStream_t st) {
+    SellRows rows{A.offcnt, A.col, A.val, s.id, c.K, c.n};
+    k_sym_fingerprint<<<grid_for(c.n), kSymThreads, 0, st>>>(rows, &ds->sym_fp);
+    k_sym_locate<<<grid_for(c.n), kSymThreads, 0, st>>>(rows, &ds->sym_fp, &ds->asym_big, &ds->asym_any,
+                                                        &ds->status);
+    g_launches += 2;
+}
+
+// The message of a failed check: the reference's text for the first pair
+// (src/mps.cpp:425-431), from the keys the locate pass left in DevStats.
+std::string symmetry_message(const mps_engine* e) {
+    const unsigned long long key = e->hs->asym_big ? ~e->hs->asym_big : ~e->hs->asym_any;
+    const int i = (int)(key >> 32), j = (int)(key & 0xffffffffu);
+    double* dv = nullptr;
+    double hv[2] = {0.0, 0.0};
+    SellRows rows{e->A.offcnt, e->A.col, e->A.val, e->buf[e->cur].id, e->c.K, e->c.n};
+    if (cudaMalloc(&dv, 2 * sizeof(double)) == cudaSuccess) {
+        cudaMemsetAsync(dv, 0, 2 * sizeof(double), e->st);
+        k_sym_values<<<grid_for(e->c.n), kSymThreads, 0, e->st>>>(rows, i, j, dv);
+        cudaMemcpyAsync(hv, dv, sizeof hv, cudaMemcpyDeviceToHost, e->st);
+        cudaStreamSynchronize(e->st);
+        cudaFree(dv);
+    }
+    cudaGetLastError();
+    return "Matrix is not symmetric at (" + std::to_string(i) + ", " + std::to_string(j) + "): A(" +
+           std::to_string(i) + ", " + std::to_string(j) + ") = " + std::to_string(hv[0]) + ", A(" +
+           std::to_string(j) + ", " + std::to_string(i) + ") = " + std::to_string(hv[1]) +
+           (e->hs->asym_big ? "" : " (all differences <= 1e-10)");
+}
+
+}  // namespace mpsg
+
+using namespace mpsg;
+
+extern "C" int mps_check_symmetry(int32_t n, const int64_t* row_ptr, const int32_t* col,
+                                  const double* val, int32_t* pair_i, int32_t* pair_j) {
+    if (n <= 0 || !row_ptr || !col || !val) {
+        set_last_error("mps_check_symmetry: null pointer or n <= 0");
+        return MPS_ERR_ARG;
+    }
+    // the host CSR is validated before anything reaches the device
+    if (row_ptr[0] != 0) {
+        set_last_error("mps_check_symmetry: row_ptr[0] must be 0");
+        return MPS_ERR_ARG;
+    }
+    for (int32_t r = 0; r < n; r++)
+        if (row_ptr[r + 1] < row_ptr[r] || row_ptr[r + 1] - row_ptr[r] > (int64_t)1 << 30) {
+            set_last_error("mps_check_symmetry: row_ptr must be non-decreasing");
+            return MPS_ERR_ARG;
+        }
+    const int64_t nnz = row_ptr[n];
+    if (nnz > ((int64_t)1 << 31) - 1) {
+        set_last_error("mps_check_symmetry: more than 2^31 - 1 entries");
+        return MPS_ERR_ARG;
+    }
+    for (int64_t q = 0; q < nnz; q++)
+        if (col[q] < 0 || col[q] >= n) {
+            set_last_error("mps_check_symmetry: column index out of range");
+            return MPS_ERR_ARG;
+        }
+    int64_t* drp = nullptr;
+    int32_t* dcol = nullptr;
+    double* dval = nullptr;
+    unsigned long long* dw = nullptr;  // fp, big, any
+    int32_t* dstat = nullptr;
+    double* dv = nullptr;
+    int rc = MPS_OK;
+    unsigned long long hw[3] = {0, 0, 0};
+    double hv[2] = {0.0, 0.0};
+    auto cuda_fail = [&](cudaError_t ce) {
+        set_last_error(std::string("mps_check_symmetry: ") + cudaGetErrorString(ce));
+        return MPS_ERR_CUDA;
+    };
+    cudaError_t ce = cudaSuccess;
+    if ((ce = cudaMalloc(&drp, sizeof(int64_t) * (n + 1))) != cudaSuccess ||
+        (ce = cudaMalloc(&dcol, sizeof(int32_t) * std::max<int64_t>(nnz, 1))) != cudaSuccess ||
+        (ce = cudaMalloc(&dval, sizeof(double) * std::max<int64_t>(nnz, 1))) != cudaSuccess ||
+        (ce = cudaMalloc(&dw, sizeof hw)) != cudaSuccess || (ce = cudaMalloc(&dstat, sizeof(int32_t))) != cudaSuccess ||
+        (ce = cudaMalloc(&dv, sizeof hv)) != cudaSuccess) {
+        rc = cuda_fail(ce);
+    } else {
+        cudaMemcpy(drp, row_ptr, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice);
+        if (nnz) {
+            cudaMemcpy(dcol, col, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice);
+            cudaMemcpy(dval, val, sizeof(double) * nnz, cudaMemcpyHostToDevice);
+        }
+        cudaMemset(dw, 0, sizeof hw);
+        cudaMemset(dstat, 0, sizeof(int32_t));
+        cudaMemset(dv, 0, sizeof hv);
+        CsrRows rows{drp, dcol, dval, n};
+        k_sym_fingerprint<<<grid_for(n), kSymThreads>>>(rows, dw);
+        k_sym_locate<<<grid_for(n), kSymThreads>>>(rows, dw, dw + 1, dw + 2, dstat);
+        if ((ce = cudaMemcpy(hw, dw, sizeof hw, cudaMemcpyDeviceToHost)) != cudaSuccess) {
+            rc = cuda_fail(ce);
+        } else if (hw[0] != 0ull) {
+            const unsigned long long key = hw[1] ? ~hw[1] : ~hw[2];
+            const int i = (int)(key >> 32), j = (int)(key & 0xffffffffu);
+            k_sym_values<<<grid_for(n), kSymThreads>>>(rows, i, j, dv);
+            cudaMemcpy(hv, dv, sizeof hv, cudaMemcpyDeviceToHost);
+            if (pair_i) *pair_i = i;
+            if (pair_j) *pair_j = j;
+            set_last_error("Matrix is not symmetric at (" + std::to_string(i) + ", " + std::to_string(j) +
+                           "): A(" + std::to_string(i) + ", " + std::to_string(j) + ") = " +
+                           std::to_string(hv[0]) + ", A(" + std::to_string(j) + ", " + std::to_string(i) +
+                           ") = " + std::to_string(hv[1]) + (hw[1] ? "" : " (all differences <= 1e-10)"));
+            rc = MPS_ERR_ASYMMETRIC;
+        }
+        if (rc != MPS_ERR_CUDA && (ce = cudaGetLastError()) != cudaSuccess) rc = cuda_fail(ce);
+    }
+    cudaFree(drp);
+    cudaFree(dcol);
+    cudaFree(dval);
+    cudaFree(dw);
+    cudaFree(dstat);
+    cudaFree(dv);
+    if (rc == MPS_OK) {
+        if (pair_i) *pair_i = -1;
+        if (pair_j) *pair_j = -1;
+    }
+    return rc;
+}

@@ -15,7 +15,7 @@ import numpy as np
 from . import build as _build
 
 (MPS_OK, MPS_ERR_ARG, MPS_ERR_CUDA, MPS_ERR_CAPACITY, MPS_ERR_TIMEOUT, MPS_ERR_NO_DEVICE,
- MPS_ERR_NONFINITE) = range(7)
+ MPS_ERR_NONFINITE, MPS_ERR_NOT_CONVERGED, MPS_ERR_ASYMMETRIC) = range(9)
 FP64, MIXED = 0, 1
 
 
@@ -163,6 +163,8 @@ def load(build_if_missing: bool = False):
     L.mps_read_csv.restype = C.c_int
     L.mps_selftest_wait_limit.argtypes = [P(C.c_int32), P(C.c_double)]
     L.mps_selftest_wait_limit.restype = C.c_int
+    L.mps_check_symmetry.argtypes = [C.c_int32, vp, vp, vp, P(C.c_int32), P(C.c_int32)]
+    L.mps_check_symmetry.restype = C.c_int
     L.mps_last_error.restype = C.c_char_p
     for name in ("mps_create", "mps_destroy", "mps_set_solver", "mps_step", "mps_run",
                  "mps_download", "mps_upload", "mps_neighbors", "mps_system", "mps_collisions"):
@@ -215,6 +217,18 @@ def selftest_wait_limit():
     sec = C.c_double(0.0)
     rc = L.mps_selftest_wait_limit(C.byref(g), C.byref(sec))
     return rc, g.value, sec.value
+
+
+def check_symmetry(row_ptr, col, val):
+    """mps_check_symmetry on a CSR matrix: (return code, i, j, message); i, j
+    are the first asymmetric pair (-1, -1 when symmetric)."""
+    L = load()
+    rp = np.ascontiguousarray(row_ptr, np.int64)
+    cl = np.ascontiguousarray(col, np.int32)
+    vl = np.ascontiguousarray(val, np.float64)
+    i, j = C.c_int32(-2), C.c_int32(-2)
+    rc = L.mps_check_symmetry(len(rp) - 1, _p(rp), _p(cl), _p(vl), C.byref(i), C.byref(j))
+    return rc, i.value, j.value, (L.mps_last_error().decode() if rc else "")
 
 
 def make_params(p: dict) -> MpsParams:

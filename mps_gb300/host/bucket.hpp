@@ -1,7 +1,9 @@
 // Bucket of the reference (src/bucket.hpp:8-19): the uniform cell grid of the
 // neighbour search, cell edge re_max with one padding cell on every side.
-// The GPU engine builds its own cell table each step; this host class keeps
-// the reference's interface for callers that inspect the grid.
+// An interface mirror only: neither the engine nor this front end calls it
+// (the GPU builds its own cell table every neighbour search, sort.cu).  It is
+// kept so that host code written against the reference's Bucket still
+// compiles; its storeParticles has no test of its own.
 #pragma once
 #include <vector>
 

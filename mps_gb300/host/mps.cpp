@@ -1,6 +1,8 @@
 #include "mps.hpp"
 
 #include <cmath>
+#include <cstdlib>
+#include <iostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -137,7 +139,15 @@ void MPS::syncParticles() {
 // reference logs one by one are logged here as counts.
 double MPS::stepForward(const bool isTimeToExport) {
     if (!engine) throw std::runtime_error("MPS::stepForward before loadInitialState");
-    check(mps_step(engine.get(), isTimeToExport ? 1 : 0, &stats));
+    const int rc = mps_step(engine.get(), isTimeToExport ? 1 : 0, &stats);
+    if (rc == MPS_ERR_ASYMMETRIC) {  // src/mps.cpp:425-439: print the pair and exit
+        std::cout << mps_last_error() << std::endl;
+        std::exit(1);
+    }
+    if (rc == MPS_ERR_NOT_CONVERGED)  // src/mps.cpp:462-464: the step goes on
+        mpslog::debug(std::string("Pressure calculation failed: ") + mps_last_error());
+    else
+        check(rc);
     if (stats.n_new_ghosts > 0)
         mpslog::debug(std::to_string(stats.n_new_ghosts) + " particle(s) went out of the domain.");
     if (stats.n_unconnected > 0)

@@ -8,7 +8,7 @@ stores what it computed.  The scenes are produced by mps_gb300.scenes, whose
 lattice generator reproduces the reference's own inputs/*/input.csv byte for
 byte (checked below before anything is written).
 
-    python tests/golden/make_golden.py [REF_ROOT]
+    python tests/golden/make_golden.py REF_ROOT
 
 Each fixture holds the initial condition, the settings, and per step either
 the full per-particle arrays or SHA-256 digests of them (for the larger
@@ -190,7 +190,9 @@ def box3d(l0=0.02, nf=5):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: python tests/golden/make_golden.py REF_ROOT (the reference checkout)")
+    ref_root = sys.argv[1]
     src = os.path.join(ref_root, "src")
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF_SRC={src}"],
                    check=True)

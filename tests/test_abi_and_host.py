@@ -238,3 +238,62 @@ def test_csv_reader_matches_python_parser(built, tmp_path):
     bad.write_text("\n".join(lines[:5] + [lines[6]] + lines[6:]) + "\n")
     with pytest.raises(Exception, match="bad row"):
         read_particles_csv(bad)
+
+
+def _no_gpu_or_skip():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: these calls pass unchecked host pointers")
+
+
+@pytest.mark.parametrize("domain", ["inverted_x", "inverted_y_by_one_cell", "nan", "inf"])
+def test_bad_domain_rejected_before_the_gpu(built, domain):
+    """A domain that is not finite or whose max lies below its min on an axis
+    would give the bucket grid fewer than 3 cells on that axis (or undefined
+    integer casts); mps_create and mps_number_density_static refuse it with
+    MPS_ERR_ARG before any device call, so here (no GPU) the code is ARG, not
+    NO_DEVICE."""
+    _no_gpu_or_skip()
+    import ctypes as C
+
+    from mps_gb300 import engine, scenes
+
+    prm, pos, vel, t = scenes.dam_break(0.05, tank=(0.5, 0.4), column=(0.2, 0.2))
+    lo, hi = list(prm["domain_min"]), list(prm["domain_max"])
+    re = max(prm["re_pressure"], prm["re_viscosity"], prm["re_surface"])
+    if domain == "inverted_x":
+        lo[0], hi[0] = hi[0], lo[0]
+    elif domain == "inverted_y_by_one_cell":
+        hi[1] = lo[1] - 1.5 * re
+    elif domain == "nan":
+        lo[0] = float("nan")
+    else:
+        hi[1] = float("inf")
+    bad = dict(prm, domain_min=lo, domain_max=hi)
+    with pytest.raises(engine.MpsError) as ex:
+        engine.Engine(bad, pos, vel, t)
+    assert ex.value.code == engine.MPS_ERR_ARG and "domain" in str(ex.value)
+    lib = engine.load()
+    fn = lib.mps_number_density_static
+    fn.argtypes = [C.POINTER(engine.MpsParams), C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                   C.c_void_p]
+    fn.restype = C.c_int
+    # non-null placeholders: the call must return before it would use them
+    rc = fn(C.byref(engine.make_params(bad)), 10, 16, 16, 16, None)
+    assert rc == engine.MPS_ERR_ARG and b"domain" in lib.mps_last_error()
+
+
+def test_check_symmetry_rejects_bad_csr_on_the_host(built):
+    """mps_check_symmetry validates a host CSR before it copies anything to
+    the device: a decreasing row_ptr or an out-of-range column is MPS_ERR_ARG
+    (so on this GPU-less machine no CUDA error can occur first)."""
+    _no_gpu_or_skip()
+    from mps_gb300 import engine
+
+    rc, *_ = engine.check_symmetry([0, 2, 1], [0, 1], [1.0, 2.0])
+    assert rc == engine.MPS_ERR_ARG
+    rc, *_ = engine.check_symmetry([0, 1, 2], [0, 2], [1.0, 2.0])
+    assert rc == engine.MPS_ERR_ARG
+    rc, *_ = engine.check_symmetry([0, 1, 2], [0, -1], [1.0, 2.0])
+    assert rc == engine.MPS_ERR_ARG

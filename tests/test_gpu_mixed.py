@@ -35,3 +35,53 @@ def test_mixed_matches_fp64(mode):
         assert sb["cg_iterations"] < sa["cg_iterations"] / 4  # the multigrid pays off
     ea.close()
     eb.close()
+
+
+# Mixed trajectory against FP64 and the oracle (the 1M workload's solver on a crop)
+P_TRAJ = 1e-6    # pressure relative L2 (the mixed solve's own error is ~1e-10 per step)
+X_TRAJ = 1e-9    # metres, positions (particles move ~1e-6 m per step here)
+V_TRAJ = 1e-6    # m/s
+
+
+def test_mixed_trajectory_against_fp64_and_oracle():
+    """60 steps of a 20,000-fluid-particle dam break (l0 2e-3 m, dt 2e-4 s:
+    the 1M workload's dt / l0 ratio of 0.1 s/m) with the mixed solver and
+    its default multigrid, side by side with the FP64 engine and the CPU
+    oracle from the same initial state.  Every 10 steps: pressure within
+    P_TRAJ relative L2, positions within X_TRAJ, velocities within V_TRAJ,
+    surface flags, Dirichlet flags and types identical, collision pairs of
+    every step identical."""
+    m = engine_or_skip()
+    from oracle import Oracle
+
+    from mps_gb300 import scenes
+
+    l0 = 2e-3
+    prm, pos, vel, t = scenes.dam_break(l0, tank=(0.6, 0.5), column=(0.2, 0.4), dt=0.1 * l0)
+    assert (t == scenes.FLUID).sum() == 20000 and len(t) <= 50000
+    em = m.Engine(prm, pos, vel, t, precision=m.MIXED)
+    ef = m.Engine(prm, pos, vel, t, precision=m.FP64)
+    o = Oracle(prm, pos, vel, t)
+    o.set_cg(solves=1)
+    worst = {"p_fp64": 0.0, "p_oracle": 0.0, "x": 0.0, "v": 0.0}
+    for s in range(1, 61):
+        sm, sf, so = em.step(), ef.step(), o.step()
+        assert sm["status"] == 0 and sm["cg_relative_residual"] <= 1e-10
+        assert sm["debug_log_count"] == sf["debug_log_count"] == so["debug_log_count"], s
+        mi, mj, _ = em.collisions()
+        oi, oj, _ = o.collisions()
+        assert np.array_equal(mi, oi) and np.array_equal(mj, oj), s
+        if s % 10:
+            continue
+        a, b, c = em.state(), ef.state(), o.state()
+        for k in ("type", "bc", "dirichlet"):
+            assert np.array_equal(a[k], b[k]) and np.array_equal(a[k], c[k]), (s, k)
+        assert np.linalg.norm(c["pressure"]) > 0
+        worst["p_fp64"] = max(worst["p_fp64"], rel_l2(a["pressure"], b["pressure"]))
+        worst["p_oracle"] = max(worst["p_oracle"], rel_l2(a["pressure"], c["pressure"]))
+        worst["x"] = max(worst["x"], float(np.max(np.abs(a["pos"] - c["pos"]))))
+        worst["v"] = max(worst["v"], float(np.max(np.abs(a["vel"] - c["vel"]))))
+    assert worst["p_fp64"] < P_TRAJ and worst["p_oracle"] < P_TRAJ, worst
+    assert worst["x"] < X_TRAJ and worst["v"] < V_TRAJ, worst
+    em.close()
+    ef.close()

@@ -54,6 +54,60 @@ def test_first_step_bit_exact(name):
     assert st["status"] == 0
 
 
+# MIXED step 1 against the FP64 goldens (see the test's docstring)
+PM_TOL = 1e-6    # relative L2 of pressure: the mixed solve stops at relative residual 1e-10
+XM_TOL = 1e-10   # metres: the FP32 pressure-gradient sum moves particles by ~1e-12 m
+VM_TOL = 1e-7    # m/s
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_first_step_mixed_against_reference(name):
+    """The MIXED step (FP32 viscosity and pressure-gradient sums, FP32
+    Krylov iterations with FP64 refinement) on the reference's golden scenes.
+    From rest the viscosity sum is exactly 0 in any precision (every
+    v_j - v_i is 0), so the positions before the pressure part are the FP64
+    step's and the pressure phase's neighbour lists (ids, order, FP64
+    distances), collision pairs, surface and Dirichlet flags, source term and
+    matrix equal the goldens bit for bit.  Scenes that start moving (the
+    jittered ones, the 3-D box) carry the FP32 viscosity's rounding into their
+    positions: there ids, order, flags and collision pairs are still exact and
+    distances agree within 1e-15 relative.  Pressure, positions and
+    velocities within PM_TOL, XM_TOL, VM_TOL."""
+    m = engine_or_skip()
+    g = load(name)
+    at_rest = not np.any(g["vel0"])
+    e = m.Engine(g["params"], g["pos0"], g["vel0"], g["type0"], precision=m.MIXED)
+    st = e.step(export=bool(g["meta"]["export_every"] == 1))
+    assert st["status"] == 0
+    ci, cj, cd = e.collisions()
+    assert np.array_equal(ci, g["s1_coll_i"]) and np.array_equal(cj, g["s1_coll_j"])
+    if at_rest:
+        assert np.array_equal(cd, g["s1_coll_d"])
+    else:
+        assert np.allclose(cd, g["s1_coll_d"], rtol=1e-15, atol=0)
+    s = e.state()
+    if "s1_bc" in g:
+        for k in ("bc", "type", "dirichlet"):
+            assert np.array_equal(s[k], g[f"s1_{k}"]), k
+        assert rel_l2(s["pressure"], g["s1_pressure"]) < PM_TOL
+        assert np.max(np.abs(s["pos"] - g["s1_pos"])) < XM_TOL
+        assert np.max(np.abs(s["vel"] - g["s1_vel"])) < VM_TOL
+    if "s1_nb_off" in g:
+        off, ids, dist = e.neighbors()
+        assert np.array_equal(off, g["s1_nb_off"])
+        assert np.array_equal(ids, g["s1_nb_id"])
+        src, rp, col, val = e.system()
+        assert np.array_equal(rp, g["s1_row_ptr"]) and np.array_equal(col, g["s1_col"])
+        if at_rest:
+            assert np.array_equal(dist, g["s1_nb_dist"])
+            assert np.array_equal(src, g["s1_source"])
+            assert np.array_equal(val, g["s1_val"])
+        else:
+            assert np.allclose(dist, g["s1_nb_dist"], rtol=1e-15, atol=0)
+            assert np.allclose(val, g["s1_val"], rtol=1e-14, atol=0)
+    e.close()
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_trajectory_against_reference(name):
     m = engine_or_skip()
@@ -70,6 +124,8 @@ def test_trajectory_against_reference(name):
             for k in ("type", "bc", "dirichlet"):
                 assert np.array_equal(r[k], g[f"s{s}_{k}"]), (s, k)
             assert rel_l2(r["pressure"], g[f"s{s}_pressure"]) < 1e-7, s
+            # setMinimumPressure (src/mps.cpp:481-503) of those pressures
+            assert rel_l2(r["min_pressure"], g[f"s{s}_min_pressure"]) < 1e-7, s
             assert np.max(np.abs(r["pos"] - g[f"s{s}_pos"])) < 1e-10, s
             assert np.max(np.abs(r["vel"] - g[f"s{s}_vel"])) < 1e-7, s
             assert rel_l2(r["ndr"], g[f"s{s}_ndr"]) < 1e-12, s

@@ -30,8 +30,11 @@ def _entry():
     return engine, fn
 
 
-@pytest.mark.parametrize("scene", ["dambreak", "jittered_with_ghosts"])
+@pytest.mark.parametrize("scene", ["dambreak", "jittered_with_ghosts", "box3d", "outside_domain"])
 def test_static_scratch_number_density_matches_create(scene):
+    """Planar scenes (which mps_create sweeps with its planar cell keys while
+    this entry point always uses the 3-D key), a 3-D box, and particles placed
+    outside the domain (their cell coordinates clamped to the grid)."""
     m = engine_or_skip()
     import torch
 
@@ -44,6 +47,20 @@ def test_static_scratch_number_density_matches_create(scene):
         fl = t == scenes.FLUID
         pos[fl, :2] += rng.uniform(-0.3, 0.3, (fl.sum(), 2)) * 0.01
         t[np.flatnonzero(fl)[::17]] = scenes.GHOST
+    elif scene == "box3d":
+        from golden_cases import load
+
+        g = load("box3d")
+        prm, pos, vel, t = g["params"], g["pos0"].copy(), g["vel0"].copy(), g["type0"].copy()
+        assert prm["dim"] == 3 and len(t) < 65536
+    elif scene == "outside_domain":
+        fl = np.flatnonzero(t == scenes.FLUID)
+        lo, hi = prm["domain_min"], prm["domain_max"]
+        pos[fl[0], 0] = lo[0] - 0.05        # left of the grid
+        pos[fl[1], 1] = hi[1] + 0.2         # above it
+        pos[fl[2], :2] = [hi[0] + 1.0, lo[1] - 1.0]
+        pos[fl[3], 0] = pos[fl[2], 0] + 0.005  # a neighbour out there too
+        pos[fl[3], 1] = pos[fl[2], 1]
     # the allocating path: mps_create computes the initial number density ratios
     eng = m.Engine(prm, pos, vel, t)
     want = eng.state()["ndr"]
@@ -84,3 +101,21 @@ def test_static_scratch_rejects_oversize_requests():
             None)
     assert rc == engine.MPS_ERR_ARG
     assert "cells" in engine.load().mps_last_error().decode()
+
+
+def test_static_scratch_rejects_a_bad_domain():
+    """An inverted or non-finite domain is refused before any launch (it
+    would give an axis fewer than the 3 cells the clamped sweep needs)."""
+    engine_or_skip()
+    import torch
+
+    from mps_gb300 import scenes
+
+    engine, fn = _entry()
+    prm, *_ = scenes.dam_break(0.01)
+    buf = torch.zeros(30, dtype=torch.float64, device=torch.device("cuda:0"))
+    for lo, hi in (([0.5, -0.1, 0.0], [-0.1, 0.7, 0.0]), ([float("nan"), -0.1, 0.0], [1.1, 0.7, 0.0])):
+        bad = dict(prm, domain_min=lo, domain_max=hi)
+        rc = fn(C.byref(engine.make_params(bad)), 10, buf.data_ptr(), buf.data_ptr(), buf.data_ptr(), None)
+        assert rc == engine.MPS_ERR_ARG
+        assert "domain" in engine.load().mps_last_error().decode()
