@@ -116,13 +116,17 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
  * mode 1 (default): aggregation multigrid, additive at the particle level,
  * u = omega D^-1 r + scale P V(P^T r) with P the piecewise-constant
  * particle-to-cell transfer and V a V(1,1) cycle over the cell grids (one
- * operator pass per iteration); mode 3: the same with the smoothed
+ * operator pass per iteration, applied to D^-1 r while the cycle runs, and
+ * A u assembled from it and the rows' 3x3-cell sums of A); mode 4: mode 1's
+ * preconditioner with the operator applied to u after the cycle (the same
+ * iteration in the order of the textbook loop; kept for comparison, and the
+ * form every batch scene uses); mode 3: the same with the smoothed
  * transfer P = P1 - omega D^-1 A P1, applied through the rows' 3x3-cell sums
  * of A (fewer iterations, no extra operator pass); mode 2:
  * the multiplicative V(1,1) cycle from the particle level (three operator
  * passes per iteration).  omega = Jacobi weight in (0,1], scale =
- * coarse-correction weight in [1,2); 0 picks the mode's default (modes 1
- * and 3: 1.0, 1.4; mode 2: 0.9, 1.5).  No counterpart in the reference (its
+ * coarse-correction weight in [1,2); 0 picks the mode's default (modes 1,
+ * 3 and 4: 1.0, 1.4; mode 2: 0.9, 1.5).  No counterpart in the reference (its
  * CG is Jacobi-preconditioned). */
 int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale);
 

@@ -206,6 +206,7 @@ int mps_batch_create(int32_t n_scenes, const mps_params* params, const int32_t* 
         mps_engine* e = nullptr;
         int rc = mps_create(&params[s], counts[s], pos + 3 * off, vel + 3 * off, type + off, &e);
         if (rc) return bail(rc);
+        e->cycle_overlap = 0;  // the batched solve kernel runs mode 1 in its plain form
         b->eng.push_back(e);
         if ((rc = mps_set_solver(e, MPS_PRECISION_MIXED, b->tol, 0))) return bail(rc);
         off += counts[s];

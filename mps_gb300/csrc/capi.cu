@@ -185,8 +185,9 @@ int alloc_state(mps_engine* e, StateBuf& s) {
 Mg active_mg(const mps_engine* e) {
     Mg g = e->mg;
     g.enabled = e->mg.enabled && e->mg_requested != 0;
-    g.additive = e->mg_requested == 1 || e->mg_requested == 3;
+    g.additive = e->mg_requested == 1 || e->mg_requested == 3 || e->mg_requested == 4;
     g.smooth = e->mg_requested == 3;
+    g.overlap = e->mg_requested == 1 && e->cycle_overlap;
     return g;
 }
 
@@ -297,24 +298,30 @@ void enqueue_step(mps_engine* e, bool do_export) {
 // 72 B (segment bounds, the up pass's 9-point stencil and 8 vector words)
 // and of levels >= 2 132 B (the same plus the 4x4 restriction weights), and,
 // additive at level 0, 81 B per row (161 B with the smoothed transfer: the
-// 9 row-to-cell sums read twice and the neighbourhood's residuals),
+// 9 row-to-cell sums read twice and the neighbourhood's residuals; 141 B in
+// the overlapped arrangement of mode 1: the operator pass on y = D^-1 r
+// 25 B, the pass that forms u, w and the dot products 64 B with the 9
+// row-to-cell sums, the vector update 48 B, the level-1 sums 4 B),
 // multiplicative 143 B per row and two more level-0 operator passes.  MIXED adds per refinement the FP64
 // residual (12 B/entry + 36 B/row) and once the FP32 operator setup
-// (17 B/entry + 16 B/row written and read).
+// (17 B/entry + 16 B/row written and read; 36 B/row more for the row-to-cell
+// sums of modes 1 and 3).
 double solve_bytes(const mps_engine* e, const DevStats& h) {
     const double nnz = (double)h.nnz_off, n = (double)e->n, it = (double)h.cg_iterations;
     if (e->precision == MPS_PRECISION_FP64) return it * (12.0 * nnz + 116.0 * n) + 36.0 * n;
-    const bool mg = e->mg.enabled && e->mg_requested != 0;
-    const bool additive = mg && (e->mg_requested == 1 || e->mg_requested == 3);
-    const bool smooth = mg && e->mg_requested == 3;
+    const Mg g = active_mg(e);
+    const bool mg = g.enabled != 0;
+    const bool additive = mg && g.additive;
     const double ent = e->c.planar ? 5.0 : 8.0;
+    const double row_add = g.smooth ? 161.0 : g.overlap ? 141.0 : 81.0;
     double per_it = !mg ? (ent * nnz + 65.0 * n)
-                        : additive ? (ent * nnz + (smooth ? 161.0 : 81.0) * n) : (3.0 * ent * nnz + 143.0 * n);
+                        : additive ? (ent * nnz + row_add * n) : (3.0 * ent * nnz + 143.0 * n);
     if (mg)
         for (int l = 1; l <= e->mg.nlev; l++)
             per_it += (l == 1 ? 72.0 : 132.0) * e->mg.lev[l].nx * e->mg.lev[l].ny;
     const double ref = (double)h.refinements + 1.0;
-    return it * per_it + ref * (12.0 * nnz + 36.0 * n) + (17.0 * nnz + 16.0 * n);
+    const double setup = 17.0 * nnz + 16.0 * n + (mg && (g.smooth || g.overlap) ? 36.0 * n : 0.0);
+    return it * per_it + ref * (12.0 * nnz + 36.0 * n) + setup;
 }
 
 void fill_stats(mps_engine* e, mps_step_stats* out) {
@@ -700,7 +707,7 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
 
 int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale) {
     if (!e) return fail(MPS_ERR_ARG, "null engine");
-    if (mode < 0 || mode > 3) return fail(MPS_ERR_ARG, "multigrid mode must be 0, 1, 2 or 3");
+    if (mode < 0 || mode > 4) return fail(MPS_ERR_ARG, "multigrid mode must be 0, 1, 2, 3 or 4");
     if (mode && !e->mg.enabled)
         return fail(MPS_ERR_ARG, "multigrid needs a planar scene (2-D, constant z)");
     float dw, ds;

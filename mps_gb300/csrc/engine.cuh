@@ -234,6 +234,11 @@ struct Mg {
     // additive with a smoothed particle-to-cell transfer: P = P1 - omega D^-1 A P1
     // in place of P1 (the cell levels keep the operators of plain aggregation)
     int32_t smooth;
+    // additive (plain transfer) in the overlapped arrangement of the
+    // single-scene solve: the level-0 operator is applied to D^-1 r while the
+    // cell levels run, and A u is assembled from it and B e1 (solver.cu,
+    // solve_mixed_overlap)
+    int32_t overlap;
     // B = A P1 per slot: the operator row's sums over the 3x3 cells around the
     // slot's own, entry d = (dx+1)*3 + (dy+1), diagonal included (9 x n_pad)
     float* rowcell;

@@ -54,8 +54,12 @@ struct mps_engine {
     mpsg::MatFree mf{};
     mpsg::Mg mg{};
     // 0 Jacobi, 1 multigrid additive at level 0, 2 multiplicative, 3 additive
-    // with the smoothed particle-to-cell transfer
+    // with the smoothed particle-to-cell transfer, 4 mode 1's preconditioner
+    // with the operator pass after the cycle (mode 1 overlaps them)
     int32_t mg_requested = 1;
+    // mode 1 may use the overlapped single-scene kernel (batch scenes share
+    // the batched kernel, which has no overlapped form)
+    int32_t cycle_overlap = 1;
     int32_t *cand_cnt = nullptr, *cand_base = nullptr;
     mpsg::CollPair* pairs = nullptr;
     int32_t pair_cap = 0;

@@ -242,7 +242,7 @@ void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg&
                      cudaStream_t st) {
     if (!mg.enabled) return;
     const int T = 256;
-    if (mg.smooth) {
+    if (mg.smooth || mg.overlap) {
         k_mg_rowcell<<<(c.n + T - 1) / T, T, 0, st>>>(c, A, mf, (size_t)mg.n_pad, mg.rowcell);
         ++g_launches;
     }

@@ -87,9 +87,24 @@ __device__ __forceinline__ void red_release_add(unsigned int* p, unsigned int v)
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Block-level barrier of a thread group: NT = 0 is the whole block
+// (__syncthreads), else the block's first NT threads (named barrier 1, NT a
+// multiple of 32); the rest of the block runs on meanwhile.
+template <int NT>
+__device__ __forceinline__ void group_bar() {
+    if constexpr (NT == 0)
+        __syncthreads();
+    else
+        asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
+}
+
+// A grid barrier passed by a thread group of every block (NT as above):
+// thread 0 arrives for the block.  Only thread 0's epoch and warp 0's partials
+// parity matter, and thread 0 belongs to every group.
+template <int NT = 0>
 __device__ __forceinline__ bool grid_sync(GridBar& gb, DevStats* ds) {
     __shared__ int s_ok;
-    __syncthreads();
+    group_bar<NT>();
     gb.epoch++;
     if (threadIdx.x == 0) {
         const unsigned int target = gb.epoch * (unsigned int)gb.size;
@@ -115,7 +130,7 @@ __device__ __forceinline__ bool grid_sync(GridBar& gb, DevStats* ds) {
         }
         s_ok = ok;
     }
-    __syncthreads();
+    group_bar<NT>();
     return s_ok != 0;
 }
 
@@ -555,11 +570,12 @@ __device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, 
 
 // Levels lo..nlev of the V-cycle, run by the group's first block alone (they
 // are small): down smoothing + restriction, the dense coarsest solve, up
-// smoothing with the prolongation folded in.  Only __syncthreads inside; the
+// smoothing with the prolongation folded in.  Only block-level barriers of the group NT inside; the
 // caller brackets it with grid barriers.  `lv` are this block's views of the
 // levels (their e/t roles swap after each up-smoothing).
+template <int NT>
 __device__ void mg_block_levels(const Mg& mg, int lo, MgLevel* lv) {
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int tid = threadIdx.x, nt = NT == 0 ? (int)blockDim.x : NT;
     // level lo's r and pre-smoothed e are already written (by the grid pass)
     for (int l = lo; l < mg.nlev; l++) {
         const MgLevel& L = lv[l];
@@ -572,7 +588,7 @@ __device__ void mg_block_levels(const Mg& mg, int lo, MgLevel* lv) {
             C.r[I] = rr;
             if (smooth) C.e[I] = mg.omega * iv * rr;
         }
-        __syncthreads();
+        group_bar<NT>();
     }
     {
         // coarsest level: e = A_c^-1 r, one warp per row (lanes split the row)
@@ -586,14 +602,14 @@ __device__ void mg_block_levels(const Mg& mg, int lo, MgLevel* lv) {
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0) L.e[i] = ldc(L.invd, i) > 0.f ? acc : 0.f;
         }
-        __syncthreads();
+        group_bar<NT>();
     }
     for (int l = mg.nlev - 1; l >= lo; l--) {
         MgLevel& L = lv[l];
         MgLevel& C = lv[l + 1];
         const int n = L.nx * L.ny;
         for (int I = tid; I < n; I += nt) L.t[I] = ldc(L.invd, I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
-        __syncthreads();
+        group_bar<NT>();
         // the views are this block's own: swap instead of copying
         float* tmp = L.e;
         L.e = L.t;
@@ -601,22 +617,110 @@ __device__ void mg_block_levels(const Mg& mg, int lo, MgLevel* lv) {
     }
 }
 
+template <int NT>
 __device__ void mg_block_cycle(Mg& mg, int lo) {
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, nt = NT == 0 ? (int)blockDim.x : NT;
     MgLevel v[kMgMaxLevels];
     for (int l = lo; l <= mg.nlev; l++) v[l] = mg.lev[l];
-    mg_block_levels(mg, lo, v);
+    mg_block_levels<NT>(mg, lo, v);
     // after the swap level lo's correction sits in its t array: copy it to
     // e, where every block reads it
     const int nlo = v[lo].nx * v[lo].ny;
     if (v[lo].e != mg.lev[lo].e)
-        for (int i = tid; i < nlo; i += blockDim.x) mg.lev[lo].e[i] = __ldcg(v[lo].e + i);
-    __syncthreads();
+        for (int i = tid; i < nlo; i += nt) mg.lev[lo].e[i] = __ldcg(v[lo].e + i);
+    group_bar<NT>();
     // levels above lo keep their swapped roles in this block's copy
     for (int l = lo + 1; l <= mg.nlev; l++) {
         mg.lev[l].e = v[l].e;
         mg.lev[l].t = v[l].t;
     }
+}
+
+// Level 1 of plain aggregation: the sum over each cell's contiguous slots of
+// src0, pre-smoothed (e = omega invd r).  Four of this thread's cells at
+// once, their slots four at a time, all loads of a round before any use
+// (predicated: slots past a cell's end are not read, which also keeps the
+// many empty cells off any one address): each cell still sums its slots in
+// slot order.  gcell / gsz: this thread's first cell and the group's stride.
+__device__ __forceinline__ void mg_level1_plain(Mg& mg, const MatFree& mf,
+                                                const float* __restrict__ src0, int gcell, int gsz) {
+    MgLevel& L1 = mg.lev[1];
+    const int n1 = L1.nx * L1.ny;
+    for (int I0 = gcell; I0 < n1; I0 += 4 * gsz) {
+        int b[4], cnt[4];
+        float iv[4], acc[4];
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            const int I = min(I0 + h * gsz, n1 - 1);
+            b[h] = __ldg(mf.cs + I);
+            cnt[h] = __ldg(mf.cs + I + 1) - b[h];
+            iv[h] = __ldg(L1.invd + I);
+            acc[h] = 0.f;
+        }
+        const int m = max(max(cnt[0], cnt[1]), max(cnt[2], cnt[3]));
+        for (int j = 0; j < m; j += 4) {
+            float x[4][4];
+#pragma unroll
+            for (int h = 0; h < 4; h++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) x[h][q] = j + q < cnt[h] ? __ldcg(src0 + b[h] + j + q) : 0.f;
+#pragma unroll
+            for (int h = 0; h < 4; h++)
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (j + q < cnt[h]) acc[h] += x[h][q];
+        }
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            const int I = I0 + h * gsz;
+            if (I < n1) {
+                L1.r[I] = acc[h];
+                L1.e[I] = mg.omega * iv[h] * acc[h];
+            }
+        }
+    }
+}
+
+// The cell levels of the V-cycle after level 1's residual and pre-smoothing
+// were written: a grid barrier, the grid-wide levels down (restriction
+// fused with the next level's pre-smoothing), the small levels in the
+// group's first block, the grid-wide levels up (prolongation folded into the
+// post-smoothing), each phase closed by a grid barrier of the thread group NT
+// (0: whole blocks).  Afterwards level 1's correction is complete in
+// mg.lev[1].e for every block.
+template <int NT>
+__device__ __forceinline__ bool mg_cell_levels(Mg& mg, GridBar& gb, DevStats* ds, int gcell, int gsz) {
+    if (!grid_sync<NT>(gb, ds)) return false;
+    // grid-wide levels, down: restrict level l into l+1 and pre-smooth there
+    // (every level but the coarsest, whose e comes from its dense inverse)
+    for (int l = 1; l <= mg.ngrid; l++) {
+        MgLevel& L = mg.lev[l];
+        MgLevel& C = mg.lev[l + 1];
+        const bool smooth = l + 1 < mg.nlev;
+        for (int I = gcell; I < C.nx * C.ny; I += gsz) {
+            const int X = I / C.ny, Y = I - X * C.ny;
+            const float iv = __ldg(C.invd + I);
+            const float rr = iv > 0.f ? restrict_cell(L, C, I, X, Y) : 0.f;
+            C.r[I] = rr;
+            if (smooth) C.e[I] = mg.omega * iv * rr;
+        }
+        if (!grid_sync<NT>(gb, ds)) return false;
+    }
+    // small levels in the group's first block
+    if (gb.rank == 0) mg_block_cycle<NT>(mg, mg.ngrid + 1);
+    if (!grid_sync<NT>(gb, ds)) return false;
+    // grid-wide levels, up: prolongation folded into the post-smoothing
+    for (int l = mg.ngrid; l >= 1; l--) {
+        MgLevel& L = mg.lev[l];
+        MgLevel& C = mg.lev[l + 1];
+        const int nl = L.nx * L.ny;
+        for (int I = gcell; I < nl; I += gsz) L.t[I] = __ldg(L.invd + I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
+        if (!grid_sync<NT>(gb, ds)) return false;
+        float* tmp = L.e;
+        L.e = L.t;
+        L.t = tmp;
+    }
+    return true;
 }
 
 // u = M r: one symmetric V(1,1) cycle with damped Jacobi smoothing.  The
@@ -714,72 +818,9 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
             L1.e[I] = mg.omega * iv * rr;
         }
     } else {
-        MgLevel& L1 = mg.lev[1];
-        const int n1 = L1.nx * L1.ny;
-        for (int I0 = gcell; I0 < n1; I0 += 4 * gsz) {
-            int b[4], cnt[4];
-            float iv[4], acc[4];
-#pragma unroll
-            for (int h = 0; h < 4; h++) {
-                const int I = min(I0 + h * gsz, n1 - 1);
-                b[h] = __ldg(mf.cs + I);
-                cnt[h] = __ldg(mf.cs + I + 1) - b[h];
-                iv[h] = __ldg(L1.invd + I);
-                acc[h] = 0.f;
-            }
-            const int m = max(max(cnt[0], cnt[1]), max(cnt[2], cnt[3]));
-            for (int j = 0; j < m; j += 4) {
-                float x[4][4];
-#pragma unroll
-                for (int h = 0; h < 4; h++)
-#pragma unroll
-                    for (int q = 0; q < 4; q++) x[h][q] = j + q < cnt[h] ? __ldcg(src0 + b[h] + j + q) : 0.f;
-#pragma unroll
-                for (int h = 0; h < 4; h++)
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        if (j + q < cnt[h]) acc[h] += x[h][q];
-            }
-#pragma unroll
-            for (int h = 0; h < 4; h++) {
-                const int I = I0 + h * gsz;
-                if (I < n1) {
-                    L1.r[I] = acc[h];
-                    L1.e[I] = mg.omega * iv[h] * acc[h];
-                }
-            }
-        }
+        mg_level1_plain(mg, mf, src0, gcell, gsz);
     }
-    if (!grid_sync(gb, ds)) return false;
-    // grid-wide levels, down: restrict level l into l+1 and pre-smooth there
-    // (every level but the coarsest, whose e comes from its dense inverse)
-    for (int l = 1; l <= mg.ngrid; l++) {
-        MgLevel& L = mg.lev[l];
-        MgLevel& C = mg.lev[l + 1];
-        const bool smooth = l + 1 < mg.nlev;
-        for (int I = gcell; I < C.nx * C.ny; I += gsz) {
-            const int X = I / C.ny, Y = I - X * C.ny;
-            const float iv = __ldg(C.invd + I);
-            const float rr = iv > 0.f ? restrict_cell(L, C, I, X, Y) : 0.f;
-            C.r[I] = rr;
-            if (smooth) C.e[I] = mg.omega * iv * rr;
-        }
-        if (!grid_sync(gb, ds)) return false;
-    }
-    // small levels in the group's first block
-    if (gb.rank == 0) mg_block_cycle(mg, mg.ngrid + 1);
-    if (!grid_sync(gb, ds)) return false;
-    // grid-wide levels, up: prolongation folded into the post-smoothing
-    for (int l = mg.ngrid; l >= 1; l--) {
-        MgLevel& L = mg.lev[l];
-        MgLevel& C = mg.lev[l + 1];
-        const int nl = L.nx * L.ny;
-        for (int I = gcell; I < nl; I += gsz) L.t[I] = __ldg(L.invd + I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
-        if (!grid_sync(gb, ds)) return false;
-        float* tmp = L.e;
-        L.e = L.t;
-        L.t = tmp;
-    }
+    if (!mg_cell_levels<0>(mg, gb, ds, gcell, gsz)) return false;
     if (mg.additive && mg.smooth) {
         // u = omega D^-1 r + scale * P e1, P e1 = e1[cell(i)] - omega / d_i sum_d B[d][i] e1[cell(i) + d]
         MgLevel& L1 = mg.lev[1];
@@ -1064,6 +1105,243 @@ __global__ void __launch_bounds__(kMixedBlock, 1) k_cg_mixed(Ppe A, MatFree mf, 
     solve_mixed<kMixedBlock>(A, mf, mg, kv, a, ds, gb);
 }
 
+// ----------------------------------------------- overlapped additive cycle
+// Multigrid mode 1 (additive, plain transfer) arranged so that the level-0
+// operator pass overlaps the cell levels of the V-cycle.  With y = D^-1 r and
+// e1 the level-1 correction, the preconditioned residual is
+//     u = omega y + scale P1 e1
+// and, since A P1 = B (the rows' 3x3-cell sums, k_mg_rowcell),
+//     w = A u = omega (A y) + scale B e1,
+// where A y needs only r, not the cycle.  So after the vector update (which
+// writes y) and one grid barrier, each block splits: its first kCycleThreads
+// threads run the cycle (level-1 sums, the grid-wide levels with grid
+// barriers of that group, the small levels in block 0), the other warps
+// apply the FP32 operator to y for the block's own rows (z = A y).  The
+// block joins, and one pass over its rows forms u, w and the three dot
+// products.  The operator pass (most of an iteration's HBM traffic) is thus
+// off the cycle's chain of dependent phases, and u and w never leave the
+// block (no operator pass reads them).  Same Chronopoulos-Gear recurrences,
+// refinement and stopping rules as solve_mixed.
+//
+// Rows of block b: the 32-row slices b, b + G, b + 2G, ... (G blocks).
+constexpr int kCycleThreads = 512;
+
+template <int BS, int NV>
+__device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree& mf, Mg& mg,
+                                                    const Krylov& kv, const SolveArgs& a, DevStats* ds,
+                                                    GridBar& gb) {
+    if (*(volatile int32_t*)&ds->status & ST_ASYMMETRIC) {  // the reference exits here
+        if (gb.rank == 0 && threadIdx.x == 0) {
+            ds->cg_iterations = 0;
+            ds->refinements = 0;
+            ds->cg_rel_residual = -1.0;
+        }
+        return;
+    }
+    constexpr int kW = BS / 32, kVW = NV / 32, kZW = kW - kVW;
+    static_assert(kVW > 0 && kZW > 0, "both groups need warps");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int G = gb.size, b = gb.rank;
+    const int gtid = b * BS + tid, gsz = G * BS;
+    const int gwarp = gtid >> 5, nwarps = gsz >> 5;
+    const int n = a.n, nsl = a.nslices;
+    // per-slot FP32 work vectors of this arrangement (the additive cycle uses
+    // neither the level-0 correction nor the level-0 residual arrays)
+    float* __restrict__ y = mg.e0;    // D^-1 r
+    float* __restrict__ z = mg.res0;  // A y
+    const size_t np = (size_t)mg.n_pad;
+    const int NY = mg.lev[1].ny, n1 = mg.lev[1].nx * NY;
+    __shared__ float* s_e1;
+    __shared__ int s_cycle_ok;
+
+    double acc[1] = {0.0}, tot[1];
+    for (int sl = gwarp; sl < nsl; sl += nwarps) {
+        int i = sl * 32 + lane;
+        if (i >= n) continue;
+        kv.x[i] = 0.0;
+        double bb = A.src[i];
+        acc[0] = fma(bb, bb, acc[0]);
+    }
+    if (!reduce_sync<1, BS>(gb, acc, tot, ds)) return;
+    const double rhs2 = tot[0];
+    const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
+    int64_t inner_total = 0;
+    int refine = 0;
+    double rn2 = rhs2;
+    while (rhs2 > 0.0) {
+        // FP64 residual r = b - A x
+        double a0[1] = {0.0}, t0[1];
+        for (int sl = gwarp; sl < nsl; sl += nwarps) {
+            int i = sl * 32 + lane;
+            if (i >= n) continue;
+            double r = A.src[i] - spmv64_row(A, a.K, sl, lane, i, kv.x, kv.x[i]);
+            kv.r[i] = r;
+            a0[0] = fma(r, r, a0[0]);
+        }
+        if (!reduce_sync<1, BS>(gb, a0, t0, ds)) return;
+        rn2 = t0[0];
+        if (rn2 < thr || refine >= a.max_refine || inner_total >= a.max_iter) break;
+        refine++;
+        const float ithr = (float)fmax(a.inner_tol * a.inner_tol, 0.25 * thr / rn2);
+        const float scale = (float)(1.0 / sqrt(rn2));
+        for (int i = gtid; i < n; i += gsz) {
+            const float r = (float)kv.r[i] * scale;
+            kv.r32[i] = r;
+            kv.x32[i] = 0.f;
+            kv.p32[i] = 0.f;
+            kv.s32[i] = 0.f;
+            y[i] = kv.inv_diag32[i] * r;
+        }
+        if (!grid_sync(gb, ds)) return;
+        float alpha = 0.f, beta = 0.f, gamma_old = 1.f;
+        int64_t k = 0;
+        for (;;) {
+            // ---- split: the cycle on r, the operator on y
+            if (warp < kVW) {
+                const int gcell = ((warp * G + b) << 5) + lane;
+                mg_level1_plain(mg, mf, kv.r32, gcell, G * NV);
+                const bool ok = mg_cell_levels<NV>(mg, gb, ds, gcell, G * NV);
+                if (tid == 0) {
+                    s_e1 = mg.lev[1].e;
+                    s_cycle_ok = ok;
+                }
+            } else {
+                for (int q = warp - kVW;; q += 2 * kZW) {
+                    const int sl1 = b + G * q;
+                    if (sl1 >= nsl) break;
+                    const int sl2 = b + G * (q + kZW);
+                    const int i = sl1 * 32 + lane;
+                    int i2 = sl2 < nsl ? sl2 * 32 + lane : -1;
+                    if (i2 >= n) i2 = -1;
+                    if (i >= n) continue;  // the partial last slice (then i2 < 0 too)
+                    const int j2 = i2 >= 0 ? i2 : i;
+                    const float dg0 = A.diag32[i], dg1 = A.diag32[j2];
+                    const float y0 = __ldcg(y + i), y1 = __ldcg(y + j2);
+                    float o, o2;
+                    off_rows(A, mf, a.K, i, i2, y, o, o2);
+                    z[i] = dg0 > 0.f ? fmaf(dg0, y0, o) : 0.f;
+                    if (i2 >= 0) z[i2] = dg1 > 0.f ? fmaf(dg1, y1, o2) : 0.f;
+                }
+            }
+            __syncthreads();
+            if (!s_cycle_ok) return;
+            const float* __restrict__ e1 = s_e1;
+            // ---- u = omega y + scale e1[cell], w = omega z + scale B e1, dot products
+            F2 g = {0.f, 0.f}, dl = {0.f, 0.f}, rr = {0.f, 0.f};
+            for (int q = warp;; q += 2 * kW) {
+                const int sla = b + G * q;
+                if (sla >= nsl) break;
+                const int slb = b + G * (q + kW);
+                int ii[2] = {sla * 32 + lane, slb < nsl ? slb * 32 + lane : n};
+                float dg[2], ri[2], yi[2], zi[2];
+                int key[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int i = min(ii[h], n - 1);
+                    dg[h] = A.diag32[i];
+                    ri[h] = __ldcg(kv.r32 + i);
+                    yi[h] = __ldcg(y + i);
+                    zi[h] = __ldcg(z + i);
+                    key[h] = min(__ldg(mf.skey + i), n1 - 1);
+                }
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    if (ii[h] >= n) break;
+                    const int i = ii[h];
+                    float u = 0.f, w = 0.f;
+                    if (dg[h] > 0.f) {  // an unknown: its cell is interior
+                        float bt[9], en[9];
+#pragma unroll
+                        for (int d = 0; d < 9; d++) {
+                            bt[d] = __ldg(mg.rowcell + (size_t)d * np + i);
+                            en[d] = __ldcg(e1 + key[h] + (d / 3 - 1) * NY + (d % 3 - 1));
+                        }
+                        float corr = 0.f;
+#pragma unroll
+                        for (int d = 0; d < 9; d++) corr = fmaf(bt[d], en[d], corr);
+                        u = fmaf(mg.scale, en[4], mg.omega * yi[h]);
+                        w = fmaf(mg.scale, corr, mg.omega * zi[h]);
+                    }
+                    kv.u32[i] = u;
+                    kv.w32[i] = w;
+                    acc_prod(g, ri[h], u);
+                    acc_prod(dl, w, u);
+                    acc_prod(rr, ri[h], ri[h]);
+                }
+            }
+            double v3[3] = {f2d(g), f2d(dl), f2d(rr)}, t3[3];
+            if (!reduce_sync<3, BS>(gb, v3, t3, ds)) return;
+            if ((float)t3[2] < ithr || inner_total + k >= a.max_iter) break;
+            const float gamma = (float)t3[0], delta = (float)t3[1];
+            if (k == 0) {
+                beta = 0.f;
+                alpha = gamma / delta;
+            } else {
+                beta = gamma / gamma_old;
+                float den = delta - beta * gamma / alpha;
+                if (!(den > 0.f)) break;  // loss of positive definiteness in FP32
+                alpha = gamma / den;
+            }
+            gamma_old = gamma;
+            // ---- p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; y = D^-1 r
+            // (this block's rows: u and w are its own; four rows in flight)
+            for (int q = warp;; q += 4 * kW) {
+                if (b + G * q >= nsl) break;
+                int ii[4];
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int sl = b + G * (q + h * kW);
+                    ii[h] = sl < nsl ? sl * 32 + lane : n;
+                }
+                float u[4], p[4], sv[4], w[4], x[4], r[4], id[4];
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int i = min(ii[h], n - 1);
+                    u[h] = __ldcg(kv.u32 + i);
+                    p[h] = kv.p32[i];
+                    sv[h] = kv.s32[i];
+                    w[h] = __ldcg(kv.w32 + i);
+                    x[h] = kv.x32[i];
+                    r[h] = __ldcg(kv.r32 + i);
+                    id[h] = kv.inv_diag32[i];
+                }
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int i = ii[h];
+                    if (i >= n) break;
+                    const float pn = fmaf(beta, p[h], u[h]);
+                    const float sn = fmaf(beta, sv[h], w[h]);
+                    kv.p32[i] = pn;
+                    kv.s32[i] = sn;
+                    kv.x32[i] = fmaf(alpha, pn, x[h]);
+                    const float rn = fmaf(-alpha, sn, r[h]);
+                    kv.r32[i] = rn;
+                    y[i] = id[h] * rn;
+                }
+            }
+            k++;
+            if (!grid_sync(gb, ds)) return;
+        }
+        inner_total += k;
+        // x += d (FP64)
+        const double back = sqrt(rn2);
+        for (int i = gtid; i < n; i += gsz) kv.x[i] = fma((double)kv.x32[i], back, kv.x[i]);
+        if (!grid_sync(gb, ds)) return;
+    }
+    if (gb.rank == 0 && threadIdx.x == 0) {
+        ds->cg_iterations = inner_total;
+        ds->refinements = refine;
+        ds->cg_rel_residual = rhs2 > 0.0 ? sqrt(rn2 / rhs2) : 0.0;
+        if (rhs2 > 0.0 && !(rn2 < thr)) atomicOr(&ds->status, ST_NOT_CONVERGED);
+    }
+}
+
+__global__ void __launch_bounds__(kMixedBlock, 1) k_cg_mixed_ov(Ppe A, MatFree mf, Mg mg, Krylov kv,
+                                                                SolveArgs a, DevStats* ds) {
+    GridBar gb = whole_grid(kv);
+    solve_mixed_overlap<kMixedBlock, kCycleThreads>(A, mf, mg, kv, a, ds, gb);
+}
+
 // Many scenes in one persistent launch: block b belongs to group bmap[b].x
 // (one scene) with rank bmap[b].y; each group converges on its own.
 struct SceneSolve {
@@ -1162,7 +1440,8 @@ SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
 void solver_setup(Krylov& k, int32_t /*n_pad*/, int device) {
     int g1 = coop_grid((const void*)k_cg64, device, kBlock, 0, 1);
     int g2 = coop_grid((const void*)k_cg_mixed, device, kMixedBlock, 0, 1);
-    k.grid = g1 < g2 ? g1 : g2;
+    int g3 = coop_grid((const void*)k_cg_mixed_ov, device, kMixedBlock, 0, 1);
+    k.grid = std::min({g1, g2, g3});
     k.block = kBlock;
 }
 
@@ -1344,7 +1623,8 @@ void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const 
     Krylov kk = k;
     void* args[] = {&AA, &mm, &gg, &kk, &a, &ds};
     cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
-    cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(k.grid), dim3(kMixedBlock), args, 0, st);
+    const void* fn = mg.enabled && mg.overlap ? (const void*)k_cg_mixed_ov : (const void*)k_cg_mixed;
+    cudaLaunchCooperativeKernel(fn, dim3(k.grid), dim3(kMixedBlock), args, 0, st);
     ++g_launches;
 }
 

@@ -70,9 +70,10 @@ def test_first_step_mixed_against_reference(name):
     distances), collision pairs, surface and Dirichlet flags, source term and
     matrix equal the goldens bit for bit.  Scenes that start moving (the
     jittered ones, the 3-D box) carry the FP32 viscosity's rounding into their
-    positions: there ids, order, flags and collision pairs are still exact and
-    distances agree within 1e-15 relative.  Pressure, positions and
-    velocities within PM_TOL, XM_TOL, VM_TOL."""
+    positions (at 12 m/s, ~1e-13 m after one step): there ids, order, flags
+    and collision pairs are still exact, distances agree within 1e-10
+    relative and matrix entries within 1e-9 of the largest.  Pressure,
+    positions and velocities within PM_TOL, XM_TOL, VM_TOL."""
     m = engine_or_skip()
     g = load(name)
     at_rest = not np.any(g["vel0"])
@@ -84,7 +85,7 @@ def test_first_step_mixed_against_reference(name):
     if at_rest:
         assert np.array_equal(cd, g["s1_coll_d"])
     else:
-        assert np.allclose(cd, g["s1_coll_d"], rtol=1e-15, atol=0)
+        assert np.allclose(cd, g["s1_coll_d"], rtol=1e-10, atol=0)
     s = e.state()
     if "s1_bc" in g:
         for k in ("bc", "type", "dirichlet"):
@@ -103,8 +104,8 @@ def test_first_step_mixed_against_reference(name):
             assert np.array_equal(src, g["s1_source"])
             assert np.array_equal(val, g["s1_val"])
         else:
-            assert np.allclose(dist, g["s1_nb_dist"], rtol=1e-15, atol=0)
-            assert np.allclose(val, g["s1_val"], rtol=1e-14, atol=0)
+            assert np.allclose(dist, g["s1_nb_dist"], rtol=1e-10, atol=0)
+            assert np.max(np.abs(val - g["s1_val"])) <= 1e-9 * np.max(np.abs(g["s1_val"]))
     e.close()
 
 
