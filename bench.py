@@ -57,6 +57,16 @@ def workload(name: str):
     raise SystemExit(f"unknown workload {name}")
 
 
+def workload_config(name: str, prm: dict, nf: int, n: int) -> dict:
+    """The `config` of both arms' JSON lines (the same workload, whatever
+    runs it)."""
+    return {"workload": f"{name}: 2-D dam break, {nf} fluid / {n} particles, dt {prm['dt']} s, "
+                        f"l0 {prm['particle_distance']:.6g} m",
+            "particles": n, "fluid_particles": nf,
+            "cache": "inputs larger than L2: the state, neighbour lists and PPE matrix of one "
+                     "step are GBs, re-sorted and re-assembled every step"}
+
+
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
@@ -137,6 +147,77 @@ def traffic_per_row_iter(kernel: str):
 
 # ---------------------------------------------------------------- CPU baseline
 CPU_SAMPLE = "dambreak_cols200"  # 200 x 400 = 80,000 fluid particles, same tank and physics
+
+# The CPU oracle on the benchmark's own scene (a child process, so that it
+# runs on the host cores while the GPU legs run): `warmup` steps with the CG
+# capped at CPU_WARMUP_CG iterations (they only bring the state to the
+# physical time of the timed steps, as the GPU legs' warm-up steps do), then
+# one full step as the reference runs it (CG to machine epsilon, solved
+# twice, src/mps.cpp:452-460) and one step with one CG solve to the GPU
+# solver's tolerance 1e-10.  Each full step of the 1M scene takes minutes
+# (the reference's CG is serial), so one of each is the bounded sample.
+CPU_WARMUP_CG = 50
+_CPU_1M_CODE = """
+import sys, time, json
+sys.path.insert(0, %(repo)r); sys.path.insert(0, %(oracle)r)
+import bench
+from oracle import Oracle, build
+build()
+prm, pos, vel, t = bench.workload(%(wl)r)
+nf = int((t == 0).sum())
+o = Oracle(prm, pos, vel, t)
+o.set_cg(max_iter=%(wcap)d, solves=1)
+t0 = time.perf_counter()
+for _ in range(%(warmup)d):
+    o.step()
+tw = time.perf_counter() - t0
+out = {"nf": nf, "n": int(len(t)), "warmup": %(warmup)d, "warmup_s": tw, "legs": []}
+for tol, solves, name in %(legs)r:
+    if tol is None:
+        o.set_cg(solves=solves)
+    else:
+        o.set_cg(tol=tol, solves=solves)
+    t0 = time.perf_counter()
+    st = o.step()
+    out["legs"].append({"name": name, "seconds": time.perf_counter() - t0,
+                        "cg_iterations": int(st["cg_iterations"]), "cg_error": st["cg_error"],
+                        "solves": solves})
+    print(json.dumps(out), flush=True)
+"""
+
+
+def start_cpu_1m(warmup: int, legs, workload_name: str = "dambreak_1m", threads: int = 0):
+    """Starts the CPU oracle on the full workload in a child process; returns
+    (process, threads).  `legs`: list of (tol or None for eps, solves, name)."""
+    cores = os.cpu_count() or 1
+    threads = threads or max(1, cores - 2)  # leave the GPU legs' host thread and the sampler a core
+    code = _CPU_1M_CODE % {"repo": REPO, "oracle": os.path.join(REPO, "oracle"), "wl": workload_name,
+                           "wcap": CPU_WARMUP_CG, "warmup": warmup, "legs": list(legs)}
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    proc = subprocess.Popen([sys.executable, "-c", code], stdout=subprocess.PIPE,
+                            stderr=subprocess.PIPE, text=True, env=env)
+    return proc, threads
+
+
+def finish_cpu_1m(proc, threads: int, timeout: float = 3600) -> dict:
+    out, err = proc.communicate(timeout=timeout)
+    if proc.returncode != 0:
+        raise RuntimeError(err[-2000:])
+    d = json.loads(out.strip().splitlines()[-1])
+    legs = {}
+    for leg in d["legs"]:
+        legs[leg["name"]] = {"value": d["nf"] / leg["seconds"], "unit": UNIT,
+                             "seconds_per_step": leg["seconds"], "cg_iterations": leg["cg_iterations"],
+                             "cg_solves": leg["solves"], "cg_relative_error": leg["cg_error"]}
+    ref = d["legs"][0]
+    return {"value": d["nf"] / ref["seconds"], "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"dambreak_1m itself ({d['nf']} fluid / {d['n']} particles) on the CPU oracle: "
+                       f"{d['warmup']} warm-up steps with the CG capped at {CPU_WARMUP_CG} iterations "
+                       f"({d['warmup_s']:.1f} s, untimed), then one full step per leg: "
+                       + "; ".join(f"{x['name']}: {x['seconds']:.1f} s, {x['cg_iterations']} CG iterations "
+                                   f"x {x['solves']} solve(s)" for x in d["legs"])
+                       + f"; {threads} OpenMP threads (the CG is serial, as the reference's)"),
+            "legs": legs}
 
 
 def cpu_sample(steps: int = 3, workload_name: str = CPU_SAMPLE) -> dict:
@@ -374,6 +455,77 @@ def run_export(steps: int = 30, every: int = 10) -> dict:
             "d2h_bytes_per_export": int(len(t) * 72)}
 
 
+def run_accuracy_trajectory(prm, pos, vel, types, steps: int = 500, every: int = 50) -> dict:
+    """The mixed step against the plain FP64 step over `steps` steps from the
+    same initial state (config 2: "500 steps; report pressure and position
+    error vs the FP64 run"): every `every` steps the pressure relative L2,
+    the largest position and velocity differences and the count of surface
+    flags that differ.  The mixed engine's device time over the whole window
+    is reported too (its throughput over the configuration's 500 steps)."""
+    import torch
+
+    from mps_gb300 import FP64, MIXED, Engine
+
+    nf = int((types == 0).sum())
+    em = Engine(prm, pos, vel, types, precision=MIXED)
+    ef = Engine(prm, pos, vel, types, precision=FP64)
+    rows, sec_m, sec_f = [], 0.0, 0.0
+    its_m, its_f = [], []
+    for s0 in range(0, steps, every):
+        dt_m, st_m = _event_timed(em.stream_ptr(), lambda: [em.step() for _ in range(every)])
+        dt_f, st_f = _event_timed(ef.stream_ptr(), lambda: [ef.step() for _ in range(every)])
+        sec_m += dt_m
+        sec_f += dt_f
+        its_m += [x["cg_iterations"] for x in st_m]
+        its_f += [x["cg_iterations"] for x in st_f]
+        a, b = em.state(), ef.state()
+        pb = np.linalg.norm(b["pressure"]) or 1.0
+        rows.append({"step": s0 + every,
+                     "pressure_rel_l2": float(np.linalg.norm(a["pressure"] - b["pressure"]) / pb),
+                     "position_max_abs_m": float(np.max(np.abs(a["pos"] - b["pos"]))),
+                     "velocity_max_abs_mps": float(np.max(np.abs(a["vel"] - b["vel"]))),
+                     "surface_flags_differing": int(np.sum(a["bc"] != b["bc"])),
+                     "types_differing": int(np.sum(a["type"] != b["type"]))})
+    em.close()
+    ef.close()
+    torch.cuda.synchronize()
+    return {"steps": steps, "every": every, "rows": rows,
+            "max_pressure_rel_l2": max(r["pressure_rel_l2"] for r in rows),
+            "max_position_abs_m": max(r["position_max_abs_m"] for r in rows),
+            "mixed_value": nf * steps / sec_m, "fp64_value": nf * steps / sec_f, "unit": UNIT,
+            "mixed_ms_per_step": 1e3 * sec_m / steps, "fp64_ms_per_step": 1e3 * sec_f / steps,
+            "mixed_cg_iterations_mean": float(np.mean(its_m)),
+            "fp64_cg_iterations_mean": float(np.mean(its_f))}
+
+
+def run_precision_split(prm, state, steps: int = 4) -> dict:
+    """How much of the mixed/FP64 ratio is precision and how much is the
+    preconditioner: from one developed state, `steps` steps each of the FP64
+    solver (the reference's Jacobi CG), the mixed solver with the same Jacobi
+    preconditioner (multigrid mode 0), and the mixed solver with its default
+    multigrid; ms per solve and iterations of each."""
+    from mps_gb300 import FP64, MIXED, Engine
+
+    out = {}
+    for name, prec, mode in (("fp64_jacobi", FP64, None), ("mixed_jacobi", MIXED, 0),
+                             ("mixed_multigrid", MIXED, 1)):
+        e = Engine(prm, state["pos"], state["vel"], state["type"], precision=prec)
+        if mode is not None:
+            e.set_multigrid(mode)
+        e.step()
+        st = [e.step() for _ in range(steps)]
+        out[name] = {"ms_solve_mean": float(np.mean([x["ms_solve"] for x in st])),
+                     "cg_iterations_mean": float(np.mean([x["cg_iterations"] for x in st])),
+                     "refinements_mean": float(np.mean([x["refinements"] for x in st]))}
+        e.close()
+    f, j, g = out["fp64_jacobi"], out["mixed_jacobi"], out["mixed_multigrid"]
+    out["solve_speedup_precision_only"] = f["ms_solve_mean"] / j["ms_solve_mean"]
+    out["solve_speedup_preconditioner_on_top"] = j["ms_solve_mean"] / g["ms_solve_mean"]
+    out["solve_speedup_total"] = f["ms_solve_mean"] / g["ms_solve_mean"]
+    out["steps"] = steps
+    return out
+
+
 def run_small_case() -> dict:
     """The reference's own CPU-sized case (1,250 fluid particles, dt 1e-3 s,
     1,000 steps), FP64 on the GPU (graph replays) and on the CPU oracle."""
@@ -390,7 +542,48 @@ def run_small_case() -> dict:
     return {"workload": f"dambreak_small: {nf} fluid / {len(t)} particles, 1000 steps, FP64",
             "gpu_wall_s": round(gpu_s, 3), "gpu_value": nf * 1000 / gpu_s,
             "courant_final": st["courant"], "unit": UNIT,
-            "cpu_oracle": {k: cpu[k] for k in ("value", "cores", "kind", "sample")}}
+            "cpu_oracle": {k: cpu[k] for k in ("value", "cores", "kind", "sample")},
+            "accuracy_vs_oracle": small_case_accuracy(prm, pos, vel, t)}
+
+
+def small_case_accuracy(prm, pos, vel, t, steps: int = 1000, report=(100, 500, 1000)) -> dict:
+    """The FP64 GPU step against the CPU oracle over the 1,000 steps: the
+    first step (if any) at which types, surface or Dirichlet flags, or the
+    collision candidate pairs differ, and the pressure / position /
+    velocity differences at the reported steps."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    from oracle import Oracle
+
+    from mps_gb300 import FP64, Engine
+
+    e = Engine(prm, pos, vel, t, precision=FP64)
+    o = Oracle(prm, pos, vel, t)
+    o.set_cg(solves=1)  # the second solve repeats the first exactly
+    first_diff = {"flags": None, "collisions": None}
+    at = {}
+    n_coll = 0
+    for s in range(1, steps + 1):
+        e.step()
+        o.step()
+        ci, cj, _ = e.collisions()
+        oi, oj, _ = o.collisions()
+        n_coll += len(oi)
+        if first_diff["collisions"] is None and not (np.array_equal(ci, oi) and np.array_equal(cj, oj)):
+            first_diff["collisions"] = s
+        a, b = e.state(), o.state()
+        if first_diff["flags"] is None and not all(np.array_equal(a[k], b[k]) for k in ("type", "bc", "dirichlet")):
+            first_diff["flags"] = s
+        if s in report:
+            pb = np.linalg.norm(b["pressure"]) or 1.0
+            at[str(s)] = {"pressure_rel_l2": float(np.linalg.norm(a["pressure"] - b["pressure"]) / pb),
+                          "position_max_abs_m": float(np.max(np.abs(a["pos"] - b["pos"]))),
+                          "velocity_max_abs_mps": float(np.max(np.abs(a["vel"] - b["vel"]))),
+                          "ghosts": int(np.sum(a["type"] == -1))}
+    e.close()
+    o.close()
+    return {"steps": steps, "first_step_flags_differ": first_diff["flags"],
+            "first_step_collisions_differ": first_diff["collisions"],
+            "collision_candidates_total": n_coll, "at_step": at}
 
 # ---------------------------------------------------------------- GPU arm
 def run_ours(args, rank: int, world: int, dist):
@@ -404,6 +597,12 @@ def run_ours(args, rank: int, world: int, dist):
     n = len(types)
     nf = int((types == 0).sum())
     prec = MIXED if args.precision == "mixed" else FP64
+    # the CPU baseline on this workload runs on the host cores meanwhile
+    cpu_job = None
+    if rank == 0 and not args.no_cpu:
+        cpu_job = start_cpu_1m(args.warmup, [(None, 2, "reference_eps_two_solves"),
+                                             (1e-10, 1, "gpu_tolerance_1e-10_one_solve")],
+                               args.workload)
 
     def timed(eng, k):
         stream = torch.cuda.ExternalStream(eng.stream_ptr())
@@ -476,6 +675,14 @@ def run_ours(args, rank: int, world: int, dist):
         ea.close()
         eb.close()
 
+    # config 2's own window: mixed against FP64 over 500 steps from rest
+    traj = None
+    if prec == MIXED and not args.no_fp64 and args.trajectory_steps > 0:
+        traj = run_accuracy_trajectory(prm, pos, vel, types, steps=args.trajectory_steps)
+    split = None
+    if prec == MIXED and not args.no_fp64:
+        split = run_precision_split(prm, warm_state)
+
     # end to end through the C ABI with host buffers, every step
     e2e = None
     if not args.no_e2e:
@@ -504,7 +711,7 @@ def run_ours(args, rank: int, world: int, dist):
 
     others = {}
     if not args.no_others and world == 1:  # single-GPU runs only: keeps scaling runs short
-        others["batched"] = run_batched(steps=10, warmup=3)
+        others["batched"] = run_batched(steps=300, warmup=3)
         others["adjoint"] = run_adjoint()
         others["fp64_2m"] = run_fp64_2m(steps=3)
         others["small_case"] = run_small_case()
@@ -513,9 +720,9 @@ def run_ours(args, rank: int, world: int, dist):
     if rank != 0:
         return None
     cpu = None
-    if not args.no_cpu:
+    if cpu_job is not None:
         try:
-            cpu = cpu_sample()
+            cpu = finish_cpu_1m(*cpu_job)
         except Exception as ex:  # reported, not hidden
             cpu = {"value": None, "error": str(ex)[-300:]}
     mean = lambda k: float(np.mean([s[k] for s in stats]))  # noqa
@@ -524,35 +731,42 @@ def run_ours(args, rank: int, world: int, dist):
         "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32-krylov/fp64" if prec == MIXED else "f64",
         "data": "synthetic (seeded lattice dam break, the reference generator's layout)",
-        "config": {"workload": f"{args.workload}: dam break, {nf} fluid / {n} particles, "
-                               f"dt {prm['dt']}, {args.precision} PPE solver",
-                   "particles": n, "fluid_particles": nf, "precision": args.precision,
-                   "cache": "working set > L2 (state + neighbour lists + matrix ~ GBs per step)",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(args.workload, prm, nf, n),
+        "solver": f"{args.precision} PPE solver", "parallelism": f"replicas x{world}",
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "cuda_graph_steps": int(sum(s["graph_replayed"] for s in stats)),
         "cg_iterations_mean": mean("cg_iterations"), "refinements_mean": mean("refinements"),
         "ms_solve_mean": mean("ms_solve"),
         "roofline": roofline, "fp64": fp64,
         "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
-        "accuracy": acc, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+        "accuracy": acc, "accuracy_trajectory": traj, "precision_split": split,
+        "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
         "other_workloads": others or None,
     }
     return line
 
 
 def run_reference(args, rank: int):
+    """The reference's algorithm on the host cores (the CPU oracle: the
+    reference's own sources need Eigen, absent here), on this arm's workload:
+    W warm-up steps with the CG capped, then one full step as the reference
+    runs it (CG to machine epsilon, solved twice).  One step of the 1M scene
+    takes minutes, so one step is the timed sample whatever --steps says."""
     if rank != 0:
         return None
-    per = []
-    for _ in range(args.warmup if args.warmup < 1 else 0):
-        pass
-    cpu = cpu_sample(steps=max(1, args.steps // 5) + 1)
-    per.append(cpu["value"])
-    return {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{args.workload} (CPU sample: {CPU_SAMPLE})"},
+    prm, pos, vel, types = workload(args.workload)
+    nf, n = int((types == 0).sum()), len(types)
+    proc, threads = start_cpu_1m(args.warmup, [(None, 2, "reference_eps_two_solves")], args.workload,
+                                 threads=os.cpu_count() or 1)
+    cpu = finish_cpu_1m(proc, threads)
+    cfg = workload_config(args.workload, prm, nf, n)
+    leg = cpu["legs"]["reference_eps_two_solves"]
+    return {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": 1, "steps_requested": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * leg["seconds_per_step"], "higher_is_better": True, "impl": "reference",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+            "solver": "FP64 Jacobi CG to machine epsilon, solved twice (the reference's), on the CPU",
+            "parallelism": f"{threads} host threads (OpenMP where the reference has it)",
             "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -568,6 +782,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--trajectory-steps", type=int, default=500,
+                    help="mixed vs FP64 accuracy window (0: skip)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-others", action="store_true",

@@ -616,7 +616,8 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
             size_t cells = (size_t)nx * ny;
             if (e->alloc(&g.lev[l].st, 9 * cells) || e->alloc(&g.lev[l].invd, cells) ||
                 e->alloc(&g.lev[l].r, cells) || e->alloc(&g.lev[l].e, cells) ||
-                e->alloc(&g.lev[l].t, cells) || (l >= 2 && e->alloc(&g.lev[l].rw, 16 * cells)))
+                e->alloc(&g.lev[l].t, cells) || e->alloc(&g.lev[l].act, cells) ||
+                (l >= 2 && e->alloc(&g.lev[l].rw, 16 * cells)))
                 return bail(fail(MPS_ERR_CUDA, "cudaMalloc multigrid level"));
             if (cells <= (size_t)kMgMaxCoarsest || l == kMgMaxLevels - 1) break;
             nx = (nx + 1) / 2;
@@ -629,7 +630,8 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         while (g.ngrid + 1 < g.nlev && (size_t)g.lev[g.ngrid + 1].nx * g.lev[g.ngrid + 1].ny > kMgBlockCells)
             g.ngrid++;
         if (e->alloc(&g.e0, np) || e->alloc(&g.res0, np) ||
-            e->alloc(&g.dense, (size_t)kMgMaxCoarsest * kMgMaxCoarsest) || e->alloc(&g.rowcell, 9 * np))
+            e->alloc(&g.dense, (size_t)kMgMaxCoarsest * kMgMaxCoarsest) || e->alloc(&g.rowcell, 9 * np) ||
+            e->alloc(&g.nact, kMgMaxLevels))
             return bail(fail(MPS_ERR_CUDA, "cudaMalloc multigrid"));
         g.n_pad = (int32_t)np;
     }

@@ -216,6 +216,11 @@ struct MgLevel {
     // residuals after one Jacobi step from zero, folded into one 4x4 stencil
     // on the finer residual alone
     float* rw;
+    // the cells with unknowns (invd > 0), listed by the setup in warp-sized
+    // runs of ascending index; Mg::nact[l] of them.  The grid-wide phases of
+    // the cycle visit only these: every other cell holds 0 in r, e and t
+    // (cleared by the setup), which is what the full loops used to write
+    int32_t* act;
 };
 struct Mg {
     int32_t enabled;
@@ -243,6 +248,7 @@ struct Mg {
     // slot's own, entry d = (dx+1)*3 + (dy+1), diagonal included (9 x n_pad)
     float* rowcell;
     int32_t n_pad;
+    int32_t* nact;  // per level: the length of lev[l].act (device, written by the setup)
 };
 
 // --------------------------------------------------------------- solver.cu

@@ -25,7 +25,37 @@ __device__ __forceinline__ void add_tap(float (&st)[9], int d, float v) {
     for (int q = 0; q < 9; q++) st[q] += q == d ? v : 0.f;
 }
 
-__global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L) {
+// Appends cell I to the level's list of cells with unknowns: one atomic per
+// warp, the warp's cells in ascending order.
+__device__ __forceinline__ void list_active(bool act, int I, int32_t* list, int32_t* count) {
+    const unsigned am = __activemask();
+    const unsigned m = __ballot_sync(am, act);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(am, base, leader);
+    if (act) list[base + __popc(m & ((1u << lane) - 1u))] = I;
+}
+
+// Every cell's r, e and t to 0 on the levels the grid-wide phases visit by
+// list (levels 1 .. ngrid + 1), and the list lengths to 0.
+__global__ void k_mg_clear(Mg mg) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    if (t < kMgMaxLevels) mg.nact[t] = 0;
+    for (int l = 1; l <= mg.ngrid + 1 && l <= mg.nlev; l++) {
+        const MgLevel& L = mg.lev[l];
+        const int n = L.nx * L.ny;
+        for (int I = t; I < n; I += nt) {
+            L.r[I] = 0.f;
+            L.e[I] = 0.f;
+            L.t[I] = 0.f;
+        }
+    }
+}
+
+__global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L, int32_t* nact) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= L.nx * L.ny) return;
     const int cx = I / L.ny, cy = I - cx * L.ny;
@@ -90,6 +120,7 @@ __global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L) {
 #pragma unroll
     for (int d = 0; d < 9; d++) L.st[(size_t)d * n + I] = st[d];
     L.invd[I] = st[4] > 0.f ? 1.f / st[4] : 0.f;
+    list_active(st[4] > 0.f, I, L.act, nact + 1);
 }
 
 // Smoothed transfer: B = A P1 per slot (the row's sums over the 3x3 cells
@@ -162,7 +193,7 @@ __global__ void k_mg_rowcell(Consts c, Ppe A, MatFree mf, size_t np, float* __re
 // omega invd_j r_j (one Jacobi step from zero on F, then its residual);
 // summed over the 2x2 children it is a fixed 4x4 stencil on r_F, whose
 // weights depend only on the operator and omega.
-__global__ void k_mg_coarsen(MgLevel F, MgLevel C, float omega) {
+__global__ void k_mg_coarsen(MgLevel F, MgLevel C, float omega, int32_t* nact_c) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int nc = C.nx * C.ny;
     if (I >= nc) return;
@@ -192,6 +223,7 @@ __global__ void k_mg_coarsen(MgLevel F, MgLevel C, float omega) {
 #pragma unroll
     for (int d = 0; d < 9; d++) C.st[(size_t)d * nc + I] = st[d];
     C.invd[I] = st[4] > 0.f ? 1.f / st[4] : 0.f;
+    list_active(st[4] > 0.f, I, C.act, nact_c);
 #pragma unroll
     for (int k = 0; k < 16; k++) C.rw[(size_t)k * nc + I] = w[k];
 }
@@ -247,11 +279,12 @@ void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg&
         ++g_launches;
     }
     const MgLevel& L1 = mg.lev[1];
-    k_mg_level1<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(c, A, mf, L1);
-    ++g_launches;
+    k_mg_clear<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(mg);
+    k_mg_level1<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(c, A, mf, L1, mg.nact);
+    g_launches += 2;
     for (int l = 1; l < mg.nlev; l++) {
         const MgLevel& C = mg.lev[l + 1];
-        k_mg_coarsen<<<(C.nx * C.ny + T - 1) / T, T, 0, st>>>(mg.lev[l], C, mg.omega);
+        k_mg_coarsen<<<(C.nx * C.ny + T - 1) / T, T, 0, st>>>(mg.lev[l], C, mg.omega, mg.nact + l + 1);
         ++g_launches;
     }
     k_mg_dense<<<1, 1024, 0, st>>>(mg.lev[mg.nlev], mg.dense);

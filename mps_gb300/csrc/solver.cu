@@ -140,12 +140,16 @@ __device__ __forceinline__ bool grid_sync(GridBar& gb, DevStats* ds) {
 // in block order, so all blocks hold bitwise the same totals.  Partials are
 // double-buffered so that a fast block's next reduction never overwrites
 // values a slow block is still reading.
+// The two halves of that: publish_partials reduces the block's M values
+// and writes its partials into the next buffer (returned); sum_partials,
+// after a grid barrier that every block passed after publishing, sums the
+// partials in block order.  Between the two any number of phases and
+// barriers may run (the pipelined solve overlaps its reduction with the
+// preconditioner that way).
 template <int M, int BS>
-__device__ __forceinline__ bool reduce_sync(GridBar& gb, const double (&v)[M], double (&tot)[M],
-                                            DevStats* ds) {
+__device__ __forceinline__ const double* publish_partials(GridBar& gb, const double (&v)[M]) {
     constexpr int kW = BS / 32;
     __shared__ double sh[M][BS];
-    __shared__ double s_tot[M];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double* part = gb.partials + (size_t)gb.parity * gb.size * 8;
     gb.parity ^= 1;
@@ -163,7 +167,13 @@ __device__ __forceinline__ bool reduce_sync(GridBar& gb, const double (&v)[M], d
             if (lane == 0) part[gb.rank * 8 + m] = a;
         }
     }
-    if (!grid_sync(gb, ds)) return false;
+    return part;
+}
+
+template <int M>
+__device__ __forceinline__ void sum_partials(const GridBar& gb, const double* part, double (&tot)[M]) {
+    __shared__ double s_tot[M];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (warp == 0) {
 #pragma unroll
         for (int m = 0; m < M; m++) {
@@ -177,6 +187,14 @@ __device__ __forceinline__ bool reduce_sync(GridBar& gb, const double (&v)[M], d
     __syncthreads();
 #pragma unroll
     for (int m = 0; m < M; m++) tot[m] = s_tot[m];
+}
+
+template <int M, int BS>
+__device__ __forceinline__ bool reduce_sync(GridBar& gb, const double (&v)[M], double (&tot)[M],
+                                            DevStats* ds) {
+    const double* part = publish_partials<M, BS>(gb, v);
+    if (!grid_sync(gb, ds)) return false;
+    sum_partials<M>(gb, part, tot);
     return true;
 }
 
@@ -637,21 +655,23 @@ __device__ void mg_block_cycle(Mg& mg, int lo) {
 }
 
 // Level 1 of plain aggregation: the sum over each cell's contiguous slots of
-// src0, pre-smoothed (e = omega invd r).  Four of this thread's cells at
-// once, their slots four at a time, all loads of a round before any use
-// (predicated: slots past a cell's end are not read, which also keeps the
-// many empty cells off any one address): each cell still sums its slots in
-// slot order.  gcell / gsz: this thread's first cell and the group's stride.
+// src0, pre-smoothed (e = omega invd r), for the cells with unknowns (the
+// others hold 0).  Four of this thread's cells at once, their slots four at
+// a time, all loads of a round before any use (predicated: slots past a
+// cell's end are not read): each cell still sums its slots in slot order.
+// gcell / gsz: this thread's first list entry and the group's stride.
 __device__ __forceinline__ void mg_level1_plain(Mg& mg, const MatFree& mf,
                                                 const float* __restrict__ src0, int gcell, int gsz) {
     MgLevel& L1 = mg.lev[1];
-    const int n1 = L1.nx * L1.ny;
-    for (int I0 = gcell; I0 < n1; I0 += 4 * gsz) {
-        int b[4], cnt[4];
+    const int na = __ldg(mg.nact + 1);
+    for (int a0 = gcell; a0 < na; a0 += 4 * gsz) {
+        int b[4], cnt[4], cell[4];
         float iv[4], acc[4];
 #pragma unroll
+        for (int h = 0; h < 4; h++) cell[h] = __ldg(L1.act + min(a0 + h * gsz, na - 1));
+#pragma unroll
         for (int h = 0; h < 4; h++) {
-            const int I = min(I0 + h * gsz, n1 - 1);
+            const int I = cell[h];
             b[h] = __ldg(mf.cs + I);
             cnt[h] = __ldg(mf.cs + I + 1) - b[h];
             iv[h] = __ldg(L1.invd + I);
@@ -672,10 +692,9 @@ __device__ __forceinline__ void mg_level1_plain(Mg& mg, const MatFree& mf,
         }
 #pragma unroll
         for (int h = 0; h < 4; h++) {
-            const int I = I0 + h * gsz;
-            if (I < n1) {
-                L1.r[I] = acc[h];
-                L1.e[I] = mg.omega * iv[h] * acc[h];
+            if (a0 + h * gsz < na) {
+                L1.r[cell[h]] = acc[h];
+                L1.e[cell[h]] = mg.omega * iv[h] * acc[h];
             }
         }
     }
@@ -687,20 +706,25 @@ __device__ __forceinline__ void mg_level1_plain(Mg& mg, const MatFree& mf,
 // group's first block, the grid-wide levels up (prolongation folded into the
 // post-smoothing), each phase closed by a grid barrier of the thread group NT
 // (0: whole blocks).  Afterwards level 1's correction is complete in
-// mg.lev[1].e for every block.
+// mg.lev[1].e for every block.  sync_first = false skips the first barrier
+// where the caller passed one since level 1 was written.
 template <int NT>
-__device__ __forceinline__ bool mg_cell_levels(Mg& mg, GridBar& gb, DevStats* ds, int gcell, int gsz) {
-    if (!grid_sync<NT>(gb, ds)) return false;
+__device__ __forceinline__ bool mg_cell_levels(Mg& mg, GridBar& gb, DevStats* ds, int gcell, int gsz,
+                                               bool sync_first = true) {
+    if (sync_first && !grid_sync<NT>(gb, ds)) return false;
     // grid-wide levels, down: restrict level l into l+1 and pre-smooth there
     // (every level but the coarsest, whose e comes from its dense inverse)
+    // (the cells with unknowns only: the others hold 0)
     for (int l = 1; l <= mg.ngrid; l++) {
         MgLevel& L = mg.lev[l];
         MgLevel& C = mg.lev[l + 1];
         const bool smooth = l + 1 < mg.nlev;
-        for (int I = gcell; I < C.nx * C.ny; I += gsz) {
+        const int na = __ldg(mg.nact + l + 1);
+        for (int a = gcell; a < na; a += gsz) {
+            const int I = __ldg(C.act + a);
             const int X = I / C.ny, Y = I - X * C.ny;
             const float iv = __ldg(C.invd + I);
-            const float rr = iv > 0.f ? restrict_cell(L, C, I, X, Y) : 0.f;
+            const float rr = restrict_cell(L, C, I, X, Y);
             C.r[I] = rr;
             if (smooth) C.e[I] = mg.omega * iv * rr;
         }
@@ -713,8 +737,11 @@ __device__ __forceinline__ bool mg_cell_levels(Mg& mg, GridBar& gb, DevStats* ds
     for (int l = mg.ngrid; l >= 1; l--) {
         MgLevel& L = mg.lev[l];
         MgLevel& C = mg.lev[l + 1];
-        const int nl = L.nx * L.ny;
-        for (int I = gcell; I < nl; I += gsz) L.t[I] = __ldg(L.invd + I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
+        const int na = __ldg(mg.nact + l);
+        for (int a = gcell; a < na; a += gsz) {
+            const int I = __ldg(L.act + a);
+            L.t[I] = smooth_up_cell(mg, L, C, I);
+        }
         if (!grid_sync<NT>(gb, ds)) return false;
         float* tmp = L.e;
         L.e = L.t;

@@ -56,8 +56,9 @@ def test_first_step_bit_exact(name):
 
 # MIXED step 1 against the FP64 goldens (see the test's docstring)
 PM_TOL = 1e-6    # relative L2 of pressure: the mixed solve stops at relative residual 1e-10
-XM_TOL = 1e-10   # metres: the FP32 pressure-gradient sum moves particles by ~1e-12 m
-VM_TOL = 1e-7    # m/s
+XM_TOL = 1e-9    # metres: the FP32 pressure-gradient sum (relative error ~1e-7 of accelerations
+                 # up to ~1e3 m/s^2 in the jittered scenes) moves particles by up to ~1e-10 m per step
+VM_TOL = 1e-6    # m/s
 
 
 @pytest.mark.parametrize("name", CASES)
