@@ -659,9 +659,11 @@ __device__ void mg_block_cycle(Mg& mg, int lo) {
 // others hold 0).  Four of this thread's cells at once, their slots four at
 // a time, all loads of a round before any use (predicated: slots past a
 // cell's end are not read): each cell still sums its slots in slot order.
-// gcell / gsz: this thread's first list entry and the group's stride.
+// gcell / gsz: this thread's first list entry and the group's stride;
+// e_out: the array that receives the pre-smoothing (the cycle's level-1 e).
 __device__ __forceinline__ void mg_level1_plain(Mg& mg, const MatFree& mf,
-                                                const float* __restrict__ src0, int gcell, int gsz) {
+                                                const float* __restrict__ src0, int gcell, int gsz,
+                                                float* __restrict__ e_out) {
     MgLevel& L1 = mg.lev[1];
     const int na = __ldg(mg.nact + 1);
     for (int a0 = gcell; a0 < na; a0 += 4 * gsz) {
@@ -694,9 +696,159 @@ __device__ __forceinline__ void mg_level1_plain(Mg& mg, const MatFree& mf,
         for (int h = 0; h < 4; h++) {
             if (a0 + h * gsz < na) {
                 L1.r[cell[h]] = acc[h];
-                L1.e[cell[h]] = mg.omega * iv[h] * acc[h];
+                e_out[cell[h]] = mg.omega * iv[h] * acc[h];
             }
         }
+    }
+}
+
+// ------------------------------------------ the small levels in shared memory
+// The levels the group's first block runs alone (lo = ngrid + 1 .. nlev) are
+// small (at most kMgBlockCells cells at lo, a quarter of that below), and
+// their stencils do not change during a solve.  Held in block 0's shared
+// memory, a cycle through them costs shared-memory latency instead of L2
+// round trips.  Layout, per level lo..nlev: r, e, t (n floats each); per
+// level lo+1..nlev: 9-point stencil, inverse diagonal, 4x4 restriction
+// weights (26 n floats; level lo's stencil and inverse diagonal stay in
+// global memory); then the coarsest level's dense inverse.
+struct SmemLevels {
+    MgLevel lev[kMgMaxLevels];  // pointers into shared memory (level lo: st, invd global)
+    float* dense;
+};
+
+__host__ __device__ inline size_t block_smem_floats(const Mg& mg, int lo) {
+    size_t f = 0;
+    for (int l = lo; l <= mg.nlev; l++) {
+        const size_t n = (size_t)mg.lev[l].nx * mg.lev[l].ny;
+        f += 3 * n + (l > lo ? 26 * n : 0);
+    }
+    const size_t nc = (size_t)mg.lev[mg.nlev].nx * mg.lev[mg.nlev].ny;
+    return f + nc * nc;
+}
+
+__device__ __forceinline__ void smem_levels_carve(const Mg& mg, int lo, float* base, SmemLevels& S) {
+    float* q = base;
+    for (int l = lo; l <= mg.nlev; l++) {
+        const int n = mg.lev[l].nx * mg.lev[l].ny;
+        MgLevel L = mg.lev[l];
+        L.r = q;
+        L.e = q + n;
+        L.t = q + 2 * n;
+        q += 3 * n;
+        if (l > lo) {
+            L.st = q;
+            L.invd = q + 9 * n;
+            L.rw = q + 10 * n;
+            q += 26 * n;
+        }
+        S.lev[l] = L;
+    }
+    S.dense = q;
+}
+
+// Copies the levels' constant arrays into the layout (once per solve; the
+// calling threads, tid < nt, then meet at a block barrier).
+__device__ void smem_levels_stage(const Mg& mg, int lo, const SmemLevels& S, int tid, int nt) {
+    for (int l = lo + 1; l <= mg.nlev; l++) {
+        const int n = mg.lev[l].nx * mg.lev[l].ny;
+        for (int i = tid; i < 9 * n; i += nt) S.lev[l].st[i] = __ldg(mg.lev[l].st + i);
+        for (int i = tid; i < n; i += nt) S.lev[l].invd[i] = __ldg(mg.lev[l].invd + i);
+        for (int i = tid; i < 16 * n; i += nt) S.lev[l].rw[i] = __ldg(mg.lev[l].rw + i);
+    }
+    const int nc = mg.lev[mg.nlev].nx * mg.lev[mg.nlev].ny;
+    for (int i = tid; i < nc * nc; i += nt) S.dense[i] = __ldg(mg.dense + i);
+}
+
+// restrict_cell and smooth_up_cell on shared-memory levels (plain loads;
+// level lo's stencil is read from global memory by the same plain loads).
+__device__ __forceinline__ float restrict_cell_s(const MgLevel& F, const MgLevel& C, int I, int X, int Y) {
+    const int nc = C.nx * C.ny;
+    int xs[4], ys[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        xs[k] = min(max(2 * X - 1 + k, 0), F.nx - 1) * F.ny;
+        ys[k] = min(max(2 * Y - 1 + k, 0), F.ny - 1);
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; k++) acc = fmaf(C.rw[(size_t)k * nc + I], F.r[xs[k >> 2] + ys[k & 3]], acc);
+    return acc;
+}
+
+__device__ __forceinline__ float smooth_up_cell_s(const Mg& mg, const MgLevel& L, const MgLevel& C, int I) {
+    const int n = L.nx * L.ny;
+    const int x = I / L.ny, y = I - x * L.ny;
+    const float ei = fmaf(mg.scale, C.e[(x / 2) * C.ny + y / 2], L.e[I]);
+    float acc = 0.f;
+#pragma unroll
+    for (int d = 0; d < 9; d++) {
+        bool ok;
+        const int j = tap(L, x, y, d, ok);
+        const int jx = j / L.ny, jy = j - jx * L.ny;
+        const float ej = fmaf(mg.scale, C.e[(jx / 2) * C.ny + jy / 2], L.e[j]);
+        if (ok) acc = fmaf(L.st[(size_t)d * n + I], ej, acc);
+    }
+    return fmaf(mg.omega * L.invd[I], L.r[I] - acc, ei);
+}
+
+// The small levels' cycle of mg_block_cycle, in shared memory: level lo's
+// residual and pre-smoothing come in from global memory, its correction goes
+// back to mg.lev[lo].e, where the grid-wide up pass reads it.  The thread
+// group NT of block 0 runs it.
+template <int NT>
+__device__ void mg_block_cycle_smem(const Mg& mg, int lo, const SmemLevels& S0) {
+    const int tid = threadIdx.x, nt = NT == 0 ? (int)blockDim.x : NT;
+    MgLevel v[kMgMaxLevels];
+    for (int l = lo; l <= mg.nlev; l++) v[l] = S0.lev[l];
+    v[lo].st = mg.lev[lo].st;
+    v[lo].invd = mg.lev[lo].invd;
+    {
+        const int n = v[lo].nx * v[lo].ny;
+        for (int i = tid; i < n; i += nt) {
+            v[lo].r[i] = __ldcg(mg.lev[lo].r + i);
+            v[lo].e[i] = __ldcg(mg.lev[lo].e + i);
+        }
+        group_bar<NT>();
+    }
+    for (int l = lo; l < mg.nlev; l++) {
+        const MgLevel& L = v[l];
+        MgLevel& C = v[l + 1];
+        const bool smooth = l + 1 < mg.nlev;
+        for (int I = tid; I < C.nx * C.ny; I += nt) {
+            const int X = I / C.ny, Y = I - X * C.ny;
+            const float iv = C.invd[I];
+            const float rr = iv > 0.f ? restrict_cell_s(L, C, I, X, Y) : 0.f;
+            C.r[I] = rr;
+            if (smooth) C.e[I] = mg.omega * iv * rr;
+        }
+        group_bar<NT>();
+    }
+    {
+        MgLevel& L = v[mg.nlev];
+        const int n = L.nx * L.ny;
+        const int lane = tid & 31;
+        // a hierarchy whose first block level is the coarsest hands its
+        // correction straight to global memory
+        float* eout = mg.nlev == lo ? mg.lev[lo].e : L.e;
+        for (int i = tid >> 5; i < n; i += nt >> 5) {
+            float acc = 0.f;
+            for (int j = lane; j < n; j += 32) acc = fmaf(S0.dense[i * n + j], L.r[j], acc);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) eout[i] = L.invd[i] > 0.f ? acc : 0.f;
+        }
+        group_bar<NT>();
+    }
+    for (int l = mg.nlev - 1; l >= lo; l--) {
+        MgLevel& L = v[l];
+        const MgLevel& C = v[l + 1];
+        const int n = L.nx * L.ny;
+        float* out = l == lo ? mg.lev[lo].e : L.t;
+        for (int I = tid; I < n; I += nt) out[I] = L.invd[I] > 0.f ? smooth_up_cell_s(mg, L, C, I) : 0.f;
+        group_bar<NT>();
+        float* tmp = L.e;
+        L.e = L.t;
+        L.t = tmp;
     }
 }
 
@@ -710,7 +862,7 @@ __device__ __forceinline__ void mg_level1_plain(Mg& mg, const MatFree& mf,
 // where the caller passed one since level 1 was written.
 template <int NT>
 __device__ __forceinline__ bool mg_cell_levels(Mg& mg, GridBar& gb, DevStats* ds, int gcell, int gsz,
-                                               bool sync_first = true) {
+                                               bool sync_first = true, const SmemLevels* S = nullptr) {
     if (sync_first && !grid_sync<NT>(gb, ds)) return false;
     // grid-wide levels, down: restrict level l into l+1 and pre-smooth there
     // (every level but the coarsest, whose e comes from its dense inverse)
@@ -731,7 +883,12 @@ __device__ __forceinline__ bool mg_cell_levels(Mg& mg, GridBar& gb, DevStats* ds
         if (!grid_sync<NT>(gb, ds)) return false;
     }
     // small levels in the group's first block
-    if (gb.rank == 0) mg_block_cycle<NT>(mg, mg.ngrid + 1);
+    if (gb.rank == 0) {
+        if (S)
+            mg_block_cycle_smem<NT>(mg, mg.ngrid + 1, *S);
+        else
+            mg_block_cycle<NT>(mg, mg.ngrid + 1);
+    }
     if (!grid_sync<NT>(gb, ds)) return false;
     // grid-wide levels, up: prolongation folded into the post-smoothing
     for (int l = mg.ngrid; l >= 1; l--) {
@@ -845,7 +1002,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
             L1.e[I] = mg.omega * iv * rr;
         }
     } else {
-        mg_level1_plain(mg, mf, src0, gcell, gsz);
+        mg_level1_plain(mg, mf, src0, gcell, gsz, mg.lev[1].e);
     }
     if (!mg_cell_levels<0>(mg, gb, ds, gcell, gsz)) return false;
     if (mg.additive && mg.smooth) {
@@ -1152,11 +1309,15 @@ __global__ void __launch_bounds__(kMixedBlock, 1) k_cg_mixed(Ppe A, MatFree mf, 
 //
 // Rows of block b: the 32-row slices b, b + G, b + 2G, ... (G blocks).
 constexpr int kCycleThreads = 512;
+// Upper bound of the shared-memory copy of the small levels (beside the
+// kernel's 33 KB of static shared memory); larger hierarchies keep them in
+// global memory.
+constexpr int kBlockSmemCap = 100 * 1024;
 
 template <int BS, int NV>
 __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree& mf, Mg& mg,
                                                     const Krylov& kv, const SolveArgs& a, DevStats* ds,
-                                                    GridBar& gb) {
+                                                    GridBar& gb, float* dsm) {
     if (*(volatile int32_t*)&ds->status & ST_ASYMMETRIC) {  // the reference exits here
         if (gb.rank == 0 && threadIdx.x == 0) {
             ds->cg_iterations = 0;
@@ -1180,6 +1341,18 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
     const int NY = mg.lev[1].ny, n1 = mg.lev[1].nx * NY;
     __shared__ float* s_e1;
     __shared__ int s_cycle_ok;
+    // level 1's e as the cycle group sees it (its copy swaps e and t each
+    // cycle); the level-1 sums of all warps write there
+    if (tid == 0) s_e1 = mg.lev[1].e;
+    // the small levels in block 0's shared memory (staged once per solve;
+    // the first reduction's barriers order it before any cycle)
+    SmemLevels sl;
+    const SmemLevels* slp = nullptr;
+    if (mg.block_smem > 0) {
+        smem_levels_carve(mg, mg.ngrid + 1, dsm, sl);
+        slp = &sl;
+        if (b == 0) smem_levels_stage(mg, mg.ngrid + 1, sl, tid, BS);
+    }
 
     double acc[1] = {0.0}, tot[1];
     for (int sl = gwarp; sl < nsl; sl += nwarps) {
@@ -1223,11 +1396,15 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
         float alpha = 0.f, beta = 0.f, gamma_old = 1.f;
         int64_t k = 0;
         for (;;) {
-            // ---- split: the cycle on r, the operator on y
+            // ---- level 1 of the cycle: every warp sums r over the cells with
+            // unknowns (before the split, while nothing else streams), into
+            // the cycle group's level-1 arrays
+            mg_level1_plain(mg, mf, kv.r32, ((warp * G + b) << 5) + lane, gsz, s_e1);
+            if (!grid_sync(gb, ds)) return;
+            // ---- split: the cycle's cell levels on r, the operator on y
             if (warp < kVW) {
                 const int gcell = ((warp * G + b) << 5) + lane;
-                mg_level1_plain(mg, mf, kv.r32, gcell, G * NV);
-                const bool ok = mg_cell_levels<NV>(mg, gb, ds, gcell, G * NV);
+                const bool ok = mg_cell_levels<NV>(mg, gb, ds, gcell, G * NV, false, slp);
                 if (tid == 0) {
                     s_e1 = mg.lev[1].e;
                     s_cycle_ok = ok;
@@ -1365,8 +1542,9 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
 
 __global__ void __launch_bounds__(kMixedBlock, 1) k_cg_mixed_ov(Ppe A, MatFree mf, Mg mg, Krylov kv,
                                                                 SolveArgs a, DevStats* ds) {
+    extern __shared__ float dsm[];
     GridBar gb = whole_grid(kv);
-    solve_mixed_overlap<kMixedBlock, kCycleThreads>(A, mf, mg, kv, a, ds, gb);
+    solve_mixed_overlap<kMixedBlock, kCycleThreads>(A, mf, mg, kv, a, ds, gb, dsm);
 }
 
 // Many scenes in one persistent launch: block b belongs to group bmap[b].x
@@ -1470,6 +1648,24 @@ void solver_setup(Krylov& k, int32_t /*n_pad*/, int device) {
     int g3 = coop_grid((const void*)k_cg_mixed_ov, device, kMixedBlock, 0, 1);
     k.grid = std::min({g1, g2, g3});
     k.block = kBlock;
+}
+
+int mg_block_smem_bytes(const Mg& mg) {
+    if (!mg.enabled || mg.ngrid + 1 > mg.nlev) return 0;
+    const size_t bytes = 4 * block_smem_floats(mg, mg.ngrid + 1);
+    if (bytes > (size_t)kBlockSmemCap) return 0;
+    // the overlapped solve kernel may take that much dynamic shared memory
+    // (the largest request so far stays set: every engine of the process fits)
+    static int granted = 0;
+    if ((int)bytes > granted) {
+        if (cudaFuncSetAttribute((const void*)k_cg_mixed_ov, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        granted = (int)bytes;
+    }
+    return (int)bytes;
 }
 
 void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, MatFree& mf,
@@ -1650,8 +1846,9 @@ void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const 
     Krylov kk = k;
     void* args[] = {&AA, &mm, &gg, &kk, &a, &ds};
     cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
-    const void* fn = mg.enabled && mg.overlap ? (const void*)k_cg_mixed_ov : (const void*)k_cg_mixed;
-    cudaLaunchCooperativeKernel(fn, dim3(k.grid), dim3(kMixedBlock), args, 0, st);
+    const bool ov = mg.enabled && mg.overlap;
+    const void* fn = ov ? (const void*)k_cg_mixed_ov : (const void*)k_cg_mixed;
+    cudaLaunchCooperativeKernel(fn, dim3(k.grid), dim3(kMixedBlock), args, ov ? (size_t)mg.block_smem : 0, st);
     ++g_launches;
 }
 
