@@ -586,18 +586,56 @@ __device__ __forceinline__ float smooth_up_cell(const Mg& mg, const MgLevel& L, 
     return fmaf(mg.omega * iv, ri - acc, ei);
 }
 
+// ------------------------------------------------------------ level views
+// The hierarchy descriptor (Mg) stays where the launch put it, in read-only
+// kernel parameter space: no thread keeps a copy of it.  Each up-smoothing of
+// a grid-wide level writes the level's t array, after which the roles of e
+// and t swap; a thread tracks the swaps of levels 1..ngrid in a bit mask
+// (bit l set: e and t exchanged), the same in every thread that runs the
+// cycle.  The first level the block cycle runs, lo = ngrid + 1, never swaps:
+// its pre-smoothing is in e, the correction the block cycle hands back in t.
+// The levels below lo belong to the block cycle and start from their base
+// roles in every cycle.
+__device__ __forceinline__ MgLevel lev_view(const Mg& mg, int l, uint32_t swp) {
+    MgLevel L = mg.lev[l];
+    if ((swp >> l) & 1u) {
+        float* t = L.e;
+        L.e = L.t;
+        L.t = t;
+    }
+    return L;
+}
+
+// Level lo as the coarse level of the up pass at level ngrid: e = its correction.
+__device__ __forceinline__ MgLevel lo_corrected(const Mg& mg) {
+    MgLevel L = mg.lev[mg.ngrid + 1];
+    L.e = L.t;
+    return L;
+}
+
+// Level 1's correction after a cycle, and the array that takes its next
+// pre-smoothing (the same array once level 1 is grid-wide: the correction is
+// consumed first).
+__device__ __forceinline__ float* level1_correction(const Mg& mg, uint32_t swp) {
+    return mg.ngrid >= 1 ? lev_view(mg, 1, swp).e : mg.lev[1].t;
+}
+__device__ __forceinline__ float* level1_presmooth(const Mg& mg, uint32_t swp) {
+    return lev_view(mg, 1, swp).e;
+}
+
 // Levels lo..nlev of the V-cycle, run by the group's first block alone (they
 // are small): down smoothing + restriction, the dense coarsest solve, up
-// smoothing with the prolongation folded in.  Only block-level barriers of the group NT inside; the
-// caller brackets it with grid barriers.  `lv` are this block's views of the
-// levels (their e/t roles swap after each up-smoothing).
+// smoothing with the prolongation folded in.  Only block-level barriers of
+// the group NT inside; the caller brackets it with grid barriers.  Level lo's
+// r and pre-smoothing were written by the grid pass; its correction goes to
+// its t array.
 template <int NT>
-__device__ void mg_block_levels(const Mg& mg, int lo, MgLevel* lv) {
+__device__ void mg_block_cycle(const Mg& mg, int lo) {
     const int tid = threadIdx.x, nt = NT == 0 ? (int)blockDim.x : NT;
-    // level lo's r and pre-smoothed e are already written (by the grid pass)
+    uint32_t bsw = 0;  // role swaps of the levels below lo in this cycle
     for (int l = lo; l < mg.nlev; l++) {
-        const MgLevel& L = lv[l];
-        MgLevel& C = lv[l + 1];
+        const MgLevel L = l == lo ? mg.lev[lo] : lev_view(mg, l, bsw);
+        const MgLevel C = lev_view(mg, l + 1, bsw);
         const bool smooth = l + 1 < mg.nlev;
         for (int I = tid; I < C.nx * C.ny; I += nt) {
             const int X = I / C.ny, Y = I - X * C.ny;
@@ -610,7 +648,8 @@ __device__ void mg_block_levels(const Mg& mg, int lo, MgLevel* lv) {
     }
     {
         // coarsest level: e = A_c^-1 r, one warp per row (lanes split the row)
-        MgLevel& L = lv[mg.nlev];
+        const MgLevel L = lev_view(mg, mg.nlev, bsw);
+        float* out = mg.nlev == lo ? L.t : L.e;
         const int n = L.nx * L.ny;
         const int lane = tid & 31;
         for (int i = tid >> 5; i < n; i += nt >> 5) {
@@ -618,39 +657,17 @@ __device__ void mg_block_levels(const Mg& mg, int lo, MgLevel* lv) {
             for (int j = lane; j < n; j += 32) acc = fmaf(__ldg(mg.dense + i * n + j), ldv(L.r, j), acc);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) L.e[i] = ldc(L.invd, i) > 0.f ? acc : 0.f;
+            if (lane == 0) out[i] = ldc(L.invd, i) > 0.f ? acc : 0.f;
         }
         group_bar<NT>();
     }
     for (int l = mg.nlev - 1; l >= lo; l--) {
-        MgLevel& L = lv[l];
-        MgLevel& C = lv[l + 1];
+        const MgLevel L = l == lo ? mg.lev[lo] : lev_view(mg, l, bsw);
+        const MgLevel C = lev_view(mg, l + 1, bsw);
         const int n = L.nx * L.ny;
         for (int I = tid; I < n; I += nt) L.t[I] = ldc(L.invd, I) > 0.f ? smooth_up_cell(mg, L, C, I) : 0.f;
         group_bar<NT>();
-        // the views are this block's own: swap instead of copying
-        float* tmp = L.e;
-        L.e = L.t;
-        L.t = tmp;
-    }
-}
-
-template <int NT>
-__device__ void mg_block_cycle(Mg& mg, int lo) {
-    const int tid = threadIdx.x, nt = NT == 0 ? (int)blockDim.x : NT;
-    MgLevel v[kMgMaxLevels];
-    for (int l = lo; l <= mg.nlev; l++) v[l] = mg.lev[l];
-    mg_block_levels<NT>(mg, lo, v);
-    // after the swap level lo's correction sits in its t array: copy it to
-    // e, where every block reads it
-    const int nlo = v[lo].nx * v[lo].ny;
-    if (v[lo].e != mg.lev[lo].e)
-        for (int i = tid; i < nlo; i += nt) mg.lev[lo].e[i] = __ldcg(v[lo].e + i);
-    group_bar<NT>();
-    // levels above lo keep their swapped roles in this block's copy
-    for (int l = lo + 1; l <= mg.nlev; l++) {
-        mg.lev[l].e = v[l].e;
-        mg.lev[l].t = v[l].t;
+        if (l > lo) bsw ^= 1u << l;
     }
 }
 
@@ -660,11 +677,11 @@ __device__ void mg_block_cycle(Mg& mg, int lo) {
 // a time, all loads of a round before any use (predicated: slots past a
 // cell's end are not read): each cell still sums its slots in slot order.
 // gcell / gsz: this thread's first list entry and the group's stride;
-// e_out: the array that receives the pre-smoothing (the cycle's level-1 e).
-__device__ __forceinline__ void mg_level1_plain(Mg& mg, const MatFree& mf,
+// e_out: the array that receives the pre-smoothing (level1_presmooth).
+__device__ __forceinline__ void mg_level1_plain(const Mg& mg, const MatFree& mf,
                                                 const float* __restrict__ src0, int gcell, int gsz,
                                                 float* __restrict__ e_out) {
-    MgLevel& L1 = mg.lev[1];
+    const MgLevel& L1 = mg.lev[1];
     const int na = __ldg(mg.nact + 1);
     for (int a0 = gcell; a0 < na; a0 += 4 * gsz) {
         int b[4], cnt[4], cell[4];
@@ -711,11 +728,6 @@ __device__ __forceinline__ void mg_level1_plain(Mg& mg, const MatFree& mf,
 // level lo+1..nlev: 9-point stencil, inverse diagonal, 4x4 restriction
 // weights (26 n floats; level lo's stencil and inverse diagonal stay in
 // global memory); then the coarsest level's dense inverse.
-struct SmemLevels {
-    MgLevel lev[kMgMaxLevels];  // pointers into shared memory (level lo: st, invd global)
-    float* dense;
-};
-
 __host__ __device__ inline size_t block_smem_floats(const Mg& mg, int lo) {
     size_t f = 0;
     for (int l = lo; l <= mg.nlev; l++) {
@@ -726,37 +738,39 @@ __host__ __device__ inline size_t block_smem_floats(const Mg& mg, int lo) {
     return f + nc * nc;
 }
 
-__device__ __forceinline__ void smem_levels_carve(const Mg& mg, int lo, float* base, SmemLevels& S) {
+// Level l's arrays in the layout (base roles: r, e, t in that order).
+__device__ __forceinline__ MgLevel smem_view(const Mg& mg, int lo, float* base, int l) {
     float* q = base;
-    for (int l = lo; l <= mg.nlev; l++) {
-        const int n = mg.lev[l].nx * mg.lev[l].ny;
-        MgLevel L = mg.lev[l];
-        L.r = q;
-        L.e = q + n;
-        L.t = q + 2 * n;
-        q += 3 * n;
-        if (l > lo) {
-            L.st = q;
-            L.invd = q + 9 * n;
-            L.rw = q + 10 * n;
-            q += 26 * n;
-        }
-        S.lev[l] = L;
+    for (int k = lo; k < l; k++) {
+        const int nk = mg.lev[k].nx * mg.lev[k].ny;
+        q += 3 * nk + (k > lo ? 26 * nk : 0);
     }
-    S.dense = q;
+    MgLevel L = mg.lev[l];
+    const int n = L.nx * L.ny;
+    L.r = q;
+    L.e = q + n;
+    L.t = q + 2 * n;
+    if (l > lo) {
+        L.st = q + 3 * n;
+        L.invd = q + 12 * n;
+        L.rw = q + 13 * n;
+    }
+    return L;
 }
 
 // Copies the levels' constant arrays into the layout (once per solve; the
 // calling threads, tid < nt, then meet at a block barrier).
-__device__ void smem_levels_stage(const Mg& mg, int lo, const SmemLevels& S, int tid, int nt) {
+__device__ void smem_levels_stage(const Mg& mg, int lo, float* base, int tid, int nt) {
     for (int l = lo + 1; l <= mg.nlev; l++) {
-        const int n = mg.lev[l].nx * mg.lev[l].ny;
-        for (int i = tid; i < 9 * n; i += nt) S.lev[l].st[i] = __ldg(mg.lev[l].st + i);
-        for (int i = tid; i < n; i += nt) S.lev[l].invd[i] = __ldg(mg.lev[l].invd + i);
-        for (int i = tid; i < 16 * n; i += nt) S.lev[l].rw[i] = __ldg(mg.lev[l].rw + i);
+        const MgLevel S = smem_view(mg, lo, base, l);
+        const int n = S.nx * S.ny;
+        for (int i = tid; i < 9 * n; i += nt) S.st[i] = __ldg(mg.lev[l].st + i);
+        for (int i = tid; i < n; i += nt) S.invd[i] = __ldg(mg.lev[l].invd + i);
+        for (int i = tid; i < 16 * n; i += nt) S.rw[i] = __ldg(mg.lev[l].rw + i);
     }
     const int nc = mg.lev[mg.nlev].nx * mg.lev[mg.nlev].ny;
-    for (int i = tid; i < nc * nc; i += nt) S.dense[i] = __ldg(mg.dense + i);
+    float* dense = base + (block_smem_floats(mg, lo) - (size_t)nc * nc);
+    for (int i = tid; i < nc * nc; i += nt) dense[i] = __ldg(mg.dense + i);
 }
 
 // restrict_cell and smooth_up_cell on shared-memory levels (plain loads;
@@ -791,28 +805,37 @@ __device__ __forceinline__ float smooth_up_cell_s(const Mg& mg, const MgLevel& L
     return fmaf(mg.omega * L.invd[I], L.r[I] - acc, ei);
 }
 
-// The small levels' cycle of mg_block_cycle, in shared memory: level lo's
-// residual and pre-smoothing come in from global memory, its correction goes
-// back to mg.lev[lo].e, where the grid-wide up pass reads it.  The thread
-// group NT of block 0 runs it.
+// mg_block_cycle in shared memory: level lo's residual and pre-smoothing come
+// in from global memory, its correction goes back to level lo's t array.
 template <int NT>
-__device__ void mg_block_cycle_smem(const Mg& mg, int lo, const SmemLevels& S0) {
+__device__ void mg_block_cycle_smem(const Mg& mg, int lo, float* base) {
     const int tid = threadIdx.x, nt = NT == 0 ? (int)blockDim.x : NT;
-    MgLevel v[kMgMaxLevels];
-    for (int l = lo; l <= mg.nlev; l++) v[l] = S0.lev[l];
-    v[lo].st = mg.lev[lo].st;
-    v[lo].invd = mg.lev[lo].invd;
+    auto view = [&](int l, uint32_t bsw) {
+        MgLevel L = smem_view(mg, lo, base, l);
+        if (l == lo) {
+            L.st = mg.lev[lo].st;
+            L.invd = mg.lev[lo].invd;
+        }
+        if ((bsw >> l) & 1u) {
+            float* t = L.e;
+            L.e = L.t;
+            L.t = t;
+        }
+        return L;
+    };
+    uint32_t bsw = 0;
     {
-        const int n = v[lo].nx * v[lo].ny;
+        const MgLevel L = view(lo, 0);
+        const int n = L.nx * L.ny;
         for (int i = tid; i < n; i += nt) {
-            v[lo].r[i] = __ldcg(mg.lev[lo].r + i);
-            v[lo].e[i] = __ldcg(mg.lev[lo].e + i);
+            L.r[i] = __ldcg(mg.lev[lo].r + i);
+            L.e[i] = __ldcg(mg.lev[lo].e + i);
         }
         group_bar<NT>();
     }
     for (int l = lo; l < mg.nlev; l++) {
-        const MgLevel& L = v[l];
-        MgLevel& C = v[l + 1];
+        const MgLevel L = view(l, bsw);
+        const MgLevel C = view(l + 1, bsw);
         const bool smooth = l + 1 < mg.nlev;
         for (int I = tid; I < C.nx * C.ny; I += nt) {
             const int X = I / C.ny, Y = I - X * C.ny;
@@ -824,52 +847,52 @@ __device__ void mg_block_cycle_smem(const Mg& mg, int lo, const SmemLevels& S0) 
         group_bar<NT>();
     }
     {
-        MgLevel& L = v[mg.nlev];
+        const MgLevel L = view(mg.nlev, bsw);
         const int n = L.nx * L.ny;
+        const float* dense = base + (block_smem_floats(mg, lo) - (size_t)n * n);
+        float* out = mg.nlev == lo ? mg.lev[lo].t : L.e;
         const int lane = tid & 31;
-        // a hierarchy whose first block level is the coarsest hands its
-        // correction straight to global memory
-        float* eout = mg.nlev == lo ? mg.lev[lo].e : L.e;
         for (int i = tid >> 5; i < n; i += nt >> 5) {
             float acc = 0.f;
-            for (int j = lane; j < n; j += 32) acc = fmaf(S0.dense[i * n + j], L.r[j], acc);
+            for (int j = lane; j < n; j += 32) acc = fmaf(dense[i * n + j], L.r[j], acc);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) eout[i] = L.invd[i] > 0.f ? acc : 0.f;
+            if (lane == 0) out[i] = L.invd[i] > 0.f ? acc : 0.f;
         }
         group_bar<NT>();
     }
     for (int l = mg.nlev - 1; l >= lo; l--) {
-        MgLevel& L = v[l];
-        const MgLevel& C = v[l + 1];
+        const MgLevel L = view(l, bsw);
+        const MgLevel C = view(l + 1, bsw);
         const int n = L.nx * L.ny;
-        float* out = l == lo ? mg.lev[lo].e : L.t;
+        float* out = l == lo ? mg.lev[lo].t : L.t;
         for (int I = tid; I < n; I += nt) out[I] = L.invd[I] > 0.f ? smooth_up_cell_s(mg, L, C, I) : 0.f;
         group_bar<NT>();
-        float* tmp = L.e;
-        L.e = L.t;
-        L.t = tmp;
+        if (l > lo) bsw ^= 1u << l;
     }
 }
 
 // The cell levels of the V-cycle after level 1's residual and pre-smoothing
 // were written: a grid barrier, the grid-wide levels down (restriction
 // fused with the next level's pre-smoothing), the small levels in the
-// group's first block, the grid-wide levels up (prolongation folded into the
-// post-smoothing), each phase closed by a grid barrier of the thread group NT
-// (0: whole blocks).  Afterwards level 1's correction is complete in
-// mg.lev[1].e for every block.  sync_first = false skips the first barrier
-// where the caller passed one since level 1 was written.
+// group's first block (in shared memory from `smem` when given), the
+// grid-wide levels up (prolongation folded into the post-smoothing), each
+// phase closed by a grid barrier of the thread group NT (0: whole blocks).
+// Afterwards level 1's correction is complete for every block
+// (level1_correction).  sync_first = false skips the first barrier where
+// the caller passed one since level 1 was written.  swp: the role swaps.
 template <int NT>
-__device__ __forceinline__ bool mg_cell_levels(Mg& mg, GridBar& gb, DevStats* ds, int gcell, int gsz,
-                                               bool sync_first = true, const SmemLevels* S = nullptr) {
+__device__ __forceinline__ bool mg_cell_levels(const Mg& mg, uint32_t& swp, GridBar& gb, DevStats* ds,
+                                               int gcell, int gsz, bool sync_first = true,
+                                               float* smem = nullptr) {
     if (sync_first && !grid_sync<NT>(gb, ds)) return false;
+    const int lo = mg.ngrid + 1;
     // grid-wide levels, down: restrict level l into l+1 and pre-smooth there
-    // (every level but the coarsest, whose e comes from its dense inverse)
-    // (the cells with unknowns only: the others hold 0)
+    // (every level but the coarsest, whose e comes from its dense inverse),
+    // the cells with unknowns only: the others hold 0
     for (int l = 1; l <= mg.ngrid; l++) {
-        MgLevel& L = mg.lev[l];
-        MgLevel& C = mg.lev[l + 1];
+        const MgLevel L = lev_view(mg, l, swp);
+        const MgLevel C = l + 1 == lo ? mg.lev[lo] : lev_view(mg, l + 1, swp);
         const bool smooth = l + 1 < mg.nlev;
         const int na = __ldg(mg.nact + l + 1);
         for (int a = gcell; a < na; a += gsz) {
@@ -884,25 +907,23 @@ __device__ __forceinline__ bool mg_cell_levels(Mg& mg, GridBar& gb, DevStats* ds
     }
     // small levels in the group's first block
     if (gb.rank == 0) {
-        if (S)
-            mg_block_cycle_smem<NT>(mg, mg.ngrid + 1, *S);
+        if (smem)
+            mg_block_cycle_smem<NT>(mg, lo, smem);
         else
-            mg_block_cycle<NT>(mg, mg.ngrid + 1);
+            mg_block_cycle<NT>(mg, lo);
     }
     if (!grid_sync<NT>(gb, ds)) return false;
     // grid-wide levels, up: prolongation folded into the post-smoothing
     for (int l = mg.ngrid; l >= 1; l--) {
-        MgLevel& L = mg.lev[l];
-        MgLevel& C = mg.lev[l + 1];
+        const MgLevel L = lev_view(mg, l, swp);
+        const MgLevel C = l == mg.ngrid ? lo_corrected(mg) : lev_view(mg, l + 1, swp);
         const int na = __ldg(mg.nact + l);
         for (int a = gcell; a < na; a += gsz) {
             const int I = __ldg(L.act + a);
             L.t[I] = smooth_up_cell(mg, L, C, I);
         }
         if (!grid_sync<NT>(gb, ds)) return false;
-        float* tmp = L.e;
-        L.e = L.t;
-        L.t = tmp;
+        swp ^= 1u << l;
     }
     return true;
 }
@@ -913,8 +934,8 @@ __device__ __forceinline__ bool mg_cell_levels(Mg& mg, GridBar& gb, DevStats* ds
 // pre-smoothing, prolongation with the post-smoothing.  Ends after writing u
 // (no trailing barrier).  Every block runs the same barrier sequence.
 template <int BS>
-__device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& mf, int K,
-                                          const float* __restrict__ r, float* __restrict__ u,
+__device__ __forceinline__ bool mg_vcycle(const Mg& mg, uint32_t& swp, const Ppe& A, const MatFree& mf,
+                                          int K, const float* __restrict__ r, float* __restrict__ u,
                                           const float* __restrict__ invd0, int n, GridBar& gb,
                                           DevStats* ds) {
     const int gtid = gb.rank * BS + threadIdx.x;
@@ -952,7 +973,8 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
         // of the 3x3 cells around cell I adds B[d][i] r_i / d_i with d the
         // offset from its cell to I.  A column of three cells is one slot
         // range (rows in cell order), split by the cell starts.
-        MgLevel& L1 = mg.lev[1];
+        const MgLevel& L1 = mg.lev[1];
+        float* __restrict__ e1pre = level1_presmooth(mg, swp);
         const int n1 = L1.nx * L1.ny, NY = L1.ny;
         const size_t np = (size_t)mg.n_pad;
         for (int I = gcell; I < n1; I += gsz) {
@@ -999,15 +1021,17 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
                 rr = acc - mg.omega * corr;
             }
             L1.r[I] = rr;
-            L1.e[I] = mg.omega * iv * rr;
+            e1pre[I] = mg.omega * iv * rr;
         }
     } else {
-        mg_level1_plain(mg, mf, src0, gcell, gsz, mg.lev[1].e);
+        mg_level1_plain(mg, mf, src0, gcell, gsz, level1_presmooth(mg, swp));
     }
-    if (!mg_cell_levels<0>(mg, gb, ds, gcell, gsz)) return false;
+    if (!mg_cell_levels<0>(mg, swp, gb, ds, gcell, gsz)) return false;
+    // level 1's correction
+    const float* __restrict__ e1 = level1_correction(mg, swp);
     if (mg.additive && mg.smooth) {
         // u = omega D^-1 r + scale * P e1, P e1 = e1[cell(i)] - omega / d_i sum_d B[d][i] e1[cell(i) + d]
-        MgLevel& L1 = mg.lev[1];
+        const MgLevel& L1 = mg.lev[1];
         const int n1 = L1.nx * L1.ny, NY = L1.ny;
         const size_t np = (size_t)mg.n_pad;
         for (int i0 = gtid; i0 < n; i0 += 2 * gsz) {
@@ -1027,12 +1051,12 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
                 float v = 0.f;
                 if (dg[h] > 0.f) {  // an unknown: its cell is interior
                     const int k = key[h];
-                    const float ec = __ldcg(L1.e + k);
+                    const float ec = __ldcg(e1 + k);
                     float bt[9], en[9];
 #pragma unroll
                     for (int d = 0; d < 9; d++) {
                         bt[d] = __ldg(mg.rowcell + (size_t)d * np + i);
-                        en[d] = __ldcg(L1.e + k + (d / 3 - 1) * NY + (d % 3 - 1));
+                        en[d] = __ldcg(e1 + k + (d / 3 - 1) * NY + (d % 3 - 1));
                     }
                     float corr = 0.f;
 #pragma unroll
@@ -1047,7 +1071,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     }
     if (mg.additive) {
         // u = omega D^-1 r + scale * (level-1 correction of the row's cell)
-        MgLevel& L1 = mg.lev[1];
+        const MgLevel& L1 = mg.lev[1];
         const int n1 = L1.nx * L1.ny;
         for (int i0 = gtid; i0 < n; i0 += 4 * gsz) {
             float dg[4], ri[4], ec[4];
@@ -1060,7 +1084,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
                 ri[h] = __ldcg(r + i);
             }
 #pragma unroll
-            for (int h = 0; h < 4; h++) ec[h] = dg[h] > 0.f ? __ldcg(L1.e + key[h]) : 0.f;
+            for (int h = 0; h < 4; h++) ec[h] = dg[h] > 0.f ? __ldcg(e1 + key[h]) : 0.f;
 #pragma unroll
             for (int h = 0; h < 4; h++) {
                 const int i = i0 + h * gsz;
@@ -1071,7 +1095,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
     }
     // level 1 -> 0: prolongate to the Inner particles, then post-smooth
     {
-        MgLevel& L1 = mg.lev[1];
+        const MgLevel& L1 = mg.lev[1];
         const int n1 = L1.nx * L1.ny;
         // four rows per iteration, loads first and tests after: two round
         // trips per four rows
@@ -1086,7 +1110,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
                 e0[h] = __ldcg(mg.e0 + i);
             }
 #pragma unroll
-            for (int h = 0; h < 4; h++) ec[h] = dg[h] > 0.f ? __ldcg(L1.e + key[h]) : 0.f;
+            for (int h = 0; h < 4; h++) ec[h] = dg[h] > 0.f ? __ldcg(e1 + key[h]) : 0.f;
 #pragma unroll
             for (int h = 0; h < 4; h++) {
                 const int i = i0 + h * gsz;
@@ -1114,7 +1138,7 @@ __device__ __forceinline__ bool mg_vcycle(Mg& mg, const Ppe& A, const MatFree& m
 // The mixed-precision solve of one scene by one group of BS-thread blocks
 // (the whole grid for a single scene, or one scene's share of a batch).
 template <int BS>
-__device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg& mg,
+__device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, const Mg& mg,
                                             const Krylov& kv, const SolveArgs& a, DevStats* ds,
                                             GridBar& gb) {
     if (*(volatile int32_t*)&ds->status & ST_ASYMMETRIC) {  // the reference exits here
@@ -1130,6 +1154,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
     const int lane = threadIdx.x & 31;
     const int gwarp = gtid >> 5;
     const int nwarps = gsz >> 5;
+    uint32_t swp = 0;  // e/t role swaps of the grid-wide levels (lev_view)
 
     double acc[1] = {0.0}, tot[1];
     for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
@@ -1177,7 +1202,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
         }
         if (!grid_sync(gb, ds)) return;
         if (mg.enabled) {
-            if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, kv.inv_diag32, a.n, gb, ds)) return;
+            if (!mg_vcycle<BS>(mg, swp, A, mf, a.K, kv.r32, kv.u32, kv.inv_diag32, a.n, gb, ds)) return;
             if (!grid_sync(gb, ds)) return;
         }
         float alpha = 0.f, beta = 0.f, gamma_old = 1.f;
@@ -1265,7 +1290,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
             k++;
             if (!grid_sync(gb, ds)) return;
             if (mg.enabled) {
-                if (!mg_vcycle<BS>(mg, A, mf, a.K, kv.r32, kv.u32, kv.inv_diag32, a.n, gb, ds)) return;
+                if (!mg_vcycle<BS>(mg, swp, A, mf, a.K, kv.r32, kv.u32, kv.inv_diag32, a.n, gb, ds)) return;
                 if (!grid_sync(gb, ds)) return;
             }
         }
@@ -1283,8 +1308,11 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, Mg&
     }
 }
 
-__global__ void __launch_bounds__(kMixedBlock, 1) k_cg_mixed(Ppe A, MatFree mf, Mg mg, Krylov kv,
-                                                             SolveArgs a, DevStats* ds) {
+// (Parameters are __grid_constant__: read where the launch put them, never
+// copied per thread.)
+__global__ void __launch_bounds__(kMixedBlock, 1)
+    k_cg_mixed(__grid_constant__ const Ppe A, __grid_constant__ const MatFree mf, __grid_constant__ const Mg mg,
+               __grid_constant__ const Krylov kv, __grid_constant__ const SolveArgs a, DevStats* ds) {
     GridBar gb = whole_grid(kv);
     solve_mixed<kMixedBlock>(A, mf, mg, kv, a, ds, gb);
 }
@@ -1315,7 +1343,7 @@ constexpr int kCycleThreads = 512;
 constexpr int kBlockSmemCap = 100 * 1024;
 
 template <int BS, int NV>
-__device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree& mf, Mg& mg,
+__device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree& mf, const Mg& mg,
                                                     const Krylov& kv, const SolveArgs& a, DevStats* ds,
                                                     GridBar& gb, float* dsm) {
     if (*(volatile int32_t*)&ds->status & ST_ASYMMETRIC) {  // the reference exits here
@@ -1339,20 +1367,15 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
     float* __restrict__ z = mg.res0;  // A y
     const size_t np = (size_t)mg.n_pad;
     const int NY = mg.lev[1].ny, n1 = mg.lev[1].nx * NY;
-    __shared__ float* s_e1;
     __shared__ int s_cycle_ok;
-    // level 1's e as the cycle group sees it (its copy swaps e and t each
-    // cycle); the level-1 sums of all warps write there
-    if (tid == 0) s_e1 = mg.lev[1].e;
+    // the e/t role swaps of the grid-wide levels (lev_view): the cycle group
+    // makes them, the other warps follow with the same mask after each cycle
+    uint32_t swp = 0;
+    const uint32_t cycle_swaps = ((1u << (mg.ngrid + 1)) - 1u) & ~1u;  // levels 1..ngrid
     // the small levels in block 0's shared memory (staged once per solve;
     // the first reduction's barriers order it before any cycle)
-    SmemLevels sl;
-    const SmemLevels* slp = nullptr;
-    if (mg.block_smem > 0) {
-        smem_levels_carve(mg, mg.ngrid + 1, dsm, sl);
-        slp = &sl;
-        if (b == 0) smem_levels_stage(mg, mg.ngrid + 1, sl, tid, BS);
-    }
+    float* smem = mg.block_smem > 0 ? dsm : nullptr;
+    if (smem && b == 0) smem_levels_stage(mg, mg.ngrid + 1, smem, tid, BS);
 
     double acc[1] = {0.0}, tot[1];
     for (int sl = gwarp; sl < nsl; sl += nwarps) {
@@ -1399,16 +1422,13 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
             // ---- level 1 of the cycle: every warp sums r over the cells with
             // unknowns (before the split, while nothing else streams), into
             // the cycle group's level-1 arrays
-            mg_level1_plain(mg, mf, kv.r32, ((warp * G + b) << 5) + lane, gsz, s_e1);
+            mg_level1_plain(mg, mf, kv.r32, ((warp * G + b) << 5) + lane, gsz, level1_presmooth(mg, swp));
             if (!grid_sync(gb, ds)) return;
             // ---- split: the cycle's cell levels on r, the operator on y
             if (warp < kVW) {
                 const int gcell = ((warp * G + b) << 5) + lane;
-                const bool ok = mg_cell_levels<NV>(mg, gb, ds, gcell, G * NV, false, slp);
-                if (tid == 0) {
-                    s_e1 = mg.lev[1].e;
-                    s_cycle_ok = ok;
-                }
+                const bool ok = mg_cell_levels<NV>(mg, swp, gb, ds, gcell, G * NV, false, smem);
+                if (tid == 0) s_cycle_ok = ok;
             } else {
                 for (int q = warp - kVW;; q += 2 * kZW) {
                     const int sl1 = b + G * q;
@@ -1426,10 +1446,11 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
                     z[i] = dg0 > 0.f ? fmaf(dg0, y0, o) : 0.f;
                     if (i2 >= 0) z[i2] = dg1 > 0.f ? fmaf(dg1, y1, o2) : 0.f;
                 }
+                swp ^= cycle_swaps;
             }
             __syncthreads();
             if (!s_cycle_ok) return;
-            const float* __restrict__ e1 = s_e1;
+            const float* __restrict__ e1 = level1_correction(mg, swp);
             // ---- u = omega y + scale e1[cell], w = omega z + scale B e1, dot products
             F2 g = {0.f, 0.f}, dl = {0.f, 0.f}, rr = {0.f, 0.f};
             for (int q = warp;; q += 2 * kW) {
@@ -1540,8 +1561,9 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
     }
 }
 
-__global__ void __launch_bounds__(kMixedBlock, 1) k_cg_mixed_ov(Ppe A, MatFree mf, Mg mg, Krylov kv,
-                                                                SolveArgs a, DevStats* ds) {
+__global__ void __launch_bounds__(kMixedBlock, 1)
+    k_cg_mixed_ov(__grid_constant__ const Ppe A, __grid_constant__ const MatFree mf, __grid_constant__ const Mg mg,
+                  __grid_constant__ const Krylov kv, __grid_constant__ const SolveArgs a, DevStats* ds) {
     extern __shared__ float dsm[];
     GridBar gb = whole_grid(kv);
     solve_mixed_overlap<kMixedBlock, kCycleThreads>(A, mf, mg, kv, a, ds, gb, dsm);
@@ -1564,7 +1586,7 @@ __global__ void __launch_bounds__(BS, MINB) k_cg_mixed_batched(const SceneSolve*
                                                                const int32_t* __restrict__ gsize,
                                                                unsigned int* bars) {
     const int2 m = bmap[blockIdx.x];
-    SceneSolve s = scenes[m.x];
+    const SceneSolve& s = scenes[m.x];
     GridBar gb{bars + 32 * m.x, 0u, 0, m.y, gsize[m.x], s.kv.partials};
     solve_mixed<BS>(s.A, s.mf, s.mg, s.kv, s.a, s.ds, gb);
 }
