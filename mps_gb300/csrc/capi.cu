@@ -629,10 +629,9 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         g.ngrid = 0;
         while (g.ngrid + 1 < g.nlev && (size_t)g.lev[g.ngrid + 1].nx * g.lev[g.ngrid + 1].ny > kMgBlockCells)
             g.ngrid++;
-        g.block_smem = mg_block_smem_bytes(g);
         if (e->alloc(&g.e0, np) || e->alloc(&g.res0, np) ||
             e->alloc(&g.dense, (size_t)kMgMaxCoarsest * kMgMaxCoarsest) || e->alloc(&g.rowcell, 9 * np) ||
-            e->alloc(&g.nact, kMgMaxLevels))
+            e->alloc(&g.nact, kMgMaxLevels) || e->alloc(&g.act1_rng, (size_t)c.numX * c.numY))
             return bail(fail(MPS_ERR_CUDA, "cudaMalloc multigrid"));
         g.n_pad = (int32_t)np;
     }

@@ -249,9 +249,7 @@ struct Mg {
     float* rowcell;
     int32_t n_pad;
     int32_t* nact;  // per level: the length of lev[l].act (device, written by the setup)
-    // bytes of dynamic shared memory that hold the levels the first block runs
-    // (ngrid + 1 .. nlev) in the overlapped solve; 0: they stay in global memory
-    int32_t block_smem;
+    int2* act1_rng; // per entry of lev[1].act: the cell's first slot and slot count
 };
 
 // --------------------------------------------------------------- solver.cu
@@ -306,9 +304,6 @@ int batch_solve_setup(const std::vector<BatchScene>& scenes, int block, double a
                       BatchSolve& b);
 void batch_solve_free(BatchSolve& b);
 void launch_solve_mixed_batched(const BatchSolve& b, cudaStream_t st);
-// Bytes of shared memory the overlapped solve uses for the small levels of
-// this hierarchy (0: they stay in global memory); grants the kernel that much.
-int mg_block_smem_bytes(const Mg& mg);
 // Per-solve multigrid setup (after launch_mixed_setup).
 void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
                      cudaStream_t st);

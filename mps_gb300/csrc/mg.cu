@@ -27,16 +27,19 @@ __device__ __forceinline__ void add_tap(float (&st)[9], int d, float v) {
 
 // Appends cell I to the level's list of cells with unknowns: one atomic per
 // warp, the warp's cells in ascending order.
-__device__ __forceinline__ void list_active(bool act, int I, int32_t* list, int32_t* count) {
+// Returns the entry's position (-1 for a cell that is not listed).
+__device__ __forceinline__ int list_active(bool act, int I, int32_t* list, int32_t* count) {
     const unsigned am = __activemask();
     const unsigned m = __ballot_sync(am, act);
-    if (!m) return;
+    if (!m) return -1;
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(m) - 1;
     int base = 0;
     if (lane == leader) base = atomicAdd(count, __popc(m));
     base = __shfl_sync(am, base, leader);
-    if (act) list[base + __popc(m & ((1u << lane) - 1u))] = I;
+    const int pos = base + __popc(m & ((1u << lane) - 1u));
+    if (act) list[pos] = I;
+    return act ? pos : -1;
 }
 
 // Every cell's r, e and t to 0 on the levels the grid-wide phases visit by
@@ -55,7 +58,7 @@ __global__ void k_mg_clear(Mg mg) {
     }
 }
 
-__global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L, int32_t* nact) {
+__global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L, int32_t* nact, int2* act_rng) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= L.nx * L.ny) return;
     const int cx = I / L.ny, cy = I - cx * L.ny;
@@ -120,7 +123,8 @@ __global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L, int32_t* nac
 #pragma unroll
     for (int d = 0; d < 9; d++) L.st[(size_t)d * n + I] = st[d];
     L.invd[I] = st[4] > 0.f ? 1.f / st[4] : 0.f;
-    list_active(st[4] > 0.f, I, L.act, nact + 1);
+    const int pos = list_active(st[4] > 0.f, I, L.act, nact + 1);
+    if (pos >= 0) act_rng[pos] = make_int2(b, e - b);  // the cell's slots, beside its list entry
 }
 
 // Smoothed transfer: B = A P1 per slot (the row's sums over the 3x3 cells
@@ -280,7 +284,7 @@ void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg&
     }
     const MgLevel& L1 = mg.lev[1];
     k_mg_clear<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(mg);
-    k_mg_level1<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(c, A, mf, L1, mg.nact);
+    k_mg_level1<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(c, A, mf, L1, mg.nact, mg.act1_rng);
     g_launches += 2;
     for (int l = 1; l < mg.nlev; l++) {
         const MgLevel& C = mg.lev[l + 1];

@@ -687,15 +687,16 @@ __device__ __forceinline__ void mg_level1_plain(const Mg& mg, const MatFree& mf,
         int b[4], cnt[4], cell[4];
         float iv[4], acc[4];
 #pragma unroll
-        for (int h = 0; h < 4; h++) cell[h] = __ldg(L1.act + min(a0 + h * gsz, na - 1));
-#pragma unroll
         for (int h = 0; h < 4; h++) {
-            const int I = cell[h];
-            b[h] = __ldg(mf.cs + I);
-            cnt[h] = __ldg(mf.cs + I + 1) - b[h];
-            iv[h] = __ldg(L1.invd + I);
+            const int a = min(a0 + h * gsz, na - 1);
+            cell[h] = __ldg(L1.act + a);
+            const int2 rg = __ldg(mg.act1_rng + a);
+            b[h] = rg.x;
+            cnt[h] = rg.y;
             acc[h] = 0.f;
         }
+#pragma unroll
+        for (int h = 0; h < 4; h++) iv[h] = __ldg(L1.invd + cell[h]);
         const int m = max(max(cnt[0], cnt[1]), max(cnt[2], cnt[3]));
         for (int j = 0; j < m; j += 4) {
             float x[4][4];
@@ -719,172 +720,17 @@ __device__ __forceinline__ void mg_level1_plain(const Mg& mg, const MatFree& mf,
     }
 }
 
-// ------------------------------------------ the small levels in shared memory
-// The levels the group's first block runs alone (lo = ngrid + 1 .. nlev) are
-// small (at most kMgBlockCells cells at lo, a quarter of that below), and
-// their stencils do not change during a solve.  Held in block 0's shared
-// memory, a cycle through them costs shared-memory latency instead of L2
-// round trips.  Layout, per level lo..nlev: r, e, t (n floats each); per
-// level lo+1..nlev: 9-point stencil, inverse diagonal, 4x4 restriction
-// weights (26 n floats; level lo's stencil and inverse diagonal stay in
-// global memory); then the coarsest level's dense inverse.
-__host__ __device__ inline size_t block_smem_floats(const Mg& mg, int lo) {
-    size_t f = 0;
-    for (int l = lo; l <= mg.nlev; l++) {
-        const size_t n = (size_t)mg.lev[l].nx * mg.lev[l].ny;
-        f += 3 * n + (l > lo ? 26 * n : 0);
-    }
-    const size_t nc = (size_t)mg.lev[mg.nlev].nx * mg.lev[mg.nlev].ny;
-    return f + nc * nc;
-}
-
-// Level l's arrays in the layout (base roles: r, e, t in that order).
-__device__ __forceinline__ MgLevel smem_view(const Mg& mg, int lo, float* base, int l) {
-    float* q = base;
-    for (int k = lo; k < l; k++) {
-        const int nk = mg.lev[k].nx * mg.lev[k].ny;
-        q += 3 * nk + (k > lo ? 26 * nk : 0);
-    }
-    MgLevel L = mg.lev[l];
-    const int n = L.nx * L.ny;
-    L.r = q;
-    L.e = q + n;
-    L.t = q + 2 * n;
-    if (l > lo) {
-        L.st = q + 3 * n;
-        L.invd = q + 12 * n;
-        L.rw = q + 13 * n;
-    }
-    return L;
-}
-
-// Copies the levels' constant arrays into the layout (once per solve; the
-// calling threads, tid < nt, then meet at a block barrier).
-__device__ void smem_levels_stage(const Mg& mg, int lo, float* base, int tid, int nt) {
-    for (int l = lo + 1; l <= mg.nlev; l++) {
-        const MgLevel S = smem_view(mg, lo, base, l);
-        const int n = S.nx * S.ny;
-        for (int i = tid; i < 9 * n; i += nt) S.st[i] = __ldg(mg.lev[l].st + i);
-        for (int i = tid; i < n; i += nt) S.invd[i] = __ldg(mg.lev[l].invd + i);
-        for (int i = tid; i < 16 * n; i += nt) S.rw[i] = __ldg(mg.lev[l].rw + i);
-    }
-    const int nc = mg.lev[mg.nlev].nx * mg.lev[mg.nlev].ny;
-    float* dense = base + (block_smem_floats(mg, lo) - (size_t)nc * nc);
-    for (int i = tid; i < nc * nc; i += nt) dense[i] = __ldg(mg.dense + i);
-}
-
-// restrict_cell and smooth_up_cell on shared-memory levels (plain loads;
-// level lo's stencil is read from global memory by the same plain loads).
-__device__ __forceinline__ float restrict_cell_s(const MgLevel& F, const MgLevel& C, int I, int X, int Y) {
-    const int nc = C.nx * C.ny;
-    int xs[4], ys[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        xs[k] = min(max(2 * X - 1 + k, 0), F.nx - 1) * F.ny;
-        ys[k] = min(max(2 * Y - 1 + k, 0), F.ny - 1);
-    }
-    float acc = 0.f;
-#pragma unroll
-    for (int k = 0; k < 16; k++) acc = fmaf(C.rw[(size_t)k * nc + I], F.r[xs[k >> 2] + ys[k & 3]], acc);
-    return acc;
-}
-
-__device__ __forceinline__ float smooth_up_cell_s(const Mg& mg, const MgLevel& L, const MgLevel& C, int I) {
-    const int n = L.nx * L.ny;
-    const int x = I / L.ny, y = I - x * L.ny;
-    const float ei = fmaf(mg.scale, C.e[(x / 2) * C.ny + y / 2], L.e[I]);
-    float acc = 0.f;
-#pragma unroll
-    for (int d = 0; d < 9; d++) {
-        bool ok;
-        const int j = tap(L, x, y, d, ok);
-        const int jx = j / L.ny, jy = j - jx * L.ny;
-        const float ej = fmaf(mg.scale, C.e[(jx / 2) * C.ny + jy / 2], L.e[j]);
-        if (ok) acc = fmaf(L.st[(size_t)d * n + I], ej, acc);
-    }
-    return fmaf(mg.omega * L.invd[I], L.r[I] - acc, ei);
-}
-
-// mg_block_cycle in shared memory: level lo's residual and pre-smoothing come
-// in from global memory, its correction goes back to level lo's t array.
-template <int NT>
-__device__ void mg_block_cycle_smem(const Mg& mg, int lo, float* base) {
-    const int tid = threadIdx.x, nt = NT == 0 ? (int)blockDim.x : NT;
-    auto view = [&](int l, uint32_t bsw) {
-        MgLevel L = smem_view(mg, lo, base, l);
-        if (l == lo) {
-            L.st = mg.lev[lo].st;
-            L.invd = mg.lev[lo].invd;
-        }
-        if ((bsw >> l) & 1u) {
-            float* t = L.e;
-            L.e = L.t;
-            L.t = t;
-        }
-        return L;
-    };
-    uint32_t bsw = 0;
-    {
-        const MgLevel L = view(lo, 0);
-        const int n = L.nx * L.ny;
-        for (int i = tid; i < n; i += nt) {
-            L.r[i] = __ldcg(mg.lev[lo].r + i);
-            L.e[i] = __ldcg(mg.lev[lo].e + i);
-        }
-        group_bar<NT>();
-    }
-    for (int l = lo; l < mg.nlev; l++) {
-        const MgLevel L = view(l, bsw);
-        const MgLevel C = view(l + 1, bsw);
-        const bool smooth = l + 1 < mg.nlev;
-        for (int I = tid; I < C.nx * C.ny; I += nt) {
-            const int X = I / C.ny, Y = I - X * C.ny;
-            const float iv = C.invd[I];
-            const float rr = iv > 0.f ? restrict_cell_s(L, C, I, X, Y) : 0.f;
-            C.r[I] = rr;
-            if (smooth) C.e[I] = mg.omega * iv * rr;
-        }
-        group_bar<NT>();
-    }
-    {
-        const MgLevel L = view(mg.nlev, bsw);
-        const int n = L.nx * L.ny;
-        const float* dense = base + (block_smem_floats(mg, lo) - (size_t)n * n);
-        float* out = mg.nlev == lo ? mg.lev[lo].t : L.e;
-        const int lane = tid & 31;
-        for (int i = tid >> 5; i < n; i += nt >> 5) {
-            float acc = 0.f;
-            for (int j = lane; j < n; j += 32) acc = fmaf(dense[i * n + j], L.r[j], acc);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) out[i] = L.invd[i] > 0.f ? acc : 0.f;
-        }
-        group_bar<NT>();
-    }
-    for (int l = mg.nlev - 1; l >= lo; l--) {
-        const MgLevel L = view(l, bsw);
-        const MgLevel C = view(l + 1, bsw);
-        const int n = L.nx * L.ny;
-        float* out = l == lo ? mg.lev[lo].t : L.t;
-        for (int I = tid; I < n; I += nt) out[I] = L.invd[I] > 0.f ? smooth_up_cell_s(mg, L, C, I) : 0.f;
-        group_bar<NT>();
-        if (l > lo) bsw ^= 1u << l;
-    }
-}
-
 // The cell levels of the V-cycle after level 1's residual and pre-smoothing
 // were written: a grid barrier, the grid-wide levels down (restriction
 // fused with the next level's pre-smoothing), the small levels in the
-// group's first block (in shared memory from `smem` when given), the
-// grid-wide levels up (prolongation folded into the post-smoothing), each
+// group's first block, the grid-wide levels up (prolongation folded into the post-smoothing), each
 // phase closed by a grid barrier of the thread group NT (0: whole blocks).
 // Afterwards level 1's correction is complete for every block
 // (level1_correction).  sync_first = false skips the first barrier where
 // the caller passed one since level 1 was written.  swp: the role swaps.
 template <int NT>
 __device__ __forceinline__ bool mg_cell_levels(const Mg& mg, uint32_t& swp, GridBar& gb, DevStats* ds,
-                                               int gcell, int gsz, bool sync_first = true,
-                                               float* smem = nullptr) {
+                                               int gcell, int gsz, bool sync_first = true) {
     if (sync_first && !grid_sync<NT>(gb, ds)) return false;
     const int lo = mg.ngrid + 1;
     // grid-wide levels, down: restrict level l into l+1 and pre-smooth there
@@ -906,12 +752,7 @@ __device__ __forceinline__ bool mg_cell_levels(const Mg& mg, uint32_t& swp, Grid
         if (!grid_sync<NT>(gb, ds)) return false;
     }
     // small levels in the group's first block
-    if (gb.rank == 0) {
-        if (smem)
-            mg_block_cycle_smem<NT>(mg, lo, smem);
-        else
-            mg_block_cycle<NT>(mg, lo);
-    }
+    if (gb.rank == 0) mg_block_cycle<NT>(mg, lo);
     if (!grid_sync<NT>(gb, ds)) return false;
     // grid-wide levels, up: prolongation folded into the post-smoothing
     for (int l = mg.ngrid; l >= 1; l--) {
@@ -1335,17 +1176,13 @@ __global__ void __launch_bounds__(kMixedBlock, 1)
 // block (no operator pass reads them).  Same Chronopoulos-Gear recurrences,
 // refinement and stopping rules as solve_mixed.
 //
-// Rows of block b: the 32-row slices b, b + G, b + 2G, ... (G blocks).
+// Rows: 32-row slices dealt to blocks 1..G-1 (block 0 runs the small levels).
 constexpr int kCycleThreads = 512;
-// Upper bound of the shared-memory copy of the small levels (beside the
-// kernel's 33 KB of static shared memory); larger hierarchies keep them in
-// global memory.
-constexpr int kBlockSmemCap = 100 * 1024;
 
 template <int BS, int NV>
 __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree& mf, const Mg& mg,
                                                     const Krylov& kv, const SolveArgs& a, DevStats* ds,
-                                                    GridBar& gb, float* dsm) {
+                                                    GridBar& gb) {
     if (*(volatile int32_t*)&ds->status & ST_ASYMMETRIC) {  // the reference exits here
         if (gb.rank == 0 && threadIdx.x == 0) {
             ds->cg_iterations = 0;
@@ -1361,6 +1198,13 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
     const int gtid = b * BS + tid, gsz = G * BS;
     const int gwarp = gtid >> 5, nwarps = gsz >> 5;
     const int n = a.n, nsl = a.nslices;
+    // The rows (32-row slices) of the operator pass, of the pass that forms
+    // u and w and of the vector update belong to blocks 1..G-1: slices
+    // rb, rb + RB, rb + 2 RB, ...  Block 0 runs the cycle's small levels and
+    // does not also stream rows beside them.
+    const int RB = G > 1 ? G - 1 : 1;
+    const int rb = G > 1 ? b - 1 : 0;
+    const bool has_rows = G == 1 || b > 0;
     // per-slot FP32 work vectors of this arrangement (the additive cycle uses
     // neither the level-0 correction nor the level-0 residual arrays)
     float* __restrict__ y = mg.e0;    // D^-1 r
@@ -1372,10 +1216,6 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
     // makes them, the other warps follow with the same mask after each cycle
     uint32_t swp = 0;
     const uint32_t cycle_swaps = ((1u << (mg.ngrid + 1)) - 1u) & ~1u;  // levels 1..ngrid
-    // the small levels in block 0's shared memory (staged once per solve;
-    // the first reduction's barriers order it before any cycle)
-    float* smem = mg.block_smem > 0 ? dsm : nullptr;
-    if (smem && b == 0) smem_levels_stage(mg, mg.ngrid + 1, smem, tid, BS);
 
     double acc[1] = {0.0}, tot[1];
     for (int sl = gwarp; sl < nsl; sl += nwarps) {
@@ -1427,13 +1267,13 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
             // ---- split: the cycle's cell levels on r, the operator on y
             if (warp < kVW) {
                 const int gcell = ((warp * G + b) << 5) + lane;
-                const bool ok = mg_cell_levels<NV>(mg, swp, gb, ds, gcell, G * NV, false, smem);
+                const bool ok = mg_cell_levels<NV>(mg, swp, gb, ds, gcell, G * NV, false);
                 if (tid == 0) s_cycle_ok = ok;
             } else {
-                for (int q = warp - kVW;; q += 2 * kZW) {
-                    const int sl1 = b + G * q;
+                for (int q = warp - kVW; has_rows; q += 2 * kZW) {
+                    const int sl1 = rb + RB * q;
                     if (sl1 >= nsl) break;
-                    const int sl2 = b + G * (q + kZW);
+                    const int sl2 = rb + RB * (q + kZW);
                     const int i = sl1 * 32 + lane;
                     int i2 = sl2 < nsl ? sl2 * 32 + lane : -1;
                     if (i2 >= n) i2 = -1;
@@ -1453,10 +1293,10 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
             const float* __restrict__ e1 = level1_correction(mg, swp);
             // ---- u = omega y + scale e1[cell], w = omega z + scale B e1, dot products
             F2 g = {0.f, 0.f}, dl = {0.f, 0.f}, rr = {0.f, 0.f};
-            for (int q = warp;; q += 2 * kW) {
-                const int sla = b + G * q;
+            for (int q = warp; has_rows; q += 2 * kW) {
+                const int sla = rb + RB * q;
                 if (sla >= nsl) break;
-                const int slb = b + G * (q + kW);
+                const int slb = rb + RB * (q + kW);
                 int ii[2] = {sla * 32 + lane, slb < nsl ? slb * 32 + lane : n};
                 float dg[2], ri[2], yi[2], zi[2];
                 int key[2];
@@ -1510,12 +1350,12 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
             gamma_old = gamma;
             // ---- p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; y = D^-1 r
             // (this block's rows: u and w are its own; four rows in flight)
-            for (int q = warp;; q += 4 * kW) {
-                if (b + G * q >= nsl) break;
+            for (int q = warp; has_rows; q += 4 * kW) {
+                if (rb + RB * q >= nsl) break;
                 int ii[4];
 #pragma unroll
                 for (int h = 0; h < 4; h++) {
-                    const int sl = b + G * (q + h * kW);
+                    const int sl = rb + RB * (q + h * kW);
                     ii[h] = sl < nsl ? sl * 32 + lane : n;
                 }
                 float u[4], p[4], sv[4], w[4], x[4], r[4], id[4];
@@ -1564,9 +1404,8 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
 __global__ void __launch_bounds__(kMixedBlock, 1)
     k_cg_mixed_ov(__grid_constant__ const Ppe A, __grid_constant__ const MatFree mf, __grid_constant__ const Mg mg,
                   __grid_constant__ const Krylov kv, __grid_constant__ const SolveArgs a, DevStats* ds) {
-    extern __shared__ float dsm[];
     GridBar gb = whole_grid(kv);
-    solve_mixed_overlap<kMixedBlock, kCycleThreads>(A, mf, mg, kv, a, ds, gb, dsm);
+    solve_mixed_overlap<kMixedBlock, kCycleThreads>(A, mf, mg, kv, a, ds, gb);
 }
 
 // Many scenes in one persistent launch: block b belongs to group bmap[b].x
@@ -1670,24 +1509,6 @@ void solver_setup(Krylov& k, int32_t /*n_pad*/, int device) {
     int g3 = coop_grid((const void*)k_cg_mixed_ov, device, kMixedBlock, 0, 1);
     k.grid = std::min({g1, g2, g3});
     k.block = kBlock;
-}
-
-int mg_block_smem_bytes(const Mg& mg) {
-    if (!mg.enabled || mg.ngrid + 1 > mg.nlev) return 0;
-    const size_t bytes = 4 * block_smem_floats(mg, mg.ngrid + 1);
-    if (bytes > (size_t)kBlockSmemCap) return 0;
-    // the overlapped solve kernel may take that much dynamic shared memory
-    // (the largest request so far stays set: every engine of the process fits)
-    static int granted = 0;
-    if ((int)bytes > granted) {
-        if (cudaFuncSetAttribute((const void*)k_cg_mixed_ov, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)bytes) != cudaSuccess) {
-            cudaGetLastError();
-            return 0;
-        }
-        granted = (int)bytes;
-    }
-    return (int)bytes;
 }
 
 void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, MatFree& mf,
@@ -1870,7 +1691,7 @@ void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const 
     cudaMemsetAsync(k.barrier, 0, sizeof(unsigned int), st);
     const bool ov = mg.enabled && mg.overlap;
     const void* fn = ov ? (const void*)k_cg_mixed_ov : (const void*)k_cg_mixed;
-    cudaLaunchCooperativeKernel(fn, dim3(k.grid), dim3(kMixedBlock), args, ov ? (size_t)mg.block_smem : 0, st);
+    cudaLaunchCooperativeKernel(fn, dim3(k.grid), dim3(kMixedBlock), args, 0, st);
     ++g_launches;
 }
 
