@@ -153,6 +153,17 @@ int mps_step(mps_engine* e, int32_t is_time_to_export, mps_step_stats* stats);
  * the first step that returns a status other than MPS_OK. */
 int mps_run(mps_engine* e, int32_t n_steps, mps_step_stats* stats);
 
+/* n_steps consecutive non-export steps with one host wait per up to 256
+ * steps (the driver loop of Simulation::run between two exports,
+ * src/simulation.cpp:39-60, without a host round trip per step): stats[k]
+ * (n_steps entries) holds step k's stats, as mps_step would report them,
+ * with ms_step from device timestamps and ms_solve 0.  A step whose solve
+ * reached its iteration cap does not stop the run (stats[k].status says so,
+ * and the call returns MPS_ERR_NOT_CONVERGED at the end); any other failure
+ * returns its status at once (that step's stats are the last filled; the
+ * steps that followed it in the same group of 256 have run). */
+int mps_run_report(mps_engine* e, int32_t n_steps, mps_step_stats* stats);
+
 /* The symmetry test of solvePoissonEquation (src/mps.cpp:418-442) on a host
  * CSR matrix (n rows, row_ptr n+1, col/val row_ptr[n]; columns need not be
  * sorted), run by the same device kernels every step runs on the engine's

@@ -151,6 +151,22 @@ __global__ void k_check_upload(int n, const double* __restrict__ pos, const doub
     if (type && (type[i] < -1 || type[i] > 2)) f |= 2;
     if (f) atomicOr(flag, f);
 }
+// The step's record for mps_run_report: its DevStats and the device time.
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__global__ void k_stats_record(const DevStats* __restrict__ ds, DevStats* ring, int32_t* pos, int32_t cap) {
+    const int k = *pos;
+    if (k < cap) {
+        DevStats r = *ds;
+        r.t_end = global_ns();
+        ring[k] = r;
+    }
+    *pos = k + 1;
+}
+__global__ void k_stamp(unsigned long long* t) { *t = global_ns(); }
 __global__ void k_iota(int n, int32_t* a) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) a[k] = k;
@@ -189,6 +205,16 @@ Mg active_mg(const mps_engine* e) {
     g.smooth = e->mg_requested == 3;
     g.overlap = e->mg_requested == 1 && e->cycle_overlap;
     return g;
+}
+
+// The public code of a step's device status bits (check_status's order).
+int32_t status_code(int32_t s) {
+    if (s & ST_TIMEOUT) return MPS_ERR_TIMEOUT;
+    if (s & ST_NONFINITE) return MPS_ERR_NONFINITE;
+    if (s & ST_CAPACITY) return MPS_ERR_CAPACITY;
+    if (s & ST_ASYMMETRIC) return MPS_ERR_ASYMMETRIC;
+    if (s & ST_NOT_CONVERGED) return MPS_ERR_NOT_CONVERGED;
+    return MPS_OK;
 }
 
 int check_status(mps_engine* e) {
@@ -286,6 +312,8 @@ void enqueue_step(mps_engine* e, bool do_export) {
     cudaEventRecordWithFlags(e->ev[3], st, evflag);
     if (e->tape) tape_phase(e, TAPE_SOLVE);
     enqueue_post_solve(e, do_export);
+    k_stats_record<<<1, 1, 0, st>>>(e->ds, e->ring, e->ring_pos, e->ring_cap);
+    ++g_launches;
     e->step_launches = g_launches;
 }
 
@@ -342,7 +370,7 @@ void fill_stats(mps_engine* e, mps_step_stats* out) {
     out->n_unconnected = h.n_unconnected;
     out->n_inner = h.n_inner;
     out->n_surface = h.n_surface;
-    out->status = h.status;
+    out->status = status_code(h.status);
     float ms = 0.f, ms2 = 0.f;
     // events a step did not record (batched steps) read as 0 ms
     if (cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]) != cudaSuccess) ms = 0.f;
@@ -396,7 +424,10 @@ bool capture_step(mps_engine* e) {
 
 // One MPS::stepForward: a graph replay for non-export steps where graphs are
 // on, else the kernels launched one by one.  Waits for the step's stats.
-int run_one_step(mps_engine* e, bool do_export, mps_step_stats* stats) {
+// Enqueues one MPS::stepForward (a graph replay for non-export steps where
+// graphs are on, else the kernels one by one); the step's stats reach e->hs
+// and its record e->ring when the stream gets there.
+int launch_one_step(mps_engine* e, bool do_export) {
     const int par = e->cur;
     bool graphed = false;
     if (!do_export && !e->tape && e->use_graph && !e->graph_broken) {
@@ -417,6 +448,13 @@ int run_one_step(mps_engine* e, bool do_export, mps_step_stats* stats) {
         CU(cudaMemcpyAsync(e->hs, e->ds, sizeof(DevStats), cudaMemcpyDeviceToHost, e->st));
     }
     e->last_step_graphed = graphed ? 1 : 0;
+    return MPS_OK;
+}
+
+// One MPS::stepForward; waits for its stats.
+int run_one_step(mps_engine* e, bool do_export, mps_step_stats* stats) {
+    int rc = launch_one_step(e, do_export);
+    if (rc) return rc;
     CU(cudaStreamSynchronize(e->st));
     CU(cudaGetLastError());
     fill_stats(e, stats);
@@ -637,8 +675,12 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
     }
     if (e->alloc(&e->kv.partials, (size_t)e->kv.grid * 16))
         return bail(fail(MPS_ERR_CUDA, "cudaMalloc partials"));
-    if (cudaMallocHost(&e->hs, sizeof(DevStats)) != cudaSuccess)
+    if (cudaMallocHost(&e->hs, sizeof(DevStats)) != cudaSuccess ||
+        cudaMallocHost(&e->ring_host, sizeof(DevStats) * (e->ring_cap + 1)) != cudaSuccess)
         return bail(fail(MPS_ERR_CUDA, "cudaMallocHost"));
+    if (e->alloc(&e->ring, e->ring_cap) || e->alloc(&e->ring_pos, 1) || e->alloc(&e->ring_t0, 1))
+        return bail(fail(MPS_ERR_CUDA, "cudaMalloc step records"));
+    cudaMemsetAsync(e->ring_pos, 0, sizeof(int32_t), e->st);
     // zero-init everything that a kernel may read before writing
     StateBuf& s = e->buf[0];
     for (int b = 0; b < 2; b++) {
@@ -682,6 +724,7 @@ int mps_destroy(mps_engine* e) {
     drop_graphs(e);
     for (void* p : e->allocs) cudaFree(p);
     if (e->hs) cudaFreeHost(e->hs);
+    if (e->ring_host) cudaFreeHost(e->ring_host);
     for (auto& ev : e->ev)
         if (ev) cudaEventDestroy(ev);
     if (e->xst) cudaStreamSynchronize(e->xst);
@@ -752,6 +795,43 @@ int mps_run(mps_engine* e, int32_t n_steps, mps_step_stats* stats) {
         if (rc) return rc;
     }
     return MPS_OK;
+}
+
+int mps_run_report(mps_engine* e, int32_t n_steps, mps_step_stats* stats) {
+    if (!e || n_steps < 0 || (n_steps > 0 && !stats)) return fail(MPS_ERR_ARG, "mps_run_report: bad arguments");
+    int32_t done = 0;
+    int warn = MPS_OK;
+    while (done < n_steps) {
+        const int32_t m = std::min(e->ring_cap, n_steps - done);
+        CU(cudaMemsetAsync(e->ring_pos, 0, sizeof(int32_t), e->st));
+        k_stamp<<<1, 1, 0, e->st>>>(e->ring_t0);
+        for (int32_t k = 0; k < m; k++) {
+            int rc = launch_one_step(e, false);
+            if (rc) return rc;
+        }
+        CU(cudaMemcpyAsync(e->ring_host, e->ring, sizeof(DevStats) * m, cudaMemcpyDeviceToHost, e->st));
+        unsigned long long* t0h = &e->ring_host[e->ring_cap].t_end;  // the spare record
+        CU(cudaMemcpyAsync(t0h, e->ring_t0, sizeof(unsigned long long), cudaMemcpyDeviceToHost, e->st));
+        CU(cudaStreamSynchronize(e->st));
+        CU(cudaGetLastError());
+        unsigned long long prev = *t0h;
+        for (int32_t k = 0; k < m; k++) {
+            *e->hs = e->ring_host[k];
+            mps_step_stats* o = stats + done + k;
+            fill_stats(e, o);
+            o->ms_step = (float)((double)(e->ring_host[k].t_end - prev) * 1e-6);
+            o->ms_solve = 0.f;  // not timed in these runs
+            prev = e->ring_host[k].t_end;
+            const int rc = check_status(e);
+            if (rc == MPS_ERR_NOT_CONVERGED) {  // a warning: the step completed
+                warn = rc;
+                continue;
+            }
+            if (rc) return rc;  // the later steps of this group have been made too
+        }
+        done += m;
+    }
+    return warn;
 }
 
 int mps_step(mps_engine* e, int32_t is_time_to_export, mps_step_stats* stats) {

@@ -99,6 +99,7 @@ struct DevStats {
     unsigned long long sym_fp;
     unsigned long long asym_big;
     unsigned long long asym_any;
+    unsigned long long t_end;  // device time (ns) at the end of the step, in its per-step record
 };
 
 struct CollPair {

@@ -71,6 +71,14 @@ struct mps_engine {
     int32_t* dflag = nullptr;    // device flag of the upload checks
     mpsg::DevStats* ds = nullptr;
     mpsg::DevStats* hs = nullptr;  // pinned
+    // per-step records of runs that wait once for many steps (mps_run_report):
+    // every step appends its DevStats to `ring` at ring_pos (capacity
+    // ring_cap); ring_t0 holds the device time at the start of such a run
+    mpsg::DevStats* ring = nullptr;
+    mpsg::DevStats* ring_host = nullptr;  // pinned
+    int32_t* ring_pos = nullptr;
+    unsigned long long* ring_t0 = nullptr;
+    int32_t ring_cap = 256;
     int precision = MPS_PRECISION_FP64;
     double tol = std::numeric_limits<double>::epsilon();
     int64_t max_iter = 0;

@@ -119,6 +119,8 @@ def load(build_if_missing: bool = False):
     L.mps_set_graphs.restype = C.c_int
     L.mps_step.argtypes = [vp, C.c_int32, P(MpsStepStats)]
     L.mps_run.argtypes = [vp, C.c_int32, P(MpsStepStats)]
+    L.mps_run_report.argtypes = [vp, C.c_int32, vp]
+    L.mps_run_report.restype = C.c_int
     L.mps_download.argtypes = [vp] + [vp] * 8
     L.mps_upload.argtypes = [vp, vp, vp, vp]
     L.mps_particle_count.argtypes = [vp]
@@ -323,6 +325,13 @@ class Engine:
         st = MpsStepStats()
         _check(_lib.mps_run(self._h, int(n_steps), C.byref(st)))
         return self._stats(st)
+
+    def run_report(self, n_steps: int) -> list:
+        """n non-export steps with one host wait per up to 256 steps; the
+        stats of every step (mps_run_report)."""
+        st = (MpsStepStats * max(int(n_steps), 1))()
+        _check(_lib.mps_run_report(self._h, int(n_steps), st))
+        return [self._stats(s) for s in st[:int(n_steps)]]
 
     def state(self) -> dict:
         n = self.n

@@ -135,30 +135,56 @@ void MPS::syncParticles() {
     }
 }
 
+namespace {
+// The debug and error lines the reference logs during one step
+// (src/mps.cpp:547-571, 590-593, 362-415, 462-464).
+void logStep(const mps_step_stats& st, double cfl) {
+    if (st.n_new_ghosts > 0)
+        mpslog::debug(std::to_string(st.n_new_ghosts) + " particle(s) went out of the domain.");
+    if (st.n_unconnected > 0)
+        mpslog::debug("There is no Dirichlet boundary condition connected to " + std::to_string(st.n_unconnected) +
+                      " particle(s).");
+    if (st.courant > cfl)
+        mpslog::debug("Courant number is larger than CFL condition. Courant=" + std::to_string(st.courant));
+    if (st.courant > 1.0) mpslog::error("Courant number is larger than 1.0. Exiting Simulation.");
+    if (st.status == MPS_ERR_NOT_CONVERGED)  // the step goes on with that pressure
+        mpslog::debug("Pressure calculation failed: the solve stopped at its iteration cap.");
+}
+
+// An asymmetric matrix ends the run as the reference's solvePoissonEquation
+// does (src/mps.cpp:425-439): print the pair and exit.
+void exitIfAsymmetric(int rc) {
+    if (rc == MPS_ERR_ASYMMETRIC) {
+        std::cout << mps_last_error() << std::endl;
+        std::exit(1);
+    }
+}
+}  // namespace
+
 // src/mps.cpp:111-130 (the whole step on the GPU); the debug events the
 // reference logs one by one are logged here as counts.
 double MPS::stepForward(const bool isTimeToExport) {
     if (!engine) throw std::runtime_error("MPS::stepForward before loadInitialState");
     const int rc = mps_step(engine.get(), isTimeToExport ? 1 : 0, &stats);
-    if (rc == MPS_ERR_ASYMMETRIC) {  // src/mps.cpp:425-439: print the pair and exit
-        std::cout << mps_last_error() << std::endl;
-        std::exit(1);
-    }
-    if (rc == MPS_ERR_NOT_CONVERGED)  // src/mps.cpp:462-464: the step goes on
-        mpslog::debug(std::string("Pressure calculation failed: ") + mps_last_error());
-    else
-        check(rc);
-    if (stats.n_new_ghosts > 0)
-        mpslog::debug(std::to_string(stats.n_new_ghosts) + " particle(s) went out of the domain.");
-    if (stats.n_unconnected > 0)
-        mpslog::debug("There is no Dirichlet boundary condition connected to " +
-                      std::to_string(stats.n_unconnected) + " particle(s).");
-    if (stats.courant > settings.cflCondition)
-        mpslog::debug("Courant number is larger than CFL condition. Courant=" + std::to_string(stats.courant));
-    if (stats.courant > 1.0) mpslog::error("Courant number is larger than 1.0. Exiting Simulation.");
+    exitIfAsymmetric(rc);
+    if (rc != MPS_ERR_NOT_CONVERGED) check(rc);
+    logStep(stats, settings.cflCondition);
     debugLogCount = stats.debug_log_count;
     if (isTimeToExport && syncOnExport) syncParticles();
     return stats.courant;
+}
+
+std::vector<mps_step_stats> MPS::stepForwardMany(int n) {
+    if (!engine) throw std::runtime_error("MPS::stepForwardMany before loadInitialState");
+    std::vector<mps_step_stats> st(n > 0 ? n : 0);
+    if (n <= 0) return st;
+    const int rc = mps_run_report(engine.get(), n, st.data());
+    exitIfAsymmetric(rc);
+    if (rc != MPS_ERR_NOT_CONVERGED) check(rc);
+    for (const auto& s : st) logStep(s, settings.cflCondition);
+    stats = st.back();
+    debugLogCount = stats.debug_log_count;
+    return st;
 }
 
 void MPS::beginExport() {

@@ -35,6 +35,10 @@ public:
 
     double loadInitialState();  // Initialize particles and return initial time
     double stepForward(const bool isTimeToExport);
+    // n non-export steps with one host wait per up to 256 of them; each
+    // step's stats (Courant number, debug counts) in order, with the same
+    // debug logging stepForward does per step.
+    std::vector<mps_step_stats> stepForwardMany(int n);
 
     // Additions of this implementation.
     void setSolver(int precision, double tol = 0.0, long long maxIter = 0);

@@ -26,14 +26,45 @@ void Simulation::run(const fs::path& inputYamlPath, int precision) {
 
     mpslog::info("START SIMULATION");
     simulationStartTime = system_clock::now();
-    while (time + mps.settings.dt <= mps.settings.finishTime) {
-        auto t0 = system_clock::now();
-        int before = mps.debugLogCount;
-        time += mps.settings.dt;
-        double courant = mps.stepForward(isTimeToExport());
-        if (isTimeToExport()) exportSnapshot();
-        timeStepReport(t0, system_clock::now(), courant, mps.debugLogCount > before);
-        timeStep++;
+    const double dt = mps.settings.dt, finish = mps.settings.finishTime;
+    while (time + dt <= finish) {
+        // The steps up to the next export step (or the end): the ones before
+        // it run back to back on the device with one host wait per group,
+        // and their report rows are written afterwards, each with its own
+        // device step time; the export step runs as the reference's loop.
+        int ahead = 0;
+        bool exportStep = false;
+        for (double t = time; t + dt <= finish;) {
+            t += dt;  // the same additions as the loop below
+            ahead++;
+            if (isTimeToExportAt(t)) {
+                exportStep = true;
+                break;
+            }
+        }
+        const int plain = exportStep ? ahead - 1 : ahead;
+        if (plain > 0) {
+            int before = mps.debugLogCount;
+            auto start = system_clock::now();
+            for (const mps_step_stats& s : mps.stepForwardMany(plain)) {
+                time += dt;
+                const auto end = start + std::chrono::duration_cast<system_clock::duration>(
+                                             std::chrono::duration<double, std::milli>(s.ms_step));
+                timeStepReport(start, end, s.courant, s.debug_log_count > before);
+                before = s.debug_log_count;
+                start = end;
+                timeStep++;
+            }
+        }
+        if (exportStep) {
+            auto t0 = system_clock::now();
+            int before = mps.debugLogCount;
+            time += dt;
+            double courant = mps.stepForward(true);
+            exportSnapshot();
+            timeStepReport(t0, system_clock::now(), courant, mps.debugLogCount > before);
+            timeStep++;
+        }
     }
     finishExport();
     simulationEndTime = system_clock::now();
@@ -103,9 +134,11 @@ void Simulation::timeStepReport(const system_clock::time_point& start, const sys
 }
 
 // src/simulation.cpp:224-229
-bool Simulation::isTimeToExport() {
+bool Simulation::isTimeToExport() { return isTimeToExportAt(time); }
+
+bool Simulation::isTimeToExportAt(double t) const {
     double interval = mps.settings.outputInterval;
-    double rem = std::fmod(time, interval);
+    double rem = std::fmod(t, interval);
     rem = std::min(rem, interval - rem);
     return rem < mps.settings.dt / 10.0;
 }

@@ -35,6 +35,7 @@ private:
                         const std::chrono::system_clock::time_point& timeStepEndTime,
                         const double& courantNumber, const bool& isDebugLogAdded);
     bool isTimeToExport();
+    bool isTimeToExportAt(double t) const;
     void exportParticles(const std::vector<Particle>& particles);
     void exportSnapshot();
     void finishExport();
