@@ -471,13 +471,24 @@ def run_accuracy_trajectory(prm, pos, vel, types, steps: int = 500, every: int =
     ef = Engine(prm, pos, vel, types, precision=FP64)
     rows, sec_m, sec_f = [], 0.0, 0.0
     its_m, its_f = [], []
+    first_flag_step = None  # the first step after which a surface flag differs
+    bm, bf = np.zeros(len(types), np.int32), np.zeros(len(types), np.int32)
     for s0 in range(0, steps, every):
-        dt_m, st_m = _event_timed(em.stream_ptr(), lambda: [em.step() for _ in range(every)])
-        dt_f, st_f = _event_timed(ef.stream_ptr(), lambda: [ef.step() for _ in range(every)])
+        dt_m = dt_f = 0.0
+        for s in range(s0 + 1, s0 + every + 1):
+            d, x = _event_timed(em.stream_ptr(), em.step)
+            dt_m += d
+            its_m.append(x["cg_iterations"])
+            d, x = _event_timed(ef.stream_ptr(), ef.step)
+            dt_f += d
+            its_f.append(x["cg_iterations"])
+            if first_flag_step is None:
+                em.download_into(bc=bm)
+                ef.download_into(bc=bf)
+                if not np.array_equal(bm, bf):
+                    first_flag_step = s
         sec_m += dt_m
         sec_f += dt_f
-        its_m += [x["cg_iterations"] for x in st_m]
-        its_f += [x["cg_iterations"] for x in st_f]
         a, b = em.state(), ef.state()
         pb = np.linalg.norm(b["pressure"]) or 1.0
         rows.append({"step": s0 + every,
@@ -489,7 +500,15 @@ def run_accuracy_trajectory(prm, pos, vel, types, steps: int = 500, every: int =
     em.close()
     ef.close()
     torch.cuda.synchronize()
+    before = [r for r in rows if first_flag_step is None or r["step"] < first_flag_step]
     return {"steps": steps, "every": every, "rows": rows,
+            "first_step_surface_flags_differ": first_flag_step,
+            "before_that": {"max_pressure_rel_l2": max((r["pressure_rel_l2"] for r in before), default=None),
+                            "max_position_abs_m": max((r["position_max_abs_m"] for r in before), default=None)},
+            "note": ("surface detection is a threshold on the number density (src/mps.cpp:262-278): "
+                     "once a particle within rounding of the threshold flips, the two trajectories "
+                     "follow different PPE systems; the FP64 GPU step and the CPU oracle part the "
+                     "same way (small_case.accuracy_vs_oracle)"),
             "max_pressure_rel_l2": max(r["pressure_rel_l2"] for r in rows),
             "max_position_abs_m": max(r["position_max_abs_m"] for r in rows),
             "mixed_value": nf * steps / sec_m, "fp64_value": nf * steps / sec_f, "unit": UNIT,
@@ -523,6 +542,39 @@ def run_precision_split(prm, state, steps: int = 4) -> dict:
     out["solve_speedup_preconditioner_on_top"] = j["ms_solve_mean"] / g["ms_solve_mean"]
     out["solve_speedup_total"] = f["ms_solve_mean"] / g["ms_solve_mean"]
     out["steps"] = steps
+    return out
+
+
+def run_collisions(steps: int = 12) -> dict:
+    """The collision pass with many candidates: the 25,600-particle
+    hydrostatic tank at dt = 1e-3 s (4x the stable dt / l0, so the fluid
+    churns and thousands of pairs collide per step), the same steps with the
+    pairs applied in parallel (default) and by one thread in order; the
+    states agree bit for bit (tests/test_gpu_collisions.py)."""
+    from mps_gb300 import FP64, Engine, scenes
+
+    l0 = 2.5e-3
+    prm, pos, vel, t = scenes.hydrostatic(l0, size=(0.4, 0.4), dt=1e-3)
+    rng = np.random.default_rng(0)
+    fl = t == scenes.FLUID
+    vel[fl, :2] = rng.normal(0.0, 0.01, (fl.sum(), 2))
+    out = {}
+    for name, serial in (("parallel", False), ("serial", True)):
+        e = Engine(prm, pos, vel, t, precision=FP64)
+        e.set_collisions(serial)
+        st = [e.step() for _ in range(steps)]
+        out[name] = {"ms_step": [round(x["ms_step"], 3) for x in st],
+                     "candidates": [int(x["n_collision_candidates"]) for x in st]}
+        out[name + "_state"] = e.state()
+        e.close()
+    same = all(np.array_equal(out["parallel_state"][k], out["serial_state"][k]) for k in out["serial_state"])
+    del out["parallel_state"], out["serial_state"]
+    busy = [i for i, c in enumerate(out["serial"]["candidates"]) if c > 1000]
+    tot = lambda k: float(sum(out[k]["ms_step"][i] for i in busy))  # noqa: E731
+    out.update({"workload": f"hydrostatic tank 0.4 x 0.4 m, l0 {l0} m, dt 1e-3 s, {steps} steps, FP64",
+                "states_bit_identical": bool(same),
+                "steps_with_over_1000_pairs": len(busy),
+                "ms_in_those_steps": {"parallel": tot("parallel"), "serial": tot("serial")}})
     return out
 
 
@@ -716,6 +768,7 @@ def run_ours(args, rank: int, world: int, dist):
         others["fp64_2m"] = run_fp64_2m(steps=3)
         others["small_case"] = run_small_case()
         others["export"] = run_export()
+        others["collisions"] = run_collisions()
 
     if rank != 0:
         return None

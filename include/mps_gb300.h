@@ -139,6 +139,14 @@ int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale);
  * MPS_OK when all 8 gave up with that status. */
 int mps_selftest_wait_limit(int32_t* blocks_gave_up, double* seconds);
 
+/* How the collision pass (src/mps.cpp:217-250) applies its candidate pairs.
+ * serial = 0 (default): in parallel, each pair after exactly the earlier
+ * pairs that touch its particles; serial = 1: one thread in the reference's
+ * order.  Both give the same state bit for bit (the serial form is kept for
+ * verification, and is what the parallel pass falls back to when one
+ * particle is the partner of more than 8 pairs in a step). */
+int mps_set_collisions(mps_engine* e, int32_t serial);
+
 /* Non-export steps run as a CUDA graph replay (default on): the first step
  * at each buffer parity captures the step's kernel sequence, later steps
  * replay it.  Changing the solver or the multigrid settings drops the

@@ -256,7 +256,7 @@ void enqueue_pre_solve(mps_engine* e) {
     if (taping) tape_phase(e, TAPE_EXPLICIT);
     launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
     e->swap();
-    launch_collision(c, e->S(), e->sc, e->cand_cnt, e->cand_base, nullptr, e->pairs, e->pair_cap,
+    launch_collision(c, e->S(), e->sc, e->cand_cnt, e->cand_base, e->cw, e->pairs, e->pair_cap,
                      e->sc.scan_tmp, e->ds, st);
     if (taping) tape_phase(e, TAPE_COLLISION);
     launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
@@ -632,6 +632,8 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         e->alloc(&e->kv.totals, 8) || e->alloc(&e->mf.idx8, np * K) ||
         e->alloc(&e->mf.sell_row, np) || e->alloc(&e->mf.rs, 3 * np) ||
         e->alloc(&e->cand_cnt, np + 1) || e->alloc(&e->cand_base, np + 2) ||
+        e->alloc(&e->cw.jn, np) || e->alloc(&e->cw.jl, np * kCollJList) || e->alloc(&e->cw.ver, np) ||
+        e->alloc(&e->cw.ctl, 4) ||
         e->alloc(&e->parent, np + 1) || e->alloc(&e->has_surface, np) || e->alloc(&e->ax, np) ||
         e->alloc(&e->ay, np) || e->alloc(&e->az, np) || e->alloc(&e->stage, 9 * np) ||
         e->alloc(&e->stage_i, 3 * np) || e->alloc(&e->dflag, 1) || e->alloc(&e->ds, 1))
@@ -778,6 +780,13 @@ int mps_selftest_wait_limit(int32_t* blocks_gave_up, double* seconds) {
     if (seconds) *seconds = ms * 1e-3;
     if (gave != kBlocks || !(status & ST_TIMEOUT))
         return fail(MPS_ERR_TIMEOUT, "mps_selftest_wait_limit: not every block gave up with the timeout status");
+    return MPS_OK;
+}
+
+int mps_set_collisions(mps_engine* e, int32_t serial) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    drop_graphs(e);
+    e->cw.serial = serial ? 1 : 0;
     return MPS_OK;
 }
 

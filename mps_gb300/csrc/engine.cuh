@@ -170,8 +170,17 @@ void launch_initial_number_density(const Consts& c, const StateBuf& s, const Sor
                                    const NbList& nb, DevStats* ds, cudaStream_t st);
 void launch_explicit(const Consts& c, const StateBuf& in, const StateBuf& out,
                      const SortScratch& sc, int mixed, DevStats* ds, cudaStream_t st);
+// Buffers of the collision pass's parallel application (sweeps.cu).
+constexpr int kCollJList = 8;
+struct CollWork {
+    int32_t* jn;     // per particle id: pairs that have it as the fluid partner j
+    int32_t* jl;     // per id: up to kCollJList of those pairs' indices (id * kCollJList + k)
+    int32_t* ver;    // per id: pairs applied so far that touch the particle
+    int32_t* ctl;    // [0] chunk ticket, [1] list overflow (the serial pass runs), [2] abort
+    int32_t serial;  // 1: every pair applied by one thread in order (verification mode)
+};
 void launch_collision(const Consts& c, const StateBuf& s, const SortScratch& sc,
-                      int32_t* cand_cnt, int32_t* cand_base, int32_t* order, CollPair* pairs,
+                      int32_t* cand_cnt, int32_t* cand_base, const CollWork& cw, CollPair* pairs,
                       int32_t pair_cap, int32_t* scan_tmp, DevStats* ds, cudaStream_t st);
 void launch_build_list(const Consts& c, const StateBuf& s, const SortScratch& sc,
                        const NbList& nb, DevStats* ds, cudaStream_t st);

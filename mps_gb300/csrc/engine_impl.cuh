@@ -61,6 +61,7 @@ struct mps_engine {
     // the batched kernel, which has no overlapped form)
     int32_t cycle_overlap = 1;
     int32_t *cand_cnt = nullptr, *cand_base = nullptr;
+    mpsg::CollWork cw{};
     mpsg::CollPair* pairs = nullptr;
     int32_t pair_cap = 0;
     int32_t* parent = nullptr;

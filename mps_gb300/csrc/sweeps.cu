@@ -14,6 +14,7 @@ namespace mpsg {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kCollBlocks = 304;  // blocks of the parallel collision pass (two per SM)
 
 inline int blocks_for(int n, int t = kThreads) { return (n + t - 1) / t; }
 
@@ -159,9 +160,21 @@ __global__ void __launch_bounds__(kThreads) k_explicit(Consts c, StateBuf in, St
 // ---------------------------------------------------------------------------
 // MPS::collision (src/mps.cpp:217-250).  The candidate pairs — fluid i,
 // neighbour j with the stale distance < cd, skipping fluid j with id >= id_i
-// — are found in parallel; their effect is order dependent (Gauss-Seidel,
-// in place), so they are then applied by one thread in ascending id_i and
-// sweep order, exactly as the reference's loop does.
+// — are found in parallel and laid out in the reference's order (ascending
+// id_i, sweep order).  Their effect is order dependent (Gauss-Seidel, in
+// place): pair t reads and writes the state of i and, for a fluid j, of j
+// (a wall j is read but never changed: its inverse density is 0).  Pair t
+// therefore depends exactly on the earlier pairs that touch i_t or a fluid
+// j_t, and applying every pair after those (in any order otherwise) gives
+// the serial loop's result bit for bit.  Each pair counts the earlier pairs
+// touching each of its particles: for i_t its position in i_t's own run of
+// pairs (no earlier pair has i_t as j: that needs id_i' > id_i_t); for j_t
+// the pairs of j_t's own run (all earlier) plus the earlier pairs with the
+// same j (from a short per-particle list).  A pair waits until the
+// particles' counters of applied pairs reach those numbers, applies itself
+// and increments them; chunks of pairs are taken in order from a ticket
+// counter, so every pair waited on belongs to a running or finished block.
+// More than kCollJList pairs with one j fall back to the serial pass.
 template <bool PLANAR>
 __device__ __forceinline__ int for_each_collision(const Consts& c, const StateBuf& s,
                                                   const int32_t* cs, int32_t key, int k,
@@ -212,52 +225,162 @@ __global__ void __launch_bounds__(kThreads) k_coll_write(Consts c, StateBuf s,
     for_each_collision<PLANAR>(c, s, cs, skey[k], k, pairs + b);
 }
 
+// One pair of the collision loop (the body of src/mps.cpp:222-247), with
+// loads and stores through L2 (other threads apply the neighbouring pairs).
+// A wall or dummy j has inverse density 0: its update adds +-0, which leaves
+// it unchanged unless it holds -0 (turned into +0); the parallel pass
+// (WRITE_WALL false) skips that store, so that pairs sharing a wall do not
+// race; walls hold no -0 (their velocities start at +0 and only such
+// updates touch them), so both passes give the same state.
+template <bool PLANAR, bool WRITE_WALL>
+__device__ __forceinline__ void coll_apply_pair(const Consts& c, const StateBuf& s, const CollPair& q,
+                                                double inv_rho) {
+    const int i = q.si, j = q.sj;
+    const double inv_i = inv_rho;  // i is fluid; Particle::inverseDensity, src/particle.cpp:19-29
+    const bool jfluid = s.type[j] == T_FLUID;
+    const bool wj = WRITE_WALL || jfluid;
+    const double inv_j = jfluid ? inv_rho : 0.0;
+    const double reduced = ddiv(1.0, dadd(inv_i, inv_j));
+    const double xi = __ldcg(s.x + i), yi = __ldcg(s.y + i), xj = __ldcg(s.x + j), yj = __ldcg(s.y + j);
+    const double dx = dsub(xj, xi), dy = dsub(yj, yi);
+    double zi = 0.0, zj = 0.0;
+    if (!PLANAR) {
+        zi = __ldcg(s.z + i);
+        zj = __ldcg(s.z + j);
+    }
+    const double dz = PLANAR ? 0.0 : dsub(zj, zi);
+    const double z2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+    double nx = dx, ny = dy, nz = dz;
+    if (z2 > 0.0) {
+        const double r = dsqrt(z2);
+        nx = ddiv(dx, r);
+        ny = ddiv(dy, r);
+        nz = ddiv(dz, r);
+    }
+    const double vxi = __ldcg(s.vx + i), vyi = __ldcg(s.vy + i), vxj = __ldcg(s.vx + j), vyj = __ldcg(s.vy + j);
+    double vzi = 0.0, vzj = 0.0;
+    if (!PLANAR) {
+        vzi = __ldcg(s.vz + i);
+        vzj = __ldcg(s.vz + j);
+    }
+    const double ux = dsub(vxj, vxi), uy = dsub(vyj, vyi);
+    const double uz = PLANAR ? 0.0 : dsub(vzj, vzi);
+    const double rel = dadd(dadd(dmul(ux, nx), dmul(uy, ny)), dmul(uz, nz));
+    if (rel < 0.0) {
+        const double impulse = dmul(dmul(-dadd(1.0, c.e), rel), reduced);
+        const double ci = dmul(impulse, inv_i), cj = dmul(impulse, inv_j);
+        __stcg(s.vx + i, dsub(vxi, dmul(ci, nx)));
+        __stcg(s.vy + i, dsub(vyi, dmul(ci, ny)));
+        if (wj) {
+            __stcg(s.vx + j, dadd(vxj, dmul(cj, nx)));
+            __stcg(s.vy + j, dadd(vyj, dmul(cj, ny)));
+        }
+        const double pimp = dmul(dsub(c.cd, q.dist), reduced);
+        const double pi_ = dmul(pimp, inv_i), pj_ = dmul(pimp, inv_j);
+        __stcg(s.x + i, dsub(xi, dmul(pi_, nx)));
+        __stcg(s.y + i, dsub(yi, dmul(pi_, ny)));
+        if (wj) {
+            __stcg(s.x + j, dadd(xj, dmul(pj_, nx)));
+            __stcg(s.y + j, dadd(yj, dmul(pj_, ny)));
+        }
+        if (!PLANAR) {
+            __stcg(s.vz + i, dsub(vzi, dmul(ci, nz)));
+            __stcg(s.z + i, dsub(zi, dmul(pi_, nz)));
+            if (wj) {
+                __stcg(s.vz + j, dadd(vzj, dmul(cj, nz)));
+                __stcg(s.z + j, dadd(zj, dmul(pj_, nz)));
+            }
+        }
+    }
+}
+
+// The serial pass: every pair in order by one thread (verification mode, or
+// when a particle is the partner of more than kCollJList pairs).  Also
+// reports the candidate count.
 template <bool PLANAR>
 __global__ void k_coll_apply(Consts c, StateBuf s, const CollPair* __restrict__ pairs,
-                             const int32_t* __restrict__ total_p, int32_t cap, DevStats* ds) {
+                             const int32_t* __restrict__ total_p, int32_t cap, CollWork cw, DevStats* ds) {
     int32_t total = *total_p;
     ds->n_cand = total;
     if (total > cap) total = cap;
-    const double inv_rho = ddiv(1.0, c.rho);  // Particle::inverseDensity, src/particle.cpp:19-29
-    for (int32_t t = 0; t < total; t++) {
-        CollPair q = pairs[t];
-        int i = q.si, j = q.sj;
-        double inv_i = inv_rho;  // i is fluid
-        double inv_j = s.type[j] == T_FLUID ? inv_rho : 0.0;
-        double reduced = ddiv(1.0, dadd(inv_i, inv_j));
-        double dx = dsub(s.x[j], s.x[i]), dy = dsub(s.y[j], s.y[i]);
-        double dz = PLANAR ? 0.0 : dsub(s.z[j], s.z[i]);
-        double z2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
-        double nx = dx, ny = dy, nz = dz;
-        if (z2 > 0.0) {
-            double r = dsqrt(z2);
-            nx = ddiv(dx, r);
-            ny = ddiv(dy, r);
-            nz = ddiv(dz, r);
+    if (!cw.serial && !cw.ctl[1]) return;  // the parallel pass applied them
+    const double inv_rho = ddiv(1.0, c.rho);
+    for (int32_t t = 0; t < total; t++) coll_apply_pair<PLANAR, true>(c, s, pairs[t], inv_rho);
+}
+
+// Per pair with a fluid partner j: its index in j's short list.
+__global__ void k_coll_jlists(StateBuf s, const CollPair* __restrict__ pairs, const int32_t* __restrict__ total_p,
+                              int32_t cap, CollWork cw) {
+    const int32_t total = min(*total_p, cap);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const CollPair q = pairs[t];
+        if (s.type[q.sj] != T_FLUID) continue;
+        const int p = atomicAdd(cw.jn + q.ij, 1);
+        if (p < kCollJList)
+            cw.jl[(size_t)q.ij * kCollJList + p] = t;
+        else
+            atomicOr(cw.ctl + 1, 1);
+    }
+}
+
+__device__ __forceinline__ int ld_acquire_i32(const int32_t* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Polls before a pair gives up waiting (~0.3 us each: ~2.5 s in all); a pair
+// that gives up raises ST_TIMEOUT and the abort flag, on which every waiting
+// pair gives up at once.
+constexpr int kCollSpinLimit = 1 << 23;
+
+template <bool PLANAR>
+__global__ void __launch_bounds__(kThreads) k_coll_wave(Consts c, StateBuf s, const CollPair* __restrict__ pairs,
+                                                        const int32_t* __restrict__ total_p, int32_t cap,
+                                                        const int32_t* __restrict__ cnt_by_id,
+                                                        const int32_t* __restrict__ base_by_id, CollWork cw,
+                                                        DevStats* ds) {
+    const int32_t total = min(*total_p, cap);
+    if (total == 0 || cw.serial || *(volatile int32_t*)(cw.ctl + 1)) return;
+    const double inv_rho = ddiv(1.0, c.rho);
+    __shared__ int s_chunk;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_chunk = atomicAdd(cw.ctl, 1);
+        __syncthreads();
+        const int t0 = s_chunk * (int)blockDim.x;
+        if (t0 >= total) return;
+        const int t = t0 + (int)threadIdx.x;
+        if (t >= total) continue;
+        const CollPair q = pairs[t];
+        const bool jf = s.type[q.sj] == T_FLUID;
+        const int ri = t - base_by_id[q.ii];
+        int rj = 0;
+        if (jf) {
+            rj = cnt_by_id[q.ij];
+            const int m = min(cw.jn[q.ij], kCollJList);
+            for (int u = 0; u < m; u++) rj += cw.jl[(size_t)q.ij * kCollJList + u] < t;
         }
-        double ux = dsub(s.vx[j], s.vx[i]), uy = dsub(s.vy[j], s.vy[i]);
-        double uz = PLANAR ? 0.0 : dsub(s.vz[j], s.vz[i]);
-        double rel = dadd(dadd(dmul(ux, nx), dmul(uy, ny)), dmul(uz, nz));
-        if (rel < 0.0) {
-            double impulse = dmul(dmul(-dadd(1.0, c.e), rel), reduced);
-            double ci = dmul(impulse, inv_i), cj = dmul(impulse, inv_j);
-            s.vx[i] = dsub(s.vx[i], dmul(ci, nx));
-            s.vy[i] = dsub(s.vy[i], dmul(ci, ny));
-            s.vx[j] = dadd(s.vx[j], dmul(cj, nx));
-            s.vy[j] = dadd(s.vy[j], dmul(cj, ny));
-            double pimp = dmul(dsub(c.cd, q.dist), reduced);
-            double pi_ = dmul(pimp, inv_i), pj_ = dmul(pimp, inv_j);
-            s.x[i] = dsub(s.x[i], dmul(pi_, nx));
-            s.y[i] = dsub(s.y[i], dmul(pi_, ny));
-            s.x[j] = dadd(s.x[j], dmul(pj_, nx));
-            s.y[j] = dadd(s.y[j], dmul(pj_, ny));
-            if (!PLANAR) {
-                s.vz[i] = dsub(s.vz[i], dmul(ci, nz));
-                s.vz[j] = dadd(s.vz[j], dmul(cj, nz));
-                s.z[i] = dsub(s.z[i], dmul(pi_, nz));
-                s.z[j] = dadd(s.z[j], dmul(pj_, nz));
+        bool go = true;
+        for (int it = 0; ld_acquire_i32(cw.ver + q.ii) != ri || (jf && ld_acquire_i32(cw.ver + q.ij) != rj);
+             it++) {
+            if (*(volatile int32_t*)(cw.ctl + 2)) {
+                go = false;
+                break;
             }
+            if (it > kCollSpinLimit) {
+                atomicOr(&ds->status, ST_TIMEOUT);
+                atomicExch(cw.ctl + 2, 1);
+                go = false;
+                break;
+            }
+            __nanosleep(64);
         }
+        if (!go) continue;
+        coll_apply_pair<PLANAR, false>(c, s, q, inv_rho);
+        __threadfence();
+        atomicAdd(cw.ver + q.ii, 1);
+        if (jf) atomicAdd(cw.ver + q.ij, 1);
     }
 }
 
@@ -711,7 +834,7 @@ void launch_explicit(const Consts& c, const StateBuf& in, const StateBuf& out,
 }
 
 void launch_collision(const Consts& c, const StateBuf& s, const SortScratch& sc,
-                      int32_t* cand_cnt, int32_t* cand_base, int32_t* /*order*/, CollPair* pairs,
+                      int32_t* cand_cnt, int32_t* cand_base, const CollWork& cw, CollPair* pairs,
                       int32_t pair_cap, int32_t* scan_tmp, DevStats* ds, cudaStream_t st) {
     int nb = blocks_for(c.n);
     cudaMemsetAsync(cand_cnt, 0, sizeof(int32_t) * (c.n + 1), st);
@@ -723,19 +846,33 @@ void launch_collision(const Consts& c, const StateBuf& s, const SortScratch& sc,
         ++g_launches;
     }
     launch_exclusive_scan(cand_cnt, cand_base, c.n, scan_tmp, st);
+    const int32_t* total = cand_base + c.n;
     if (c.planar) {
         k_coll_write<true><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt,
                                                     cand_base, pairs, pair_cap, ds);
-        ++g_launches;
-        k_coll_apply<true><<<1, 1, 0, st>>>(c, s, pairs, cand_base + c.n, pair_cap, ds);
-        ++g_launches;
     } else {
         k_coll_write<false><<<nb, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, cand_cnt,
                                                      cand_base, pairs, pair_cap, ds);
-        ++g_launches;
-        k_coll_apply<false><<<1, 1, 0, st>>>(c, s, pairs, cand_base + c.n, pair_cap, ds);
-        ++g_launches;
     }
+    ++g_launches;
+    if (!cw.serial) {
+        cudaMemsetAsync(cw.jn, 0, sizeof(int32_t) * c.n, st);
+        cudaMemsetAsync(cw.ver, 0, sizeof(int32_t) * c.n, st);
+        cudaMemsetAsync(cw.ctl, 0, sizeof(int32_t) * 4, st);
+        k_coll_jlists<<<kCollBlocks, kThreads, 0, st>>>(s, pairs, total, pair_cap, cw);
+        if (c.planar)
+            k_coll_wave<true><<<kCollBlocks, kThreads, 0, st>>>(c, s, pairs, total, pair_cap, cand_cnt,
+                                                                cand_base, cw, ds);
+        else
+            k_coll_wave<false><<<kCollBlocks, kThreads, 0, st>>>(c, s, pairs, total, pair_cap, cand_cnt,
+                                                                 cand_base, cw, ds);
+        g_launches += 2;
+    }
+    if (c.planar)
+        k_coll_apply<true><<<1, 1, 0, st>>>(c, s, pairs, total, pair_cap, cw, ds);
+    else
+        k_coll_apply<false><<<1, 1, 0, st>>>(c, s, pairs, total, pair_cap, cw, ds);
+    ++g_launches;
 }
 
 void launch_build_list(const Consts& c, const StateBuf& s, const SortScratch& sc,

@@ -115,6 +115,8 @@ def load(build_if_missing: bool = False):
     L.mps_set_solver.argtypes = [vp, C.c_int32, C.c_double, C.c_int64]
     L.mps_set_multigrid.argtypes = [vp, C.c_int32, C.c_float, C.c_float]
     L.mps_set_multigrid.restype = C.c_int
+    L.mps_set_collisions.argtypes = [vp, C.c_int32]
+    L.mps_set_collisions.restype = C.c_int
     L.mps_set_graphs.argtypes = [vp, C.c_int32]
     L.mps_set_graphs.restype = C.c_int
     L.mps_step.argtypes = [vp, C.c_int32, P(MpsStepStats)]
@@ -307,6 +309,10 @@ class Engine:
         omega/scale 0 take the mode's default weights."""
         mode = int(mode) if not isinstance(mode, bool) else (1 if mode else 0)
         _check(_lib.mps_set_multigrid(self._h, mode, float(omega), float(scale)))
+
+    def set_collisions(self, serial=False):
+        """Collision pairs applied in parallel (default) or by one thread in order."""
+        _check(_lib.mps_set_collisions(self._h, 1 if serial else 0))
 
     def set_graphs(self, enabled=True):
         """Non-export steps as CUDA graph replays (default) or eager launches."""
