@@ -1,8 +1,8 @@
 """The collision pass's parallel application (each candidate pair applied
 after exactly the earlier pairs that touch its particles) against the
 serial application in the reference's order (src/mps.cpp:217-250): the same
-state bit for bit, on the golden jittered scene and on a hydrostatic tank
-run at a time step where it has thousands of candidate pairs per step."""
+state bit for bit, on the golden jittered scene and on a shaken dam-break
+column with thousands of candidate pairs per step."""
 import numpy as np
 import pytest
 
@@ -46,16 +46,14 @@ def test_parallel_collisions_match_serial_on_golden_scene(precision):
 
 
 def test_parallel_collisions_match_serial_with_thousands_of_pairs():
-    """The 25,600-particle hydrostatic tank at dt = 1e-3 s (4x the stable
-    dt / l0): within a few steps thousands of pairs collide every step."""
+    """A 200 x 200 dam-break column shaken (positions +-0.4 l0, velocities
+    N(0, 0.1) m/s): thousands of candidate pairs in the first steps, at most a
+    few per particle, so the parallel pass (not its serial fallback) runs."""
     m = engine_or_skip()
     from mps_gb300 import scenes
 
     l0 = 2.5e-3
-    prm, pos, vel, t = scenes.hydrostatic(l0, size=(0.4, 0.4), dt=1e-3)
-    rng = np.random.default_rng(0)
-    fl = t == scenes.FLUID
-    vel[fl, :2] = rng.normal(0.0, 0.01, (fl.sum(), 2))
-    most, per_partner = _compare(m, prm, pos, vel, t, 12, m.FP64)
+    scene = scenes.shaken(scenes.dam_break(l0, tank=(1.0, 0.8), column=(0.5, 0.5), dt=2.5e-4))
+    most, per_partner = _compare(m, *scene, 4, m.FP64)
     assert most > 2000, most
-    print(f"candidates {most}, most pairs with one partner {per_partner}")
+    assert 0 < per_partner <= 8, per_partner
