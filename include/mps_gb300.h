@@ -186,6 +186,18 @@ int mps_run_report(mps_engine* e, int32_t n_steps, mps_step_stats* stats);
 int mps_check_symmetry(int32_t n, const int64_t* row_ptr, const int32_t* col, const double* val,
                        int32_t* pair_i, int32_t* pair_j);
 
+/* Self-check of the correctly rounded FP64 square root and division that the
+ * sweeps compute on the integer and FP32 pipes, against the GPU's FP64
+ * instructions, on n seeded cases of each (random significands and
+ * exponents, the significands next to 2^52 and 2^53, equal significands, the
+ * sweeps' operand ranges), on the current device.  result[0] and result[1]:
+ * square-root and quotient mismatches (0 when the routines are exact);
+ * result[2] and result[3]: the cases that took the integer path (the others
+ * are outside it: zero, subnormal, non-finite, or a quotient outside the
+ * normal range); result[4..6]: the first mismatch's operand bits and its kind
+ * (1 square root, 2 quotient), zeros if none.  MPS_OK or MPS_ERR_CUDA. */
+int mps_selftest_exact64(uint64_t n, uint64_t seed, uint64_t* result);
+
 /* Asynchronous export (the reference's Simulation::exportParticles,
  * src/simulation.cpp:231-245, and Exporter, src/exporter.cpp:10-167).
  * mps_export_begin snapshots the current state in id order: gathers on the

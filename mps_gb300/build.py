@@ -28,7 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--extended-lambda", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(REPO, "include")]
 ENGINE_SRCS = ["sort.cu", "sweeps.cu", "solver.cu", "mg.cu", "capi.cu", "adjoint.cu", "batch.cu", "noalloc.cu",
-               "io.cu", "symcheck.cu"]
+               "io.cu", "symcheck.cu", "selftest.cu"]
 
 
 def nvcc() -> str:

@@ -5,6 +5,7 @@
 #include <cstdint>
 
 #include "engine.cuh"
+#include "exact64.cuh"
 
 namespace mpsg {
 
@@ -13,8 +14,40 @@ namespace mpsg {
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
-__device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
+
+// The FP32 starting points of the integer-pipe square root and division:
+// the hardware approximations (2 ulp each, documented).
+struct Fp32Approx {
+    static __host__ __device__ __forceinline__ float rsqrt(float x) {
+#ifdef __CUDA_ARCH__
+        return rsqrtf(x);
+#else
+        return 1.0f / sqrtf(x);
+#endif
+    }
+    static __host__ __device__ __forceinline__ float rcp(float x) {
+#ifdef __CUDA_ARCH__
+        return __fdividef(1.0f, x);
+#else
+        return 1.0f / x;
+#endif
+    }
+};
+
+// Correctly rounded FP64 division and square root.  Normal operands with a
+// normal result (all of the sweeps' distances and weights) are computed on
+// the integer and FP32 pipes (exact64.cuh), the rest by the FP64 instruction
+// sequence; both give the IEEE round-to-nearest result.
+__device__ __forceinline__ double ddiv(double a, double b) {
+    double q;
+    if (x64::div_rn<Fp32Approx>(a, b, q)) return q;
+    return __ddiv_rn(a, b);
+}
+__device__ __forceinline__ double dsqrt(double a) {
+    double r;
+    if (x64::sqrt_rn<Fp32Approx>(a, r)) return r;
+    return __dsqrt_rn(a);
+}
 
 // weight(): src/mps.cpp:9-16
 __device__ __forceinline__ double weight(double dist, double re) {

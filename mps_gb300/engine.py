@@ -169,6 +169,8 @@ def load(build_if_missing: bool = False):
     L.mps_selftest_wait_limit.restype = C.c_int
     L.mps_check_symmetry.argtypes = [C.c_int32, vp, vp, vp, P(C.c_int32), P(C.c_int32)]
     L.mps_check_symmetry.restype = C.c_int
+    L.mps_selftest_exact64.argtypes = [C.c_uint64, C.c_uint64, P(C.c_uint64)]
+    L.mps_selftest_exact64.restype = C.c_int
     L.mps_last_error.restype = C.c_char_p
     for name in ("mps_create", "mps_destroy", "mps_set_solver", "mps_step", "mps_run",
                  "mps_download", "mps_upload", "mps_neighbors", "mps_system", "mps_collisions"):
@@ -233,6 +235,18 @@ def check_symmetry(row_ptr, col, val):
     i, j = C.c_int32(-2), C.c_int32(-2)
     rc = L.mps_check_symmetry(len(rp) - 1, _p(rp), _p(cl), _p(vl), C.byref(i), C.byref(j))
     return rc, i.value, j.value, (L.mps_last_error().decode() if rc else "")
+
+
+def selftest_exact64(n: int, seed: int = 1):
+    """mps_selftest_exact64: the integer-pipe FP64 square root and division
+    against the GPU's FP64 instructions on n seeded cases of each.  Returns
+    (return code, dict with sqrt_mismatches, div_mismatches, sqrt_fast,
+    div_fast, first_bad)."""
+    L = load()
+    res = (C.c_uint64 * 7)()
+    rc = L.mps_selftest_exact64(int(n), int(seed), res)
+    return rc, {"sqrt_mismatches": res[0], "div_mismatches": res[1], "sqrt_fast": res[2],
+                "div_fast": res[3], "first_bad": (res[4], res[5], res[6])}
 
 
 def make_params(p: dict) -> MpsParams:
