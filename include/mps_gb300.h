@@ -195,7 +195,10 @@ int mps_check_symmetry(int32_t n, const int64_t* row_ptr, const int32_t* col, co
  * result[2] and result[3]: the cases that took the integer path (the others
  * are outside it: zero, subnormal, non-finite, or a quotient outside the
  * normal range); result[4..6]: the first mismatch's operand bits and its kind
- * (1 square root, 2 quotient), zeros if none.  MPS_OK or MPS_ERR_CUDA. */
+ * (1 square root, 2 quotient), zeros if none; result[7]: mismatches of the
+ * exact subtraction of 1 in the weight function, the FP32 rounding and the
+ * distance-cutoff comparison done on the integer pipe.  result holds 8
+ * values.  MPS_OK or MPS_ERR_CUDA. */
 int mps_selftest_exact64(uint64_t n, uint64_t seed, uint64_t* result);
 
 /* Asynchronous export (the reference's Simulation::exportParticles,

@@ -34,6 +34,14 @@ struct Fp32Approx {
     }
 };
 
+// The FP64 instructions for the operands outside the integer paths below.
+// They are separate functions so that the compiler branches to them instead
+// of issuing them, predicated off, on every call.
+static __device__ __noinline__ double ddiv_fp64(double a, double b) { return __ddiv_rn(a, b); }
+static __device__ __noinline__ double dsqrt_fp64(double a) { return __dsqrt_rn(a); }
+static __device__ __noinline__ double dsub_fp64(double a, double b) { return __dsub_rn(a, b); }
+static __device__ __noinline__ float f32_fp64(double x) { return __double2float_rn(x); }
+
 // Correctly rounded FP64 division and square root.  Normal operands with a
 // normal result (all of the sweeps' distances and weights) are computed on
 // the integer and FP32 pipes (exact64.cuh), the rest by the FP64 instruction
@@ -41,17 +49,35 @@ struct Fp32Approx {
 __device__ __forceinline__ double ddiv(double a, double b) {
     double q;
     if (x64::div_rn<Fp32Approx>(a, b, q)) return q;
-    return __ddiv_rn(a, b);
+    return ddiv_fp64(a, b);
 }
 __device__ __forceinline__ double dsqrt(double a) {
     double r;
     if (x64::sqrt_rn<Fp32Approx>(a, r)) return r;
-    return __dsqrt_rn(a);
+    return dsqrt_fp64(a);
 }
 
-// weight(): src/mps.cpp:9-16
+// FP32 rounding of a double (nearest, ties to even) without the conversion
+// instruction, which runs on the FP64 pipe: the same value as (float)x.
+__device__ __forceinline__ float f32(double x) {
+    float f;
+    if (x64::to_f32(x, f)) return f;
+    return f32_fp64(x);
+}
+
+// v < cut for a cut > 0 and a v that is >= 0 or NaN (squared distances and
+// distances), on the integer pipe: the same result as the FP64 comparison.
+__device__ __forceinline__ bool lt_cut(double v, double cut) { return x64::lt_cut(v, cut); }
+
+// weight(): src/mps.cpp:9-16.  re / dist >= 1 when dist < re, so the
+// subtraction of 1 is exact and done on the integer pipe (the FP64 one only
+// for re / dist >= 2^53).
 __device__ __forceinline__ double weight(double dist, double re) {
-    return dist < re ? dsub(ddiv(re, dist), 1.0) : 0.0;
+    if (!lt_cut(dist, re)) return 0.0;
+    const double q = ddiv(re, dist);
+    double w;
+    if (x64::sub_one(q, w)) return w;
+    return dsub_fp64(q, 1.0);
 }
 
 // Cell coordinate int((x - lo) / len) + 1 (src/bucket.cpp:40-42,

@@ -114,6 +114,54 @@ MPS_X64_FN uint64_t u_of_big(float f) {
     return (uint64_t)((u & 0x7FFFFFu) | 0x800000u) << ((u >> 23) - 150u);
 }
 
+MPS_X64_FN int clz64(uint64_t v) {
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)v);
+#else
+    return __builtin_clzll(v);
+#endif
+}
+
+// q - 1 for 1 <= q < 2^53, which is exact (a multiple of q's unit in the last
+// place, below q); false for any other q.
+MPS_X64_FN bool sub_one(double q, double& out) {
+    const uint64_t Q = bits_of(q);
+    const uint32_t E = (uint32_t)(Q >> 52);  // the sign bit included
+    if (E - 1023u > 52u) return false;
+    const uint64_t D = ((Q & kMant) | kHidden) - (1ull << (1075u - E));
+    if (D == 0) {
+        out = 0.0;
+        return true;
+    }
+    const int lz = clz64(D) - 11;
+    out = double_of(((uint64_t)(E - (uint32_t)lz - 1u) << 52) + (D << lz));
+    return true;
+}
+
+// x rounded to FP32 (nearest, ties to even) for zero and for x in the FP32
+// normal range; false for the rest (subnormal or overflowing results, inf,
+// NaN).
+MPS_X64_FN bool to_f32(double x, float& out) {
+    const uint64_t X = bits_of(x);
+    const uint32_t E = (uint32_t)(X >> 52) & 0x7ffu;
+    const uint32_t sign = (uint32_t)(X >> 32) & 0x80000000u;
+    if (E - 897u > 253u) {
+        if ((X << 1) != 0) return false;
+        out = f_of(sign);
+        return true;
+    }
+    const uint64_t m = X & kMant;
+    const uint32_t top = (uint32_t)(m >> 29);
+    const uint32_t rem = (uint32_t)m & 0x1FFFFFFFu;
+    const uint32_t up = (rem > 0x10000000u || (rem == 0x10000000u && (top & 1u))) ? 1u : 0u;
+    out = f_of(sign | ((((E - 896u) << 23) | top) + up));
+    return true;
+}
+
+// v < cut for a cut > 0 and a v that is >= 0 or NaN (a squared distance or a
+// distance): the order of such doubles is the order of their bit patterns.
+MPS_X64_FN bool lt_cut(double v, double cut) { return (int64_t)bits_of(v) < (int64_t)bits_of(cut); }
+
 // One Newton step on FP32 approximations of 1/sqrt(x) and 1/x: relative
 // error below 2^-12 in, below 2^-22.5 out.
 MPS_X64_FN float refine_rsqrt(float x, float y) {

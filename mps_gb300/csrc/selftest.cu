@@ -33,11 +33,13 @@ __device__ __forceinline__ uint64_t test_mant(uint64_t r) {
 }
 
 // counts[0]: square-root mismatches, [1]: quotient mismatches, [2]/[3]: the
-// cases that took the integer path; bad[0..2]: the first mismatch's operands
-// (x or a, b) in bit form, claimed once.
+// cases that took the integer path, [4]: mismatches of the exact subtraction
+// of 1, the FP32 rounding and the comparison shortcut; bad[0..2]: the first
+// square-root or quotient mismatch's operands (x or a, b) in bit form,
+// claimed once.
 __global__ void k_exact64_check(uint64_t n, uint64_t seed, unsigned long long* counts,
                                 unsigned long long* bad) {
-    unsigned long long mis_s = 0, mis_d = 0, fast_s = 0, fast_d = 0;
+    unsigned long long mis_s = 0, mis_d = 0, fast_s = 0, fast_d = 0, mis_o = 0;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t r0 = splitmix(seed ^ (i * 0xD1B54A32D192ED03ull));
@@ -58,6 +60,13 @@ __global__ void k_exact64_check(uint64_t n, uint64_t seed, unsigned long long* c
             b = x64::double_of(((uint64_t)eb << 52) | (mb & x64::kMant) | ((r1 & 2) << 62));
         }
         double got;
+        // the exact subtraction of 1, FP32 rounding and ordering shortcut
+        const double q = 1.0 + (double)(r0 >> 11) * 0x1p-53 * 64.0;
+        double q1;
+        float f;
+        if (!x64::sub_one(q, q1) || x64::bits_of(q1) != x64::bits_of(__dsub_rn(q, 1.0))) mis_o++;
+        if (x64::to_f32(a, f) && __float_as_uint(f) != __float_as_uint(__double2float_rn(a))) mis_o++;
+        if (x64::lt_cut(fabs(a), fabs(b)) != (fabs(a) < fabs(b))) mis_o++;
         if (x64::sqrt_rn<Fp32Approx>(x, got)) {
             fast_s++;
             if (x64::bits_of(got) != x64::bits_of(__dsqrt_rn(x))) {
@@ -81,6 +90,7 @@ __global__ void k_exact64_check(uint64_t n, uint64_t seed, unsigned long long* c
             }
         }
     }
+    if (mis_o) atomicAdd(counts + 4, mis_o);
     if (mis_s) atomicAdd(counts + 0, mis_s);
     if (mis_d) atomicAdd(counts + 1, mis_d);
     atomicAdd(counts + 2, fast_s);
@@ -98,19 +108,22 @@ extern "C" int mps_selftest_exact64(uint64_t n, uint64_t seed, uint64_t* result)
         return MPS_ERR_ARG;
     }
     unsigned long long* d = nullptr;
-    cudaError_t ce = cudaMalloc(&d, 8 * sizeof(unsigned long long));
-    if (ce == cudaSuccess) ce = cudaMemset(d, 0, 8 * sizeof(unsigned long long));
+    cudaError_t ce = cudaMalloc(&d, 9 * sizeof(unsigned long long));
+    if (ce == cudaSuccess) ce = cudaMemset(d, 0, 9 * sizeof(unsigned long long));
     if (ce == cudaSuccess) {
-        k_exact64_check<<<4 * 152, 256>>>(n, seed, d, d + 4);
+        k_exact64_check<<<4 * 152, 256>>>(n, seed, d, d + 5);
         ce = cudaGetLastError();
     }
-    unsigned long long h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long h[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (ce == cudaSuccess) ce = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
     if (d) cudaFree(d);
     if (ce != cudaSuccess) {
         set_last_error(std::string("mps_selftest_exact64: ") + cudaGetErrorString(ce));
         return MPS_ERR_CUDA;
     }
-    for (int k = 0; k < 7; k++) result[k] = h[k];
+    // result: sqrt/div mismatches, fast counts, first bad (3), other mismatches
+    for (int k = 0; k < 4; k++) result[k] = h[k];
+    for (int k = 0; k < 3; k++) result[4 + k] = h[5 + k];
+    result[7] = h[4];
     return MPS_OK;
 }

@@ -198,6 +198,95 @@ __device__ __forceinline__ bool reduce_sync(GridBar& gb, const double (&v)[M], d
     return true;
 }
 
+// Double-float (hi + lo, FP32 pair) sums: the per-iteration dot products of
+// the mixed solver are reduced with FP32 instructions only.  This part issues
+// FP64 at 1/64 of the FP32 rate (one FP64 warp instruction holds its SM
+// quarter's FP64 unit for ~80 cycles), so the ~120 dependent FP64 additions
+// of a block-and-grid reduction in FP64 cost ~7 us per iteration on the
+// critical path; the pair sums keep ~44 bits, far more than an FP32 Krylov
+// iteration needs.
+struct F2 {
+    float hi, lo;
+};
+
+// Knuth's two-sum of the high parts, low parts added, renormalised.
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    const float err = (a.hi - (s - bb)) + (b.hi - bb);
+    const float lo = (a.lo + b.lo) + err;
+    const float hi = s + lo;
+    return F2{hi, lo - (hi - s)};
+}
+
+__device__ __forceinline__ F2 f2_shfl_down(F2 v, int o) {
+    return F2{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+
+// As publish_partials / sum_partials, on pairs: every warp reduces its lanes
+// by a shuffle tree, warp 0 the warps' results, and each block's M pairs go
+// to the partials buffer; after the barrier every block sums the partials in
+// the same order (bitwise the same totals everywhere) and rounds each total
+// to FP32.
+template <int M, int BS>
+__device__ __forceinline__ const F2* publish_partials_f2(GridBar& gb, const F2 (&v)[M]) {
+    constexpr int kW = BS / 32;
+    static_assert(kW <= 32 && M <= 8, "one warp reduces the warps' pairs");
+    __shared__ F2 sh[M][kW];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    F2* part = reinterpret_cast<F2*>(gb.partials + (size_t)gb.parity * gb.size * 8);
+    gb.parity ^= 1;
+#pragma unroll
+    for (int m = 0; m < M; m++) {
+        F2 a = v[m];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a = f2_add(a, f2_shfl_down(a, o));
+        if (lane == 0) sh[m][warp] = a;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+            F2 a = lane < kW ? sh[m][lane] : F2{0.f, 0.f};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a = f2_add(a, f2_shfl_down(a, o));
+            if (lane == 0) part[gb.rank * 8 + m] = a;
+        }
+    }
+    return part;
+}
+
+template <int M>
+__device__ __forceinline__ void sum_partials_f2(const GridBar& gb, const F2* part, float (&tot)[M]) {
+    __shared__ float s_tot[M];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 0) {
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+            F2 a = {0.f, 0.f};
+            for (int b = lane; b < gb.size; b += 32) {
+                const float2 q = __ldcg(reinterpret_cast<const float2*>(part + b * 8 + m));
+                a = f2_add(a, F2{q.x, q.y});
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a = f2_add(a, f2_shfl_down(a, o));
+            if (lane == 0) s_tot[m] = a.hi + a.lo;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < M; m++) tot[m] = s_tot[m];
+}
+
+template <int M, int BS>
+__device__ __forceinline__ bool reduce_sync_f2(GridBar& gb, const F2 (&v)[M], float (&tot)[M],
+                                               DevStats* ds) {
+    const F2* part = publish_partials_f2<M, BS>(gb, v);
+    if (!grid_sync(gb, ds)) return false;
+    sum_partials_f2<M>(gb, part, tot);
+    return true;
+}
+
 // ------------------------------------------------------------------ SpMV
 // y_i = sum over the SELL-32 row (padding entries are (i, 0)) + diag_i x_i,
 // loads batched four at a time so that gathers overlap.
@@ -488,9 +577,6 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg64(Ppe A, Krylov kv, SolveArgs 
 
 // --------------------------------------------------------------- mixed IR
 // Error-free FP32 product accumulated with compensation (hi, lo).
-struct F2 {
-    float hi, lo;
-};
 __device__ __forceinline__ void acc_prod(F2& a, float x, float y) {
     float p = x * y;
     float e = fmaf(x, y, -p);
@@ -500,7 +586,6 @@ __device__ __forceinline__ void acc_prod(F2& a, float x, float y) {
     a.hi = s;
     a.lo += err + e;
 }
-__device__ __forceinline__ double f2d(const F2& a) { return (double)a.hi + (double)a.lo; }
 
 // Loads of multigrid data: the vectors change during the solve (L2), the
 // stencils and inverse diagonals do not (read-only cache).
@@ -1031,7 +1116,7 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, con
         const float ithr = (float)fmax(a.inner_tol * a.inner_tol, 0.25 * thr / rn2);
         const float scale = (float)(1.0 / sqrt(rn2));
         for (int i = gtid; i < a.n; i += gsz) {
-            float r = (float)kv.r[i] * scale;
+            float r = f32(kv.r[i]) * scale;
             kv.r32[i] = r;
             kv.x32[i] = 0.f;
             kv.p32[i] = 0.f;
@@ -1078,10 +1163,11 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, con
                     acc_prod(rr, rv[h], rv[h]);
                 }
             }
-            double v3[3] = {f2d(g), f2d(dl), f2d(rr)}, t3[3];
-            if (!reduce_sync<3, BS>(gb, v3, t3, ds)) return;
-            if ((float)t3[2] < ithr || inner_total + k >= a.max_iter) break;
-            const float gamma = (float)t3[0], delta = (float)t3[1];
+            const F2 v3[3] = {g, dl, rr};
+            float t3[3];
+            if (!reduce_sync_f2<3, BS>(gb, v3, t3, ds)) return;
+            if (t3[2] < ithr || inner_total + k >= a.max_iter) break;
+            const float gamma = t3[0], delta = t3[1];
             if (k == 0) {
                 beta = 0.f;
                 alpha = gamma / delta;
@@ -1248,7 +1334,7 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
         const float ithr = (float)fmax(a.inner_tol * a.inner_tol, 0.25 * thr / rn2);
         const float scale = (float)(1.0 / sqrt(rn2));
         for (int i = gtid; i < n; i += gsz) {
-            const float r = (float)kv.r[i] * scale;
+            const float r = f32(kv.r[i]) * scale;
             kv.r32[i] = r;
             kv.x32[i] = 0.f;
             kv.p32[i] = 0.f;
@@ -1334,10 +1420,11 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
                     acc_prod(rr, ri[h], ri[h]);
                 }
             }
-            double v3[3] = {f2d(g), f2d(dl), f2d(rr)}, t3[3];
-            if (!reduce_sync<3, BS>(gb, v3, t3, ds)) return;
-            if ((float)t3[2] < ithr || inner_total + k >= a.max_iter) break;
-            const float gamma = (float)t3[0], delta = (float)t3[1];
+            const F2 v3[3] = {g, dl, rr};
+            float t3[3];
+            if (!reduce_sync_f2<3, BS>(gb, v3, t3, ds)) return;
+            if (t3[2] < ithr || inner_total + k >= a.max_iter) break;
+            const float gamma = t3[0], delta = t3[1];
             if (k == 0) {
                 beta = 0.f;
                 alpha = gamma / delta;
@@ -1439,8 +1526,8 @@ __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.n) return;
     const double d = A.diag[k];
-    A.diag32[k] = (float)d;
-    kv.inv_diag32[k] = d != 0.0 ? (float)(1.0 / d) : 1.f;
+    A.diag32[k] = f32(d);
+    kv.inv_diag32[k] = d != 0.0 ? f32(ddiv(1.0, d)) : 1.f;
     const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
     const int w = A.slice_w[k >> 5];
     const int wq = (w + 3) & ~3;
@@ -1472,7 +1559,7 @@ __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
     }
     mf.sell_row[k] = sell;
     for (int m = 0; m < wq; m++)
-        A.val32[qsell_index(k, m, c.K)] = m < w ? (float)A.val[base + (size_t)m * 32] : 0.f;
+        A.val32[qsell_index(k, m, c.K)] = m < w ? f32(A.val[base + (size_t)m * 32]) : 0.f;
 }
 
 // Co-resident blocks of a persistent kernel (0 if the configuration does not

@@ -95,14 +95,14 @@ __global__ void k_gather(int n, const int32_t* __restrict__ perm, const int32_t*
     const double x = in.x[o], y = in.y[o];
     out.x[k] = x;
     out.y[k] = y;
-    out.xf[k] = (float)x;
-    out.yf[k] = (float)y;
+    out.xf[k] = f32(x);
+    out.yf[k] = f32(y);
     out.vx[k] = in.vx[o];
     out.vy[k] = in.vy[o];
     if (!planar) {
         const double z = in.z[o];
         out.z[k] = z;
-        out.zf[k] = (float)z;
+        out.zf[k] = f32(z);
         out.vz[k] = in.vz[o];
     }
     out.p[k] = in.p[o];

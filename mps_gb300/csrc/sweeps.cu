@@ -66,7 +66,7 @@ __device__ double sweep_number_density_p(const Consts& c, const StateBuf& s, con
     for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
         if (j == k || far32<PLANAR>(s, j, fx, fy, fz, c.ft_max)) return;
         double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
-        if (d2 < c.t_max && d2 < c.t_p) nd = dadd(nd, weight(dsqrt(d2), c.re_p));
+        if (lt_cut(d2, c.t_max) && lt_cut(d2, c.t_p)) nd = dadd(nd, weight(dsqrt(d2), c.re_p));
     });
     return nd;
 }
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kThreads) k_explicit(Consts c, StateBuf in, St
             double tx = 0.0, ty = 0.0, tz = 0.0;
             for_each_near<PLANAR>(c, in, cs, key, k, c.ft_v, [&](int j) {
                 double d2 = dist2<PLANAR>(in, k, j, x, y, z);
-                if (d2 < c.t_max && d2 < c.t_v) {
+                if (lt_cut(d2, c.t_max) && lt_cut(d2, c.t_v)) {
                     double w = weight(dsqrt(d2), c.re_v);
                     tx = dadd(tx, dmul(dsub(in.vx[j], vx), w));
                     ty = dadd(ty, dmul(dsub(in.vy[j], vy), w));
@@ -107,14 +107,14 @@ __global__ void __launch_bounds__(kThreads) k_explicit(Consts c, StateBuf in, St
             // FP32 weights and FP32 accumulation; the neighbour set is the
             // exact FP64 one.
             float tx = 0.f, ty = 0.f, tz = 0.f;
-            const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
+            const float fvx = f32(vx), fvy = f32(vy), fvz = f32(vz);
             for_each_near<PLANAR>(c, in, cs, key, k, c.ft_v, [&](int j) {
                 double d2 = dist2<PLANAR>(in, k, j, x, y, z);
-                if (d2 < c.t_max && d2 < c.t_v) {
-                    float w = c.fre_v * rsqrtf((float)d2) - 1.f;
-                    tx = fmaf((float)in.vx[j] - fvx, w, tx);
-                    ty = fmaf((float)in.vy[j] - fvy, w, ty);
-                    if (!PLANAR) tz = fmaf((float)in.vz[j] - fvz, w, tz);
+                if (lt_cut(d2, c.t_max) && lt_cut(d2, c.t_v)) {
+                    float w = c.fre_v * rsqrtf(f32(d2)) - 1.f;
+                    tx = fmaf(f32(in.vx[j]) - fvx, w, tx);
+                    ty = fmaf(f32(in.vy[j]) - fvy, w, ty);
+                    if (!PLANAR) tz = fmaf(f32(in.vz[j]) - fvz, w, tz);
                 }
             });
             ax = c.g[0] + (double)(tx * c.fvisc_a);
@@ -186,7 +186,7 @@ __device__ __forceinline__ int for_each_collision(const Consts& c, const StateBu
     for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
         if (j == k || far32<PLANAR>(s, j, fx, fy, fz, c.ft_cd)) return;
         double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
-        if (!(d2 < c.t_max && d2 < c.t_cd)) return;
+        if (!(lt_cut(d2, c.t_max) && lt_cut(d2, c.t_cd))) return;
         if (s.type[j] == T_FLUID && s.id[j] >= idi) return;
         if (out) out[m] = CollPair{k, j, idi, s.id[j], dsqrt(d2)};
         m++;
@@ -417,10 +417,10 @@ __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
             for (int q = 0; q < ns; q++) {
                 const int j = nb.slot[(size_t)q * np + k];
                 const double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
-                if (!(d2 < c.t_max)) continue;
+                if (!lt_cut(d2, c.t_max)) continue;
                 const double dist = dsqrt(d2);
                 const double w = weight(dist, c.re_p);
-                if (dist < c.re_p) nd = dadd(nd, w);  // src/mps.cpp:573-583
+                if (lt_cut(dist, c.re_p)) nd = dadd(nd, w);  // src/mps.cpp:573-583
                 const size_t e = (size_t)m * np + k;
                 nb.slot[e] = j;
                 nb.dist[e] = dist;
@@ -432,10 +432,10 @@ __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
             for_each_candidate<PLANAR>(c, cs, skey[k], [&](int j) {
                 if (j == k) return;
                 const double d2 = dist2<PLANAR>(s, k, j, xi, yi, zi);
-                if (!(d2 < c.t_max)) return;
+                if (!lt_cut(d2, c.t_max)) return;
                 const double dist = dsqrt(d2);
                 const double w = weight(dist, c.re_p);
-                if (dist < c.re_p) nd = dadd(nd, w);
+                if (lt_cut(dist, c.re_p)) nd = dadd(nd, w);
                 if (m < c.K) {
                     const size_t e = (size_t)m * np + k;
                     nb.slot[e] = j;
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(kThreads) k_bc_source(Consts c, StateBuf s, Nb
         double ns = 0.0;
         for (int q = 0; q < m; q++) {
             double dist = nb.dist[(size_t)q * np + k];
-            if (dist < c.re_s) ns = dadd(ns, weight(dist, c.re_s));
+            if (lt_cut(dist, c.re_s)) ns = dadd(ns, weight(dist, c.re_s));
         }
         bc = ns < c.beta_n0s ? BC_SURFACE : BC_INNER;
     }
@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(kThreads) k_source_ho(Consts c, StateBuf s, Nb
         int j = nb.slot[(size_t)q * np + k];
         if (s.bc[j] == BC_IGNORED) continue;
         double dist = nb.dist[(size_t)q * np + k];
-        if (!(dist < c.re_p)) continue;
+        if (!lt_cut(dist, c.re_p)) continue;
         double rx = dsub(s.x[j], xi), ry = dsub(s.y[j], yi);
         double ux = dsub(s.vx[j], ui), uy = dsub(s.vy[j], vi);
         double dot = dadd(dmul(rx, ux), dmul(ry, uy));
@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(kThreads) k_assemble(Consts c, StateBuf s, NbL
                 int8_t bj = s.bc[j];
                 if (bj == BC_IGNORED) continue;
                 double dist = nb.dist[(size_t)q * np + k];
-                if (!(dist < c.re_p)) continue;
+                if (!lt_cut(dist, c.re_p)) continue;
                 double a = ddiv(dmul(c.mat_c, nb.wp[(size_t)q * np + k]), c.rho);
                 diag = dadd(diag, a);
                 if (bj == BC_INNER) {
@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(kThreads) k_cc_link(Consts c, StateBuf s, NbLi
     int links = 0;
     for (int q = 0; q < m && links < kCcLinks; q++) {
         const size_t o = (size_t)q * np + k;
-        if (nb.dist[o] < c.re_p) {
+        if (lt_cut(nb.dist[o], c.re_p)) {
             uf_union(par, k, nb.slot[o], ds);
             links++;
         }
@@ -659,7 +659,7 @@ __global__ void __launch_bounds__(kThreads) k_cc_hook(Consts c, StateBuf s, NbLi
     const int np = nb.n_pad, m = nb.cnt[k];
     for (int q = 0; q < m; q++) {
         const size_t o = (size_t)q * np + k;
-        if (nb.dist[o] < c.re_p) uf_union(par, k, nb.slot[o], ds);
+        if (lt_cut(nb.dist[o], c.re_p)) uf_union(par, k, nb.slot[o], ds);
     }
 }
 
@@ -704,7 +704,7 @@ __global__ void __launch_bounds__(kThreads) k_min_pressure(Consts c, StateBuf s,
     for (int q = 0; q < m; q++) {
         int j = nb.slot[(size_t)q * np + k];
         if (s.type[j] == T_DUMMY) continue;
-        if (nb.dist[(size_t)q * np + k] < c.re_p) {
+        if (lt_cut(nb.dist[(size_t)q * np + k], c.re_p)) {
             double pj = s.p[j];
             if (mn > pj) mn = pj;
         }
@@ -727,7 +727,7 @@ __global__ void __launch_bounds__(kThreads) k_gradient(Consts c, StateBuf s, NbL
             int j = nb.slot[(size_t)q * np + k];
             if (s.type[j] == T_DUMMY) continue;
             double dist = nb.dist[(size_t)q * np + k];
-            if (!(dist < c.re_p)) continue;
+            if (!lt_cut(dist, c.re_p)) continue;
             double dp = dsub(s.p[j], pmin);
             double w = nb.wp[(size_t)q * np + k];
             double d2 = dmul(dist, dist);
@@ -746,14 +746,14 @@ __global__ void __launch_bounds__(kThreads) k_gradient(Consts c, StateBuf s, NbL
             int j = nb.slot[(size_t)q * np + k];
             if (s.type[j] == T_DUMMY) continue;
             double dist = nb.dist[(size_t)q * np + k];
-            if (!(dist < c.re_p)) continue;
-            float fd = (float)dist;
-            float coef = (float)(s.p[j] - pmin) * (c.fre_p / fd - 1.f) / (fd * fd);
-            gx = fmaf((float)(s.x[j] - xi), coef, gx);
-            gy = fmaf((float)(s.y[j] - yi), coef, gy);
-            if (!PLANAR) gz = fmaf((float)(s.z[j] - zi), coef, gz);
+            if (!lt_cut(dist, c.re_p)) continue;
+            float fd = f32(dist);
+            float coef = f32(s.p[j] - pmin) * (c.fre_p / fd - 1.f) / (fd * fd);
+            gx = fmaf(f32(s.x[j] - xi), coef, gx);
+            gy = fmaf(f32(s.y[j] - yi), coef, gy);
+            if (!PLANAR) gz = fmaf(f32(s.z[j] - zi), coef, gz);
         }
-        const float sc = -c.fgrad_scale / (float)c.rho;
+        const float sc = -c.fgrad_scale / f32(c.rho);
         ax[k] = (double)(gx * sc);
         ay[k] = (double)(gy * sc);
         if (!PLANAR) az[k] = (double)(gz * sc);

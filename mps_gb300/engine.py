@@ -241,12 +241,12 @@ def selftest_exact64(n: int, seed: int = 1):
     """mps_selftest_exact64: the integer-pipe FP64 square root and division
     against the GPU's FP64 instructions on n seeded cases of each.  Returns
     (return code, dict with sqrt_mismatches, div_mismatches, sqrt_fast,
-    div_fast, first_bad)."""
+    div_fast, first_bad, other_mismatches)."""
     L = load()
-    res = (C.c_uint64 * 7)()
+    res = (C.c_uint64 * 8)()
     rc = L.mps_selftest_exact64(int(n), int(seed), res)
     return rc, {"sqrt_mismatches": res[0], "div_mismatches": res[1], "sqrt_fast": res[2],
-                "div_fast": res[3], "first_bad": (res[4], res[5], res[6])}
+                "div_fast": res[3], "first_bad": (res[4], res[5], res[6]), "other_mismatches": res[7]}
 
 
 def make_params(p: dict) -> MpsParams:

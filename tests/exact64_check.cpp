@@ -124,12 +124,56 @@ int check_refusals() {
     return 0;
 }
 
+int check_small_ops(long n) {
+    for (long i = 0; i < n; i++) {
+        // q - 1 for q in [1, 2^53), every binade
+        const double q = from_parts(rand_mant(), 1023 + (int)(rng() % 53));
+        double got;
+        if (!mpsg::x64::sub_one(q, got) || !same(got, q - 1.0)) {
+            std::printf("sub_one mismatch: %a\n", q);
+            return 1;
+        }
+        // FP32 rounding of doubles around and inside the FP32 range
+        double x = from_parts(rand_mant(), 880 + (int)(rng() % 290));
+        if (rng() & 1) x = -x;
+        float f;
+        if (mpsg::x64::to_f32(x, f)) {
+            if (mpsg::x64::u_of(f) != mpsg::x64::u_of((float)x)) {
+                std::printf("to_f32 mismatch: %a\n", x);
+                return 1;
+            }
+        } else if (std::fabs(x) >= 0x1p-126 && std::isfinite((float)x)) {
+            std::printf("to_f32 refused %a\n", x);
+            return 1;
+        }
+        // the ordering shortcut on non-negative values
+        const double v = from_parts(rand_mant(), 1000 + (int)(rng() % 40));
+        const double cut = from_parts(rand_mant(), 1000 + (int)(rng() % 40));
+        if (mpsg::x64::lt_cut(v, cut) != (v < cut) || mpsg::x64::lt_cut(cut, cut)) {
+            std::printf("lt_cut mismatch: %a %a\n", v, cut);
+            return 1;
+        }
+    }
+    double out;
+    float fo;
+    if (mpsg::x64::sub_one(0.5, out) || mpsg::x64::sub_one(0x1p53, out) || mpsg::x64::sub_one(INFINITY, out) ||
+        !mpsg::x64::sub_one(1.0, out) || out != 0.0 || std::signbit(out) ||
+        !mpsg::x64::to_f32(-0.0, fo) || !std::signbit(fo) || mpsg::x64::to_f32(1e-300, fo) ||
+        mpsg::x64::to_f32(NAN, fo) || !mpsg::x64::lt_cut(0.0, 1.0) || mpsg::x64::lt_cut(NAN, 1.0) ||
+        mpsg::x64::lt_cut(INFINITY, 1.0)) {
+        std::printf("small ops: special case wrong\n");
+        return 1;
+    }
+    std::printf("%ld subtractions of one, FP32 roundings and comparisons bit-identical\n", n);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
     const long n = argc > 1 ? std::atol(argv[1]) : 1000000;
     rng.seed(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 1);
-    if (check_refusals()) return 1;
+    if (check_refusals() || check_small_ops(n)) return 1;
     for (mode = 0; mode < 4; mode++) {
         if (check_sqrt(n) || check_div(n)) return 1;
         std::printf("mode %d: %ld square roots and %ld quotients bit-identical\n", mode, n, n);

@@ -24,7 +24,7 @@ def test_exact64_host_against_ieee(tmp_path):
                     os.path.join(HERE, "exact64_check.cpp")], check=True)
     out = subprocess.run([exe, "400000", "20261204"], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
-    assert out.stdout.count("bit-identical") == 4, out.stdout
+    assert out.stdout.count("bit-identical") == 5, out.stdout
 
 
 @pytest.mark.gpu
@@ -34,6 +34,7 @@ def test_exact64_device_against_fp64_instructions():
     rc, r = engine.selftest_exact64(n, seed=7)
     assert rc == 0
     assert r["sqrt_mismatches"] == 0 and r["div_mismatches"] == 0, r
+    assert r["other_mismatches"] == 0, r
     # nearly every generated case is inside the integer path
     assert r["sqrt_fast"] == n
     assert r["div_fast"] > 0.9 * n
