@@ -1264,6 +1264,26 @@ __global__ void __launch_bounds__(kMixedBlock, 1)
 //
 // Rows: 32-row slices dealt to blocks 1..G-1 (block 0 runs the small levels).
 constexpr int kCycleThreads = 512;
+// a chunk's first rows kept in shared memory for its level-1 sums, and the
+// chunks per warp whose row ranges are kept there for the whole solve
+constexpr int kChunkRows = 64;
+constexpr int kChunkCache = 8;
+
+// Rows of vector-update chunk c: from its first cell start to the first cell
+// start of the next slice that has one (or n); empty if slice c has none.
+__device__ __forceinline__ int2 chunk_rows(const int32_t* chunk, int c, int nsl, int n) {
+    const int s0 = __ldcg(chunk + c);
+    if (s0 < 0) return make_int2(0, 0);
+    int e0 = n;
+    for (int c2 = c + 1; c2 < nsl; c2++) {
+        const int t = __ldcg(chunk + c2);
+        if (t >= 0) {
+            e0 = t;
+            break;
+        }
+    }
+    return make_int2(s0, e0);
+}
 
 template <int BS, int NV>
 __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree& mf, const Mg& mg,
@@ -1298,6 +1318,8 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
     const size_t np = (size_t)mg.n_pad;
     const int NY = mg.lev[1].ny, n1 = mg.lev[1].nx * NY;
     __shared__ int s_cycle_ok;
+    __shared__ float s_chunk_r[kW][kChunkRows];
+    __shared__ int s_chunk_k[kW][kChunkRows];
     // the e/t role swaps of the grid-wide levels (lev_view): the cycle group
     // makes them, the other warps follow with the same mask after each cycle
     uint32_t swp = 0;
@@ -1306,12 +1328,31 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
     double acc[1] = {0.0}, tot[1];
     for (int sl = gwarp; sl < nsl; sl += nwarps) {
         int i = sl * 32 + lane;
+        // the vector update's chunks and the level-1 cell starts (fixed for the solve)
+        bool st = false;
+        float siv = 0.f;
+        if (i < n) {
+            const int key = __ldg(mf.skey + i);
+            st = i == 0 || key != __ldg(mf.skey + i - 1);
+            if (st && key < n1) siv = fmaxf(__ldg(mg.lev[1].invd + key), 0.f);
+            mg.start_iv[i] = siv;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, st);
+        if (lane == 0) mg.chunk[sl] = bal ? sl * 32 + __ffs(bal) - 1 : -1;
         if (i >= n) continue;
         kv.x[i] = 0.0;
         double bb = A.src[i];
         acc[0] = fma(bb, bb, acc[0]);
     }
     if (!reduce_sync<1, BS>(gb, acc, tot, ds)) return;
+    // this warp's chunks of the vector update: rows [x, y) (the first kChunkCache)
+    __shared__ int2 s_chunk[kW][kChunkCache];
+    if (has_rows)
+        for (int q = lane; q < kChunkCache; q += 32) {
+            const int c = rb + RB * (warp + q * kW);
+            s_chunk[warp][q] = c < nsl ? chunk_rows(mg.chunk, c, nsl, n) : make_int2(0, 0);
+        }
+    __syncwarp();
     const double rhs2 = tot[0];
     const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
     int64_t inner_total = 0;
@@ -1346,10 +1387,14 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
         int64_t k = 0;
         for (;;) {
             // ---- level 1 of the cycle: every warp sums r over the cells with
-            // unknowns (before the split, while nothing else streams), into
-            // the cycle group's level-1 arrays
-            mg_level1_plain(mg, mf, kv.r32, ((warp * G + b) << 5) + lane, gsz, level1_presmooth(mg, swp));
-            if (!grid_sync(gb, ds)) return;
+            // unknowns into the cycle group's level-1 arrays.  Only the first
+            // iteration of a refinement: afterwards the vector update (below)
+            // writes them for the next iteration
+            if (k == 0) {
+                mg_level1_plain(mg, mf, kv.r32, ((warp * G + b) << 5) + lane, gsz,
+                                level1_presmooth(mg, swp));
+                if (!grid_sync(gb, ds)) return;
+            }
             // ---- split: the cycle's cell levels on r, the operator on y
             if (warp < kVW) {
                 const int gcell = ((warp * G + b) << 5) + lane;
@@ -1435,40 +1480,89 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
                 alpha = gamma / den;
             }
             gamma_old = gamma;
-            // ---- p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; y = D^-1 r
-            // (this block's rows: u and w are its own; four rows in flight)
-            for (int q = warp; has_rows; q += 4 * kW) {
-                if (rb + RB * q >= nsl) break;
-                int ii[4];
+            // ---- p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; y = D^-1 r,
+            // fused with level 1 of the next cycle: each chunk (the rows from the
+            // first cell start of a slice to that of the next slice with one) holds
+            // whole level-1 cells, so its warp also sums each of them over its new
+            // residuals in slot order and writes the level's residual and
+            // pre-smoothing (the same values as the separate level-1 pass)
+            {
+                float* __restrict__ r1 = mg.lev[1].r;
+                float* __restrict__ e1n = level1_presmooth(mg, swp);
+                float* s_r = s_chunk_r[warp];
+                int* s_k = s_chunk_k[warp];
+                for (int q = 0; has_rows; q++) {
+                    const int c = rb + RB * (warp + q * kW);
+                    if (c >= nsl) break;
+                    const int2 cr = q < kChunkCache ? s_chunk[warp][q] : chunk_rows(mg.chunk, c, nsl, n);
+                    if (cr.y <= cr.x) continue;
+                    for (int base = cr.x; base < cr.y; base += 64) {
+                        float u[2], p[2], sv[2], w[2], x[2], r[2], id[2], siv[2];
+                        int key[2];
 #pragma unroll
-                for (int h = 0; h < 4; h++) {
-                    const int sl = rb + RB * (q + h * kW);
-                    ii[h] = sl < nsl ? sl * 32 + lane : n;
-                }
-                float u[4], p[4], sv[4], w[4], x[4], r[4], id[4];
+                        for (int h = 0; h < 2; h++) {
+                            const int i = min(base + 32 * h + lane, cr.y - 1);
+                            u[h] = __ldcg(kv.u32 + i);
+                            p[h] = kv.p32[i];
+                            sv[h] = kv.s32[i];
+                            w[h] = __ldcg(kv.w32 + i);
+                            x[h] = kv.x32[i];
+                            r[h] = __ldcg(kv.r32 + i);
+                            id[h] = kv.inv_diag32[i];
+                            key[h] = __ldg(mf.skey + i);
+                            siv[h] = __ldg(mg.start_iv + i);
+                        }
 #pragma unroll
-                for (int h = 0; h < 4; h++) {
-                    const int i = min(ii[h], n - 1);
-                    u[h] = __ldcg(kv.u32 + i);
-                    p[h] = kv.p32[i];
-                    sv[h] = kv.s32[i];
-                    w[h] = __ldcg(kv.w32 + i);
-                    x[h] = kv.x32[i];
-                    r[h] = __ldcg(kv.r32 + i);
-                    id[h] = kv.inv_diag32[i];
-                }
-#pragma unroll
-                for (int h = 0; h < 4; h++) {
-                    const int i = ii[h];
-                    if (i >= n) break;
-                    const float pn = fmaf(beta, p[h], u[h]);
-                    const float sn = fmaf(beta, sv[h], w[h]);
-                    kv.p32[i] = pn;
-                    kv.s32[i] = sn;
-                    kv.x32[i] = fmaf(alpha, pn, x[h]);
-                    const float rn = fmaf(-alpha, sn, r[h]);
-                    kv.r32[i] = rn;
-                    y[i] = id[h] * rn;
+                        for (int h = 0; h < 2; h++) {
+                            const int i = base + 32 * h + lane;
+                            if (i < cr.y) {
+                                const float pn = fmaf(beta, p[h], u[h]);
+                                const float sn = fmaf(beta, sv[h], w[h]);
+                                kv.p32[i] = pn;
+                                kv.s32[i] = sn;
+                                kv.x32[i] = fmaf(alpha, pn, x[h]);
+                                const float rn = fmaf(-alpha, sn, r[h]);
+                                kv.r32[i] = rn;
+                                y[i] = id[h] * rn;
+                                const int o = i - cr.x;
+                                if (o < kChunkRows) {
+                                    s_r[o] = rn;
+                                    s_k[o] = siv[h] > 0.f ? key[h] : -1 - key[h];
+                                }
+                            }
+                        }
+                    }
+                    __syncwarp();
+                    // the chunk's cells: the lane holding a cell's first slot sums it
+                    const int len = cr.y - cr.x;
+                    for (int o = lane; o < len; o += 32) {
+                        int kk;
+                        if (o < kChunkRows) {
+                            kk = s_k[o];
+                            if (kk < 0) continue;  // not the first slot of a cell with unknowns
+                        } else {
+                            if (!(__ldg(mg.start_iv + cr.x + o) > 0.f)) continue;
+                            kk = __ldg(mf.skey + cr.x + o);
+                        }
+                        float acc = 0.f;
+                        for (int j = o; j < len; j++) {
+                            int kj;
+                            float rj;
+                            if (j < kChunkRows) {
+                                kj = s_k[j];
+                                kj = kj < 0 ? -1 - kj : kj;
+                                rj = s_r[j];
+                            } else {
+                                kj = __ldg(mf.skey + cr.x + j);
+                                rj = __ldcg(kv.r32 + cr.x + j);
+                            }
+                            if (kj != kk) break;
+                            acc += rj;
+                        }
+                        r1[kk] = acc;
+                        e1n[kk] = mg.omega * __ldg(mg.start_iv + cr.x + o) * acc;
+                    }
+                    __syncwarp();
                 }
             }
             k++;
