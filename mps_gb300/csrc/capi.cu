@@ -672,7 +672,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         if (e->alloc(&g.e0, np) || e->alloc(&g.res0, np) ||
             e->alloc(&g.dense, (size_t)kMgMaxCoarsest * kMgMaxCoarsest) || e->alloc(&g.rowcell, 9 * np) ||
             e->alloc(&g.nact, kMgMaxLevels) || e->alloc(&g.act1_rng, (size_t)c.numX * c.numY) ||
-            e->alloc(&g.chunk, np / 32 + 2) || e->alloc(&g.start_iv, np))
+            e->alloc(&g.cell_end, np))
             return bail(fail(MPS_ERR_CUDA, "cudaMalloc multigrid"));
         g.n_pad = (int32_t)np;
     }

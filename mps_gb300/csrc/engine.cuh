@@ -260,12 +260,10 @@ struct Mg {
     int32_t n_pad;
     int32_t* nact;  // per level: the length of lev[l].act (device, written by the setup)
     int2* act1_rng; // per entry of lev[1].act: the cell's first slot and slot count
-    // the overlapped solve's vector-update chunks: chunk[c] = the first level-1
-    // cell start in 32-slot slice c, -1 if the slice holds none (n_pad/32 + 2)
-    int32_t* chunk;
-    // per slot: 1/diagonal of its level-1 cell if the slot is that cell's first
-    // and the cell holds an unknown, else 0 (n_pad)
-    float* start_iv;
+    // per slot, for the overlapped solve's fused level-1 sums: if the slot is
+    // the last of a level-1 cell with unknowns, (cell | min(slots, 255) << 24,
+    // bits of the cell's 1/diagonal), else (-1, 0) (n_pad)
+    int2* cell_end;
 };
 
 // --------------------------------------------------------------- solver.cu

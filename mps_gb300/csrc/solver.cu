@@ -1264,25 +1264,22 @@ __global__ void __launch_bounds__(kMixedBlock, 1)
 //
 // Rows: 32-row slices dealt to blocks 1..G-1 (block 0 runs the small levels).
 constexpr int kCycleThreads = 512;
-// a chunk's first rows kept in shared memory for its level-1 sums, and the
-// chunks per warp whose row ranges are kept there for the whole solve
-constexpr int kChunkRows = 64;
-constexpr int kChunkCache = 8;
+// The vector update of the overlapped solve gives each warp one contiguous
+// range of rows that starts and ends at level-1 cell boundaries, walked in
+// 64-row batches whose new residuals stay in a 128-row shared ring for the
+// cells' sums.
+constexpr int kRing = 128;
 
-// Rows of vector-update chunk c: from its first cell start to the first cell
-// start of the next slice that has one (or n); empty if slice c has none.
-__device__ __forceinline__ int2 chunk_rows(const int32_t* chunk, int c, int nsl, int n) {
-    const int s0 = __ldcg(chunk + c);
-    if (s0 < 0) return make_int2(0, 0);
-    int e0 = n;
-    for (int c2 = c + 1; c2 < nsl; c2++) {
-        const int t = __ldcg(chunk + c2);
-        if (t >= 0) {
-            e0 = t;
-            break;
-        }
+// The first slot at or after p that starts a level-1 cell (or n).
+__device__ __forceinline__ int cell_start_at_or_after(const int32_t* __restrict__ skey, int p, int n) {
+    const int lane = threadIdx.x & 31;
+    for (; p < n; p += 32) {
+        const int i = p + lane;
+        const bool st = i < n && (i == 0 || __ldg(skey + i) != __ldg(skey + i - 1));
+        const unsigned bal = __ballot_sync(0xffffffffu, st);
+        if (bal) return p + __ffs(bal) - 1;
     }
-    return make_int2(s0, e0);
+    return n;
 }
 
 template <int BS, int NV>
@@ -1317,9 +1314,10 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
     float* __restrict__ z = mg.res0;  // A y
     const size_t np = (size_t)mg.n_pad;
     const int NY = mg.lev[1].ny, n1 = mg.lev[1].nx * NY;
+    // level 1's sums fused into the vector update (cell indices fit 24 bits)
+    const bool fuse1 = n1 < (1 << 24);
     __shared__ int s_cycle_ok;
-    __shared__ float s_chunk_r[kW][kChunkRows];
-    __shared__ int s_chunk_k[kW][kChunkRows];
+    __shared__ float s_ring[kW][kRing];
     // the e/t role swaps of the grid-wide levels (lev_view): the cycle group
     // makes them, the other warps follow with the same mask after each cycle
     uint32_t swp = 0;
@@ -1328,31 +1326,31 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
     double acc[1] = {0.0}, tot[1];
     for (int sl = gwarp; sl < nsl; sl += nwarps) {
         int i = sl * 32 + lane;
-        // the vector update's chunks and the level-1 cell starts (fixed for the solve)
-        bool st = false;
-        float siv = 0.f;
-        if (i < n) {
-            const int key = __ldg(mf.skey + i);
-            st = i == 0 || key != __ldg(mf.skey + i - 1);
-            if (st && key < n1) siv = fmaxf(__ldg(mg.lev[1].invd + key), 0.f);
-            mg.start_iv[i] = siv;
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, st);
-        if (lane == 0) mg.chunk[sl] = bal ? sl * 32 + __ffs(bal) - 1 : -1;
         if (i >= n) continue;
+        // the last slots of the level-1 cells with unknowns (fixed for the solve)
+        if (fuse1) {
+            const int key = __ldg(mf.skey + i);
+            int2 ce = make_int2(-1, 0);
+            if (key < n1 && (i == n - 1 || key != __ldg(mf.skey + i + 1))) {
+                const float iv = __ldg(mg.lev[1].invd + key);
+                const int len = i + 1 - __ldg(mf.cs + key);
+                if (iv > 0.f) ce = make_int2(key | (min(len, 255) << 24), __float_as_int(iv));
+            }
+            mg.cell_end[i] = ce;
+        }
         kv.x[i] = 0.0;
         double bb = A.src[i];
         acc[0] = fma(bb, bb, acc[0]);
     }
     if (!reduce_sync<1, BS>(gb, acc, tot, ds)) return;
-    // this warp's chunks of the vector update: rows [x, y) (the first kChunkCache)
-    __shared__ int2 s_chunk[kW][kChunkCache];
-    if (has_rows)
-        for (int q = lane; q < kChunkCache; q += 32) {
-            const int c = rb + RB * (warp + q * kW);
-            s_chunk[warp][q] = c < nsl ? chunk_rows(mg.chunk, c, nsl, n) : make_int2(0, 0);
-        }
-    __syncwarp();
+    // this warp's rows of the vector update: [rlo, rhi), from the first cell
+    // start at or after an even split point to the next warp's
+    int rlo = 0, rhi = 0;
+    if (has_rows) {
+        const int nw = RB * kW, wi = rb * kW + warp;
+        rlo = wi == 0 ? 0 : cell_start_at_or_after(mf.skey, (int)((int64_t)n * wi / nw), n);
+        rhi = wi + 1 == nw ? n : cell_start_at_or_after(mf.skey, (int)((int64_t)n * (wi + 1) / nw), n);
+    }
     const double rhs2 = tot[0];
     const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
     int64_t inner_total = 0;
@@ -1390,7 +1388,7 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
             // unknowns into the cycle group's level-1 arrays.  Only the first
             // iteration of a refinement: afterwards the vector update (below)
             // writes them for the next iteration
-            if (k == 0) {
+            if (k == 0 || !fuse1) {
                 mg_level1_plain(mg, mf, kv.r32, ((warp * G + b) << 5) + lane, gsz,
                                 level1_presmooth(mg, swp));
                 if (!grid_sync(gb, ds)) return;
@@ -1481,86 +1479,61 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
             }
             gamma_old = gamma;
             // ---- p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; y = D^-1 r,
-            // fused with level 1 of the next cycle: each chunk (the rows from the
-            // first cell start of a slice to that of the next slice with one) holds
-            // whole level-1 cells, so its warp also sums each of them over its new
-            // residuals in slot order and writes the level's residual and
-            // pre-smoothing (the same values as the separate level-1 pass)
+            // fused with level 1 of the next cycle: this warp's rows hold whole
+            // level-1 cells, so the lane holding a cell's last slot sums the
+            // cell's new residuals in slot order and writes the level's residual
+            // and pre-smoothing (the same values as the separate level-1 pass)
             {
                 float* __restrict__ r1 = mg.lev[1].r;
                 float* __restrict__ e1n = level1_presmooth(mg, swp);
-                float* s_r = s_chunk_r[warp];
-                int* s_k = s_chunk_k[warp];
-                for (int q = 0; has_rows; q++) {
-                    const int c = rb + RB * (warp + q * kW);
-                    if (c >= nsl) break;
-                    const int2 cr = q < kChunkCache ? s_chunk[warp][q] : chunk_rows(mg.chunk, c, nsl, n);
-                    if (cr.y <= cr.x) continue;
-                    for (int base = cr.x; base < cr.y; base += 64) {
-                        float u[2], p[2], sv[2], w[2], x[2], r[2], id[2], siv[2];
-                        int key[2];
+                float* ring = s_ring[warp];
+                for (int base = rlo; base < rhi; base += 64) {
+                    float u[2], p[2], sv[2], w[2], x[2], r[2], id[2];
+                    int2 ce[2];
 #pragma unroll
-                        for (int h = 0; h < 2; h++) {
-                            const int i = min(base + 32 * h + lane, cr.y - 1);
-                            u[h] = __ldcg(kv.u32 + i);
-                            p[h] = kv.p32[i];
-                            sv[h] = kv.s32[i];
-                            w[h] = __ldcg(kv.w32 + i);
-                            x[h] = kv.x32[i];
-                            r[h] = __ldcg(kv.r32 + i);
-                            id[h] = kv.inv_diag32[i];
-                            key[h] = __ldg(mf.skey + i);
-                            siv[h] = __ldg(mg.start_iv + i);
-                        }
+                    for (int h = 0; h < 2; h++) {
+                        const int i = min(base + 32 * h + lane, rhi - 1);
+                        u[h] = __ldcg(kv.u32 + i);
+                        p[h] = kv.p32[i];
+                        sv[h] = kv.s32[i];
+                        w[h] = __ldcg(kv.w32 + i);
+                        x[h] = kv.x32[i];
+                        r[h] = __ldcg(kv.r32 + i);
+                        id[h] = kv.inv_diag32[i];
+                        ce[h] = fuse1 ? __ldg(mg.cell_end + i) : make_int2(-1, 0);
+                    }
 #pragma unroll
-                        for (int h = 0; h < 2; h++) {
-                            const int i = base + 32 * h + lane;
-                            if (i < cr.y) {
-                                const float pn = fmaf(beta, p[h], u[h]);
-                                const float sn = fmaf(beta, sv[h], w[h]);
-                                kv.p32[i] = pn;
-                                kv.s32[i] = sn;
-                                kv.x32[i] = fmaf(alpha, pn, x[h]);
-                                const float rn = fmaf(-alpha, sn, r[h]);
-                                kv.r32[i] = rn;
-                                y[i] = id[h] * rn;
-                                const int o = i - cr.x;
-                                if (o < kChunkRows) {
-                                    s_r[o] = rn;
-                                    s_k[o] = siv[h] > 0.f ? key[h] : -1 - key[h];
-                                }
-                            }
+                    for (int h = 0; h < 2; h++) {
+                        const int i = base + 32 * h + lane;
+                        if (i < rhi) {
+                            const float pn = fmaf(beta, p[h], u[h]);
+                            const float sn = fmaf(beta, sv[h], w[h]);
+                            kv.p32[i] = pn;
+                            kv.s32[i] = sn;
+                            kv.x32[i] = fmaf(alpha, pn, x[h]);
+                            const float rn = fmaf(-alpha, sn, r[h]);
+                            kv.r32[i] = rn;
+                            y[i] = id[h] * rn;
+                            ring[(i - rlo) & (kRing - 1)] = rn;
                         }
                     }
                     __syncwarp();
-                    // the chunk's cells: the lane holding a cell's first slot sums it
-                    const int len = cr.y - cr.x;
-                    for (int o = lane; o < len; o += 32) {
-                        int kk;
-                        if (o < kChunkRows) {
-                            kk = s_k[o];
-                            if (kk < 0) continue;  // not the first slot of a cell with unknowns
-                        } else {
-                            if (!(__ldg(mg.start_iv + cr.x + o) > 0.f)) continue;
-                            kk = __ldg(mf.skey + cr.x + o);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int i = base + 32 * h + lane;
+                        if (i < rhi && ce[h].x >= 0) {
+                            const int key = ce[h].x & 0xFFFFFF;
+                            int len = (int)((unsigned)ce[h].x >> 24);
+                            if (len == 255) len = i + 1 - __ldg(mf.cs + key);
+                            const int j0 = i + 1 - len;
+                            float acc = 0.f;
+                            // the ring holds this batch and the previous one
+                            const int keep = max(base - 64, rlo);
+                            for (int j = j0; j <= i; j++)
+                                acc += j >= keep ? ring[(j - rlo) & (kRing - 1)] : __ldcg(kv.r32 + j);
+                            r1[key] = acc;
+                            e1n[key] = mg.omega * __int_as_float(ce[h].y) * acc;
                         }
-                        float acc = 0.f;
-                        for (int j = o; j < len; j++) {
-                            int kj;
-                            float rj;
-                            if (j < kChunkRows) {
-                                kj = s_k[j];
-                                kj = kj < 0 ? -1 - kj : kj;
-                                rj = s_r[j];
-                            } else {
-                                kj = __ldg(mf.skey + cr.x + j);
-                                rj = __ldcg(kv.r32 + cr.x + j);
-                            }
-                            if (kj != kk) break;
-                            acc += rj;
-                        }
-                        r1[kk] = acc;
-                        e1n[kk] = mg.omega * __ldg(mg.start_iv + cr.x + o) * acc;
                     }
                     __syncwarp();
                 }
