@@ -518,19 +518,24 @@ def run_accuracy_trajectory(prm, pos, vel, types, steps: int = 500, every: int =
 
 
 def run_precision_split(prm, state, steps: int = 4) -> dict:
-    """How much of the mixed/FP64 ratio is precision and how much is the
-    preconditioner: from one developed state, `steps` steps each of the FP64
-    solver (the reference's Jacobi CG), the mixed solver with the same Jacobi
-    preconditioner (multigrid mode 0), and the mixed solver with its default
-    multigrid; ms per solve and iterations of each."""
+    """How much of the mixed/FP64 ratio is precision, how much the
+    preconditioner and how much the initial guess: from one developed state,
+    `steps` steps each of the FP64 solver (the reference's Jacobi CG from
+    zero), the mixed solver with the same Jacobi preconditioner from zero
+    (multigrid mode 0), the mixed solver with its default multigrid from zero,
+    and the same from the previous step's solution (the default); ms per
+    solve and iterations of each."""
     from mps_gb300 import FP64, MIXED, Engine
 
     out = {}
-    for name, prec, mode in (("fp64_jacobi", FP64, None), ("mixed_jacobi", MIXED, 0),
-                             ("mixed_multigrid", MIXED, 1)):
+    for name, prec, mode, warm in (("fp64_jacobi", FP64, None, False), ("mixed_jacobi", MIXED, 0, False),
+                                   ("mixed_multigrid", MIXED, 1, False),
+                                   ("mixed_multigrid_previous_guess", MIXED, 1, True)):
         e = Engine(prm, state["pos"], state["vel"], state["type"], precision=prec)
         if mode is not None:
             e.set_multigrid(mode)
+        if prec == MIXED:
+            e.set_initial_guess(warm)
         e.step()
         st = [e.step() for _ in range(steps)]
         out[name] = {"ms_solve_mean": float(np.mean([x["ms_solve"] for x in st])),
@@ -538,9 +543,11 @@ def run_precision_split(prm, state, steps: int = 4) -> dict:
                      "refinements_mean": float(np.mean([x["refinements"] for x in st]))}
         e.close()
     f, j, g = out["fp64_jacobi"], out["mixed_jacobi"], out["mixed_multigrid"]
+    gw = out["mixed_multigrid_previous_guess"]
     out["solve_speedup_precision_only"] = f["ms_solve_mean"] / j["ms_solve_mean"]
     out["solve_speedup_preconditioner_on_top"] = j["ms_solve_mean"] / g["ms_solve_mean"]
-    out["solve_speedup_total"] = f["ms_solve_mean"] / g["ms_solve_mean"]
+    out["solve_speedup_initial_guess_on_top"] = g["ms_solve_mean"] / gw["ms_solve_mean"]
+    out["solve_speedup_total"] = f["ms_solve_mean"] / gw["ms_solve_mean"]
     out["steps"] = steps
     return out
 
@@ -672,6 +679,8 @@ def run_ours(args, rank: int, world: int, dist):
 
     # main: mixed precision, state resident in HBM
     eng = Engine(prm, pos, vel, types, precision=prec)
+    if prec == MIXED:
+        eng.set_initial_guess(args.initial_guess == "previous")
     for _ in range(args.warmup):
         eng.step()
     with ClockSampler(dev) as clk:
@@ -756,7 +765,8 @@ def run_ours(args, rank: int, world: int, dist):
                "h2d_bytes_per_step": int(hpos.nbytes + hvel.nbytes + htype.nbytes),
                "d2h_bytes_per_step": int(hpos.nbytes + hvel.nbytes + hp.nbytes + hndr.nbytes
                                          + htype.nbytes + hbc.nbytes),
-               "steps": args.e2e_steps}
+               "steps": args.e2e_steps,
+               "initial_guess": "zero (every step uploads its state; mps_upload restarts the guess)"}
     eng.close()
 
     others = {}
@@ -784,6 +794,8 @@ def run_ours(args, rank: int, world: int, dist):
         "data": "synthetic (seeded lattice dam break, the reference generator's layout)",
         "config": workload_config(args.workload, prm, nf, n),
         "solver": f"{args.precision} PPE solver", "parallelism": f"replicas x{world}",
+        "initial_guess": ("the previous step's solution" if args.initial_guess == "previous" else "zero")
+        if prec == MIXED else "zero",
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "cuda_graph_steps": int(sum(s["graph_replayed"] for s in stats)),
         "cg_iterations_mean": mean("cg_iterations"), "refinements_mean": mean("refinements"),
@@ -832,6 +844,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dambreak_1m")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--initial-guess", default="previous", choices=["previous", "zero"],
+                    help="the mixed solver's start: the previous step's solution, or zero as the reference's CG")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--trajectory-steps", type=int, default=500,

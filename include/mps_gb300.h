@@ -130,6 +130,15 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
  * CG is Jacobi-preconditioned). */
 int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale);
 
+/* Initial guess of the MIXED solver.  previous = 1 (default): each solve
+ * starts from the previous step's solution of the same particles (before
+ * the negative-pressure clamp; 0 for particles that had no unknown, and for
+ * the first step and the first after mps_upload); previous = 0: from zero,
+ * as the reference's CG (Eigen's solve(), src/mps.cpp:452-460).  Either way
+ * the solve stops at ||b - A x|| <= tol ||b||; only the iterations it takes
+ * change.  The FP64 solver always starts from zero. */
+int mps_set_initial_guess(mps_engine* e, int32_t previous);
+
 /* Self-test of the device-side wait limits (no counterpart in the
  * reference): runs the solver's grid barrier on 8 blocks in a group that
  * counts 9, so no block can pass; every block must give up with the timeout

@@ -181,8 +181,7 @@ int alloc_state(mps_engine* e, StateBuf& s) {
     CU(e->alloc(&s.x, n));
     CU(e->alloc(&s.y, n));
     CU(e->alloc(&s.z, n));
-    CU(e->alloc(&s.xf, n));
-    CU(e->alloc(&s.yf, n));
+    CU(e->alloc(&s.xyf, n));
     CU(e->alloc(&s.zf, n));
     CU(e->alloc(&s.vx, n));
     CU(e->alloc(&s.vy, n));
@@ -273,7 +272,7 @@ void enqueue_pre_solve(mps_engine* e) {
 // Mixed solver only: FP32 operator and multigrid hierarchy of this step.
 void enqueue_solver_setup(mps_engine* e) {
     if (e->precision != MPS_PRECISION_MIXED) return;
-    launch_mixed_setup(e->c, e->sc, e->A, e->mf, e->kv, e->st);
+    launch_mixed_setup(e->c, e->sc, e->A, e->mf, e->kv, e->S().id, e->warm_start != 0, e->st);
     launch_mg_setup(e->c, e->A, e->mf, active_mg(e), e->st);
 }
 
@@ -283,7 +282,8 @@ void enqueue_post_solve(mps_engine* e, bool do_export) {
     Consts& c = e->c;
     cudaStream_t st = e->st;
     const int mixed = e->precision == MPS_PRECISION_MIXED;
-    launch_pressure_post(c, e->S(), e->nb, e->kv.x, e->ax, e->ay, e->az, mixed, e->ds, st);
+    launch_pressure_post(c, e->S(), e->nb, e->kv.x, e->kv.x_prev, e->ax, e->ay, e->az, mixed, e->ds,
+                         st);
     if (do_export || c.ho_on) {
         launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
         e->swap();
@@ -306,7 +306,8 @@ void enqueue_step(mps_engine* e, bool do_export) {
     enqueue_solver_setup(e);
     const int64_t mi = e->max_iter > 0 ? e->max_iter : 2 * (int64_t)e->c.n;
     if (e->precision == MPS_PRECISION_MIXED)
-        launch_solve_mixed(e->c, e->A, e->mf, active_mg(e), e->kv, e->tol, mi, e->ds, st);
+        launch_solve_mixed(e->c, e->A, e->mf, active_mg(e), e->kv, e->tol, mi, e->warm_start != 0,
+                           e->ds, st);
     else
         launch_solve_fp64(e->c, e->A, e->kv, e->tol, mi, e->ds, st);
     cudaEventRecordWithFlags(e->ev[3], st, evflag);
@@ -624,6 +625,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         e->alloc(&e->A.offcnt, np) || e->alloc(&e->A.col, np * K) || e->alloc(&e->A.val, np * K) ||
         e->alloc(&e->A.slice_w, np / 32 + 1) || e->alloc(&e->A.val32, np * K) ||
         e->alloc(&e->A.diag32, np) || e->alloc(&e->kv.x, np) || e->alloc(&e->kv.r, np) ||
+        e->alloc(&e->kv.x_prev, np) ||
         e->alloc(&e->kv.p, np) || e->alloc(&e->kv.q, np) || e->alloc(&e->kv.z, np) ||
         e->alloc(&e->kv.inv_diag, np) || e->alloc(&e->kv.r32, np) || e->alloc(&e->kv.p32, np) ||
         e->alloc(&e->kv.s32, np) || e->alloc(&e->kv.w32, np) || e->alloc(&e->kv.x32, np) ||
@@ -698,6 +700,7 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         cudaMemsetAsync(t.vz, 0, np * 8, e->st);
     }
     cudaMemsetAsync(e->kv.x, 0, np * 8, e->st);
+    cudaMemsetAsync(e->kv.x_prev, 0, np * 8, e->st);
     cudaMemsetAsync(e->nb.cnt, 0, np * 4, e->st);
     k_iota<<<(n + 255) / 256, 256, 0, e->st>>>(n, s.id);
     // upload the initial condition (identity slot order, ids = indices)
@@ -750,6 +753,13 @@ int mps_set_solver(mps_engine* e, int32_t precision, double tol, int64_t max_ite
     e->tol = tol > 0 ? tol
                      : (precision == MPS_PRECISION_FP64 ? std::numeric_limits<double>::epsilon() : 1e-10);
     e->max_iter = max_iter > 0 ? max_iter : 0;
+    return MPS_OK;
+}
+
+int mps_set_initial_guess(mps_engine* e, int32_t previous) {
+    if (!e) return fail(MPS_ERR_ARG, "null engine");
+    drop_graphs(e);
+    e->warm_start = previous ? 1 : 0;
     return MPS_OK;
 }
 
@@ -911,6 +921,8 @@ int mps_upload(mps_engine* e, const double* pos, const double* vel, const int32_
     if (pos) k_vec3_from_host<<<G, T, 0, e->st>>>(n, s.id, ps, s.x, s.y, pl ? nullptr : s.z);
     if (vel) k_vec3_from_host<<<G, T, 0, e->st>>>(n, s.id, vs, s.vx, s.vy, pl ? nullptr : s.vz);
     if (type) k_type_from_host_order<<<G, T, 0, e->st>>>(n, s.id, ts, s.type);
+    // a new state: the next mixed solve starts from zero
+    CU(cudaMemsetAsync(e->kv.x_prev, 0, np * 8, e->st));
     CU(cudaStreamSynchronize(e->st));
     CU(cudaGetLastError());
     return MPS_OK;

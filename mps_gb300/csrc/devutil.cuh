@@ -150,7 +150,8 @@ __device__ __forceinline__ double dist2(const StateBuf& s, int i, int j, double 
 template <bool PLANAR>
 __device__ __forceinline__ bool far32(const StateBuf& s, int j, float fx, float fy, float fz,
                                       float bound) {
-    const float dx = s.xf[j] - fx, dy = s.yf[j] - fy;
+    const float2 q = s.xyf[j];
+    const float dx = q.x - fx, dy = q.y - fy;
     float r = dx * dx + dy * dy;
     if (!PLANAR) {
         const float dz = s.zf[j] - fz;

@@ -67,7 +67,10 @@ struct Consts {
 
 struct StateBuf {
     double *x, *y, *z, *vx, *vy, *vz;
-    float *xf, *yf, *zf;  // FP32 copies of the positions (written by the rebuild gather)
+    // FP32 copies of the positions, x and y interleaved (one 8-byte load per
+    // candidate in the neighbour sweeps' pre-filter), written by the rebuild gather
+    float2* xyf;
+    float* zf;
     double *p, *minp, *ndr, *nd_last;
     int32_t* id;
     int8_t *type, *bc, *dir;
@@ -196,9 +199,10 @@ void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, cons
 // when it is not zero; raises ST_ASYMMETRIC, which makes the solvers skip.
 void launch_symmetry_check(const Consts& c, const StateBuf& s, const Ppe& A, DevStats* ds,
                            cudaStream_t st);
+// x_prev (may be null) receives the solution by particle id.
 void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb,
-                          const double* x, double* ax, double* ay, double* az, int mixed,
-                          DevStats* ds, cudaStream_t st);
+                          const double* x, double* x_prev, double* ax, double* ay, double* az,
+                          int mixed, DevStats* ds, cudaStream_t st);
 void launch_number_density(const Consts& c, const StateBuf& s, const NbList& nb,
                            cudaStream_t st);
 
@@ -269,6 +273,9 @@ struct Mg {
 // --------------------------------------------------------------- solver.cu
 struct Krylov {
     double *x, *r, *p, *q, *z, *inv_diag;
+    // the last solve's solution (before the negative-pressure clamp) by
+    // particle id: the mixed solver's initial guess at the next step
+    double* x_prev;
     float *r32, *p32, *s32, *w32, *x32, *u32, *inv_diag32;
     double* partials;       // 2 x grid x 8 per-block partial sums
     unsigned int* barrier;  // monotonically increasing arrival counter
@@ -283,8 +290,10 @@ int selftest_wait_limit(int blocks, int* gave_up, int* status, float* ms);
 // Solves A x = b; returns through DevStats (iterations, residual, status).
 void launch_solve_fp64(const Consts& c, const Ppe& A, const Krylov& k, double tol,
                        int64_t max_iter, DevStats* ds, cudaStream_t st);
+// warm: x already holds the initial guess (launch_mixed_setup), else the
+// solve starts from zero.
 void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
-                        const Krylov& k, double tol, int64_t max_iter, DevStats* ds,
+                        const Krylov& k, double tol, int64_t max_iter, bool warm, DevStats* ds,
                         cudaStream_t st);
 // Batched mixed-precision solve: many scenes in one cooperative launch, the
 // blocks split into one group per scene (group sizes ~ rows^alpha), each
@@ -321,8 +330,10 @@ void launch_solve_mixed_batched(const BatchSolve& b, cudaStream_t st);
 // Per-solve multigrid setup (after launch_mixed_setup).
 void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
                      cudaStream_t st);
-// FP32 copy of the assembled matrix in the compact layout of MatFree.
+// FP32 copy of the assembled matrix in the compact layout of MatFree; with
+// warm set, also the solve's initial guess x (k.x_prev at the slots' ids on
+// rows with a diagonal, else 0).
 void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, MatFree& mf,
-                        const Krylov& k, cudaStream_t st);
+                        const Krylov& k, const int32_t* ids, bool warm, cudaStream_t st);
 
 }  // namespace mpsg

@@ -83,6 +83,8 @@ struct mps_engine {
     int precision = MPS_PRECISION_FP64;
     double tol = std::numeric_limits<double>::epsilon();
     int64_t max_iter = 0;
+    // the mixed solver starts from the last solve's solution (0: from zero)
+    int32_t warm_start = 1;
     int32_t debug_log_count = 0;
     int32_t step_launches = 0;
     // CUDA graphs of a non-export step, one per buffer parity at step start

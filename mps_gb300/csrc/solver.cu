@@ -53,6 +53,7 @@ struct SolveArgs {
     int64_t max_iter;
     double inner_tol;
     int32_t max_refine;
+    int32_t warm;       // x holds an initial guess (else the solve zeroes it)
 };
 
 // ---------------------------------------------------------------- barriers
@@ -1086,12 +1087,15 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, con
     for (int sl = gwarp; sl < a.nslices; sl += nwarps) {
         int i = sl * 32 + lane;
         if (i >= a.n) continue;
-        kv.x[i] = 0.0;
+        if (!a.warm) kv.x[i] = 0.0;
         double b = A.src[i];
         acc[0] = fma(b, b, acc[0]);
     }
     if (!reduce_sync<1, BS>(gb, acc, tot, ds)) return;
     const double rhs2 = tot[0];
+    // b = 0 has the solution 0 whatever the guess (the loop below does not run)
+    if (a.warm && !(rhs2 > 0.0))
+        for (int i = gtid; i < a.n; i += gsz) kv.x[i] = 0.0;
     const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
     int64_t inner_total = 0;
     int refine = 0;
@@ -1338,7 +1342,7 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
             }
             mg.cell_end[i] = ce;
         }
-        kv.x[i] = 0.0;
+        if (!a.warm) kv.x[i] = 0.0;
         double bb = A.src[i];
         acc[0] = fma(bb, bb, acc[0]);
     }
@@ -1352,6 +1356,9 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
         rhi = wi + 1 == nw ? n : cell_start_at_or_after(mf.skey, (int)((int64_t)n * (wi + 1) / nw), n);
     }
     const double rhs2 = tot[0];
+    // b = 0 has the solution 0 whatever the guess (the loop below does not run)
+    if (a.warm && !(rhs2 > 0.0))
+        for (int i = gtid; i < n; i += gsz) kv.x[i] = 0.0;
     const double thr = fmax(a.tol * a.tol * rhs2, DBL_MIN);
     int64_t inner_total = 0;
     int refine = 0;
@@ -1589,10 +1596,14 @@ __global__ void __launch_bounds__(BS, MINB) k_cg_mixed_batched(const SceneSolve*
 // index 0), the row's three range starts, FP32 diagonal and inverse
 // diagonal.  A row whose column lies 64 or more slots into its range keeps
 // the int32 columns (sell_row = 1).
-__global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv) {
+__global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv, const int32_t* __restrict__ ids,
+                              int warm) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.n) return;
     const double d = A.diag[k];
+    // initial guess: the particle's solution of the last solve (rows without
+    // an unknown stay 0, as the zero start leaves them)
+    if (warm) kv.x[k] = d > 0.0 ? kv.x_prev[ids[k]] : 0.0;
     A.diag32[k] = f32(d);
     kv.inv_diag32[k] = d != 0.0 ? f32(ddiv(1.0, d)) : 1.f;
     const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
@@ -1652,6 +1663,7 @@ SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
     a.max_iter = max_iter;
     a.inner_tol = 1e-6;  // FP32 floor of an inner solve's residual reduction
     a.max_refine = 40;
+    a.warm = 0;
     return a;
 }
 
@@ -1666,12 +1678,12 @@ void solver_setup(Krylov& k, int32_t /*n_pad*/, int device) {
 }
 
 void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, MatFree& mf,
-                        const Krylov& k, cudaStream_t st) {
+                        const Krylov& k, const int32_t* ids, bool warm, cudaStream_t st) {
     mf.skey = sc.skey;
     mf.cs = sc.cell_start;
     mf.numY = c.numY;
     mf.nkeys = c.nkeys;
-    k_mixed_setup<<<(c.n + 255) / 256, 256, 0, st>>>(c, A, mf, k);
+    k_mixed_setup<<<(c.n + 255) / 256, 256, 0, st>>>(c, A, mf, k, ids, warm ? 1 : 0);
     ++g_launches;
 }
 
@@ -1834,9 +1846,10 @@ void launch_solve_mixed_batched(const BatchSolve& b, cudaStream_t st) {
 }
 
 void launch_solve_mixed(const Consts& c, const Ppe& A, const MatFree& mf, const Mg& mg,
-                        const Krylov& k, double tol, int64_t max_iter, DevStats* ds,
+                        const Krylov& k, double tol, int64_t max_iter, bool warm, DevStats* ds,
                         cudaStream_t st) {
     SolveArgs a = make_args(c, tol, max_iter);
+    a.warm = warm ? 1 : 0;
     Ppe AA = A;
     MatFree mm = mf;
     Mg gg = mg;

@@ -95,8 +95,7 @@ __global__ void k_gather(int n, const int32_t* __restrict__ perm, const int32_t*
     const double x = in.x[o], y = in.y[o];
     out.x[k] = x;
     out.y[k] = y;
-    out.xf[k] = f32(x);
-    out.yf[k] = f32(y);
+    out.xyf[k] = make_float2(f32(x), f32(y));
     out.vx[k] = in.vx[o];
     out.vy[k] = in.vy[o];
     if (!planar) {

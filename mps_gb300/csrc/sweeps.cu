@@ -37,7 +37,8 @@ template <bool PLANAR, class F>
 __device__ __forceinline__ void for_each_near(const Consts& c, const StateBuf& s,
                                               const int32_t* __restrict__ cs, int32_t key, int k,
                                               float bound, F&& f) {
-    const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
+    const float2 fk = s.xyf[k];
+    const float fx = fk.x, fy = fk.y, fz = PLANAR ? 0.f : s.zf[k];
     int cand[kNear];
     int ns = 0;
     for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
@@ -61,7 +62,8 @@ template <bool PLANAR>
 __device__ double sweep_number_density_p(const Consts& c, const StateBuf& s, const int32_t* cs,
                                          int32_t key, int k) {
     double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
-    const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
+    const float2 fk = s.xyf[k];
+    const float fx = fk.x, fy = fk.y, fz = PLANAR ? 0.f : s.zf[k];
     double nd = 0.0;
     for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
         if (j == k || far32<PLANAR>(s, j, fx, fy, fz, c.ft_max)) return;
@@ -180,7 +182,8 @@ __device__ __forceinline__ int for_each_collision(const Consts& c, const StateBu
                                                   const int32_t* cs, int32_t key, int k,
                                                   CollPair* out) {
     double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
-    const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
+    const float2 fk = s.xyf[k];
+    const float fx = fk.x, fy = fk.y, fz = PLANAR ? 0.f : s.zf[k];
     int32_t idi = s.id[k];
     int m = 0;
     for_each_candidate<PLANAR>(c, cs, key, [&](int j) {
@@ -400,7 +403,8 @@ __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
     int m = 0;
     if (valid) {
         const double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
-        const float fx = s.xf[k], fy = s.yf[k], fz = PLANAR ? 0.f : s.zf[k];
+        const float2 fk = s.xyf[k];
+        const float fx = fk.x, fy = fk.y, fz = PLANAR ? 0.f : s.zf[k];
         // Pass 1: the candidates that survive the FP32 pre-filter, in sweep
         // order.  Pass 2 then runs the exact FP64 test, square root and
         // division on these compact per-particle lists, with nearly all lanes
@@ -687,12 +691,14 @@ __global__ void k_cc_apply(Consts c, StateBuf s, const int* __restrict__ par,
 // ---------------------------------------------------------------------------
 // solvePoissonEquation's scatter + removeNegativePressure (src/mps.cpp:466-479)
 __global__ void k_pressure_out(int n, const double* __restrict__ x, double* __restrict__ p,
+                               const int32_t* __restrict__ id, double* __restrict__ x_prev,
                                DevStats* ds) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     double v = x[k];
     if (!isfinite(v)) atomicOr(&ds->status, ST_NONFINITE);
     p[k] = v < 0.0 ? 0.0 : v;
+    if (x_prev) x_prev[id[k]] = v;
 }
 
 // MPS::setMinimumPressure (src/mps.cpp:481-503)
@@ -931,10 +937,10 @@ void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, cons
 }
 
 void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb, const double* x,
-                          double* ax, double* ay, double* az, int mixed, DevStats* ds,
-                          cudaStream_t st) {
+                          double* x_prev, double* ax, double* ay, double* az, int mixed,
+                          DevStats* ds, cudaStream_t st) {
     int g = blocks_for(c.n);
-    k_pressure_out<<<g, kThreads, 0, st>>>(c.n, x, s.p, ds);
+    k_pressure_out<<<g, kThreads, 0, st>>>(c.n, x, s.p, s.id, x_prev, ds);
     ++g_launches;
     k_min_pressure<<<g, kThreads, 0, st>>>(c, s, nb);
     ++g_launches;

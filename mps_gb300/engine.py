@@ -115,6 +115,8 @@ def load(build_if_missing: bool = False):
     L.mps_set_solver.argtypes = [vp, C.c_int32, C.c_double, C.c_int64]
     L.mps_set_multigrid.argtypes = [vp, C.c_int32, C.c_float, C.c_float]
     L.mps_set_multigrid.restype = C.c_int
+    L.mps_set_initial_guess.argtypes = [vp, C.c_int32]
+    L.mps_set_initial_guess.restype = C.c_int
     L.mps_set_collisions.argtypes = [vp, C.c_int32]
     L.mps_set_collisions.restype = C.c_int
     L.mps_set_graphs.argtypes = [vp, C.c_int32]
@@ -319,10 +321,16 @@ class Engine:
     def set_multigrid(self, mode=1, omega=0.0, scale=0.0):
         """Preconditioner of the MIXED solver: 0 Jacobi, 1 multigrid additive at
         the particle level (default), 2 multiplicative V(1,1), 3 additive with
-        the smoothed particle-to-cell transfer (True/False map to 1/0).
+        the smoothed particle-to-cell transfer, 4 mode 1's preconditioner with the
+        operator applied after the cycle (True/False map to 1/0).
         omega/scale 0 take the mode's default weights."""
         mode = int(mode) if not isinstance(mode, bool) else (1 if mode else 0)
         _check(_lib.mps_set_multigrid(self._h, mode, float(omega), float(scale)))
+
+    def set_initial_guess(self, previous=True):
+        """MIXED solver's initial guess: the previous step's solution of the same
+        particles (default) or zero (the reference's CG start)."""
+        _check(_lib.mps_set_initial_guess(self._h, 1 if previous else 0))
 
     def set_collisions(self, serial=False):
         """Collision pairs applied in parallel (default) or by one thread in order."""
