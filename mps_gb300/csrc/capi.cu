@@ -624,7 +624,8 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         e->alloc(&e->nb.wp, np * K) || e->alloc(&e->A.src, np) || e->alloc(&e->A.diag, np) ||
         e->alloc(&e->A.offcnt, np) || e->alloc(&e->A.col, np * K) || e->alloc(&e->A.val, np * K) ||
         e->alloc(&e->A.slice_w, np / 32 + 1) || e->alloc(&e->A.val32, np * K) ||
-        e->alloc(&e->A.diag32, np) || e->alloc(&e->kv.x, np) || e->alloc(&e->kv.r, np) ||
+        e->alloc(&e->A.diag32, np) || e->alloc(&e->A.rsum, np) || e->alloc(&e->A.rsum32, np) ||
+        e->alloc(&e->kv.x, np) || e->alloc(&e->kv.r, np) ||
         e->alloc(&e->kv.x_prev, np) ||
         e->alloc(&e->kv.p, np) || e->alloc(&e->kv.q, np) || e->alloc(&e->kv.z, np) ||
         e->alloc(&e->kv.inv_diag, np) || e->alloc(&e->kv.r32, np) || e->alloc(&e->kv.p32, np) ||

@@ -142,6 +142,15 @@ struct Ppe {
     int32_t* slice_w; // max offcnt of each 32-slot slice
     float* val32;     // FP32 copy of val, quad layout (qsell_index) for the mixed solver
     float* diag32;
+    // Row sums diag + sum of the row's off-diagonals, formed in FP64 from the
+    // assembly's terms (the compressibility term plus the weights of
+    // neighbours that are not unknowns; Dirichlet doubling added), and their
+    // FP32 rounding.  The mixed solver applies its FP32 operator as
+    // sum_j a_ij (v_j - v_i) + rsum_i v_i: on smooth vectors the FP32 sum of
+    // a_ij v_j cancels to a small row sum and loses it, and the FP32-rounded
+    // entries do not sum to it.
+    double* rsum;
+    float* rsum32;
 };
 
 // Quad SELL-32 layout of the mixed solver's FP32 operator: entry m of slot k

@@ -313,17 +313,25 @@ __device__ __forceinline__ double spmv64_row(const Ppe& A, int K, int sl, int la
     return fma(A.diag[row], xi, s0 + s1);
 }
 
+// The FP32 operator rows below return the off-diagonal part in difference
+// form, sum_j a_ij (u_j - u_i), given the row's own value u_i; the caller
+// adds rsum32_i u_i (the row sum times u_i).  For a smooth u the differences
+// are small and exact to within their own rounding, so the product does not
+// lose the row's small sum to cancellation, and the FP32 rounding of the
+// entries no longer shifts the row sum (the operator's smooth modes).
+// Padding entries (value 0) add 0.
+
 // FP32 SELL row (rows without a compact form): int32 columns of the FP64
 // matrix, FP32 values in the quad layout.
 __device__ __forceinline__ float spmv32_sell_row(const Ppe& A, int K, int row,
-                                                 const float* __restrict__ u) {
+                                                 const float* __restrict__ u, float ui) {
     const int sl = row >> 5, lane = row & 31;
     const int w = __ldg(A.slice_w + sl);
     const int32_t* cp = A.col + (size_t)sl * K * 32 + lane;
     const float* vq = A.val32 + qsell_index(row, 0, K);
     float s = 0.f;
     for (int m = 0; m < w; m++)
-        s = fmaf(__ldg(vq + (m >> 2) * 128 + (m & 3)), __ldcg(u + __ldg(cp + m * 32)), s);
+        s = fmaf(__ldg(vq + (m >> 2) * 128 + (m & 3)), __ldcg(u + __ldg(cp + m * 32)) - ui, s);
     return s;
 }
 
@@ -337,7 +345,7 @@ __device__ __forceinline__ float spmv32_sell_row(const Ppe& A, int K, int row,
 // same for any kGroups.
 constexpr int kGroups = 4;
 __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf, int K, int row,
-                                                 const float* __restrict__ u) {
+                                                 const float* __restrict__ u, float ui) {
     const int sl = row >> 5;
     const int w = __ldg(A.slice_w + sl);
     const int s0 = __ldg(mf.rs + row), s1 = __ldg(mf.rs + mf.rs_stride + row),
@@ -365,7 +373,7 @@ __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf
 #pragma unroll
         for (int q = 0; q < kGroups; q++)
 #pragma unroll
-            for (int t = 0; t < 4; t++) x[q][t] = __ldcg(u + col(b4[q], t));
+            for (int t = 0; t < 4; t++) x[q][t] = __ldcg(u + col(b4[q], t)) - ui;
 #pragma unroll
         for (int q = 0; q < kGroups; q++) {
             a0 = fmaf(v[q].x, x[q][0], a0);
@@ -379,7 +387,7 @@ __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf
         const uint32_t b4 = __ldg(ip + g * 32);
         float x[4];
 #pragma unroll
-        for (int t = 0; t < 4; t++) x[t] = __ldcg(u + col(b4, t));
+        for (int t = 0; t < 4; t++) x[t] = __ldcg(u + col(b4, t)) - ui;
         a0 = fmaf(v.x, x[0], a0);
         a1 = fmaf(v.y, x[1], a1);
         a0 = fmaf(v.z, x[2], a0);
@@ -397,7 +405,8 @@ __device__ __forceinline__ float compact_row_sum(const Ppe& A, const MatFree& mf
 // a1: 1, 3) without a serial tail per row.
 __device__ __forceinline__ void compact_pair(const Ppe& A, const MatFree& mf, int K, int ra, int rb,
                                              int wa, int wb, const int (&sa)[3], const int (&sb)[3],
-                                             const float* __restrict__ u, float& oa, float& ob) {
+                                             const float* __restrict__ u, float ua, float ub, float& oa,
+                                             float& ob) {
     const float4* vpa = reinterpret_cast<const float4*>(A.val32) + (qsell_index(ra, 0, K) >> 2);
     const float4* vpb = reinterpret_cast<const float4*>(A.val32) + (qsell_index(rb, 0, K) >> 2);
     const uint32_t* ipa = reinterpret_cast<const uint32_t*>(mf.idx8) + (qsell_index(ra, 0, K) >> 2);
@@ -419,10 +428,10 @@ __device__ __forceinline__ void compact_pair(const Ppe& A, const MatFree& mf, in
         float xa[8], xb[8];
 #pragma unroll
         for (int t = 0; t < 4; t++) {
-            xa[t] = __ldcg(u + col(sa, ia0, t));
-            xa[4 + t] = __ldcg(u + col(sa, ia1, t));
-            xb[t] = __ldcg(u + col(sb, ib0, t));
-            xb[4 + t] = __ldcg(u + col(sb, ib1, t));
+            xa[t] = __ldcg(u + col(sa, ia0, t)) - ua;
+            xa[4 + t] = __ldcg(u + col(sa, ia1, t)) - ua;
+            xb[t] = __ldcg(u + col(sb, ib0, t)) - ub;
+            xb[4 + t] = __ldcg(u + col(sb, ib1, t)) - ub;
         }
         const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
         if (g >= ga) va0 = z;
@@ -454,10 +463,11 @@ __device__ __forceinline__ void compact_pair(const Ppe& A, const MatFree& mf, in
 // compact.  Both rows' format flags, slice widths and range starts are loaded
 // in one batch, before the branch that needs the flags.
 __device__ __forceinline__ void off_rows(const Ppe& A, const MatFree& mf, int K, int i, int i2,
-                                         const float* __restrict__ v, float& o, float& o2) {
+                                         const float* __restrict__ v, float vi, float vi2, float& o,
+                                         float& o2) {
     if (!mf.enabled) {
-        o = spmv32_sell_row(A, K, i, v);
-        o2 = i2 >= 0 ? spmv32_sell_row(A, K, i2, v) : 0.f;
+        o = spmv32_sell_row(A, K, i, v, vi);
+        o2 = i2 >= 0 ? spmv32_sell_row(A, K, i2, v, vi2) : 0.f;
         return;
     }
     const int j2 = i2 >= 0 ? i2 : i;  // a lone row is paired with itself
@@ -468,12 +478,12 @@ __device__ __forceinline__ void off_rows(const Ppe& A, const MatFree& mf, int K,
     // pairs need a group in each row (a slice of rows without off-diagonals
     // has width 0 and no stored groups at all)
     if (!fa && !fb && wa > 0 && wb > 0) {
-        compact_pair(A, mf, K, i, j2, wa, wb, sa, sb, v, o, o2);
+        compact_pair(A, mf, K, i, j2, wa, wb, sa, sb, v, vi, i2 >= 0 ? vi2 : vi, o, o2);
         if (i2 < 0) o2 = 0.f;
         return;
     }
-    o = fa ? spmv32_sell_row(A, K, i, v) : compact_row_sum(A, mf, K, i, v);
-    o2 = i2 < 0 ? 0.f : (fb ? spmv32_sell_row(A, K, i2, v) : compact_row_sum(A, mf, K, i2, v));
+    o = fa ? spmv32_sell_row(A, K, i, v, vi) : compact_row_sum(A, mf, K, i, v, vi);
+    o2 = i2 < 0 ? 0.f : (fb ? spmv32_sell_row(A, K, i2, v, vi2) : compact_row_sum(A, mf, K, i2, v, vi2));
 }
 
 // ----------------------------------------------------------------- FP64 CG
@@ -878,14 +888,15 @@ __device__ __forceinline__ bool mg_vcycle(const Mg& mg, uint32_t& swp, const Ppe
     if (!mg.additive) {
     for (int i = gtid; i < n; i += 2 * gsz) {
         const int i2 = i + gsz < n ? i + gsz : -1;
+        const float ea = __ldcg(mg.e0 + i), eb = i2 >= 0 ? __ldcg(mg.e0 + i2) : 0.f;
         float o, o2;
-        off_rows(A, mf, K, i, i2, mg.e0, o, o2);
+        off_rows(A, mf, K, i, i2, mg.e0, ea, eb, o, o2);
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const int row = h == 0 ? i : i2;
             if (row < 0) break;
             const float dg = A.diag32[row];
-            mg.res0[row] = dg > 0.f ? __ldcg(r + row) - fmaf(dg, __ldcg(mg.e0 + row), h == 0 ? o : o2) : 0.f;
+            mg.res0[row] = dg > 0.f ? __ldcg(r + row) - fmaf(A.rsum32[row], h == 0 ? ea : eb, h == 0 ? o : o2) : 0.f;
         }
     }
     if (!grid_sync(gb, ds)) return false;
@@ -1048,15 +1059,17 @@ __device__ __forceinline__ bool mg_vcycle(const Mg& mg, uint32_t& swp, const Ppe
     if (!grid_sync(gb, ds)) return false;
     for (int i = gtid; i < n; i += 2 * gsz) {
         const int i2 = i + gsz < n ? i + gsz : -1;
+        const float ea = __ldcg(mg.e0 + i), eb = i2 >= 0 ? __ldcg(mg.e0 + i2) : 0.f;
         float o, o2;
-        off_rows(A, mf, K, i, i2, mg.e0, o, o2);
+        off_rows(A, mf, K, i, i2, mg.e0, ea, eb, o, o2);
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const int row = h == 0 ? i : i2;
             if (row < 0) break;
             const float dg = A.diag32[row];
-            const float e0 = __ldcg(mg.e0 + row);
-            u[row] = dg > 0.f ? fmaf(mg.omega / dg, __ldcg(r + row) - fmaf(dg, e0, h == 0 ? o : o2), e0) : 0.f;
+            const float e0 = h == 0 ? ea : eb;
+            u[row] = dg > 0.f ? fmaf(mg.omega / dg, __ldcg(r + row) - fmaf(A.rsum32[row], e0, h == 0 ? o : o2), e0)
+                              : 0.f;
         }
     }
     return true;
@@ -1155,12 +1168,12 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, con
                     rv[h] = kv.r32[row];
                 }
                 float o, o2;
-                off_rows(A, mf, a.K, i, i2, kv.u32, o, o2);
+                off_rows(A, mf, a.K, i, i2, kv.u32, ui[0], ui[1], o, o2);
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int row = h == 0 ? i : i2;
                     if (row < 0) break;
-                    const float w = dg[h] > 0.f ? fmaf(dg[h], ui[h], h == 0 ? o : o2) : 0.f;
+                    const float w = dg[h] > 0.f ? fmaf(A.rsum32[row], ui[h], h == 0 ? o : o2) : 0.f;
                     kv.w32[row] = w;
                     acc_prod(g, rv[h], ui[h]);
                     acc_prod(dl, w, ui[h]);
@@ -1416,11 +1429,12 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
                     if (i >= n) continue;  // the partial last slice (then i2 < 0 too)
                     const int j2 = i2 >= 0 ? i2 : i;
                     const float dg0 = A.diag32[i], dg1 = A.diag32[j2];
+                    const float c0 = A.rsum32[i], c1 = A.rsum32[j2];
                     const float y0 = __ldcg(y + i), y1 = __ldcg(y + j2);
                     float o, o2;
-                    off_rows(A, mf, a.K, i, i2, y, o, o2);
-                    z[i] = dg0 > 0.f ? fmaf(dg0, y0, o) : 0.f;
-                    if (i2 >= 0) z[i2] = dg1 > 0.f ? fmaf(dg1, y1, o2) : 0.f;
+                    off_rows(A, mf, a.K, i, i2, y, y0, y1, o, o2);
+                    z[i] = dg0 > 0.f ? fmaf(c0, y0, o) : 0.f;
+                    if (i2 >= 0) z[i2] = dg1 > 0.f ? fmaf(c1, y1, o2) : 0.f;
                 }
                 swp ^= cycle_swaps;
             }
@@ -1434,12 +1448,13 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
                 if (sla >= nsl) break;
                 const int slb = rb + RB * (q + kW);
                 int ii[2] = {sla * 32 + lane, slb < nsl ? slb * 32 + lane : n};
-                float dg[2], ri[2], yi[2], zi[2];
+                float dg[2], cs[2], ri[2], yi[2], zi[2];
                 int key[2];
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int i = min(ii[h], n - 1);
                     dg[h] = A.diag32[i];
+                    cs[h] = A.rsum32[i];
                     ri[h] = __ldcg(kv.r32 + i);
                     yi[h] = __ldcg(y + i);
                     zi[h] = __ldcg(z + i);
@@ -1451,15 +1466,19 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
                     const int i = ii[h];
                     float u = 0.f, w = 0.f;
                     if (dg[h] > 0.f) {  // an unknown: its cell is interior
+                        // B e1 = sum_d B_d e1_d in difference form around the
+                        // row's own cell (d = 4): the B_d sum to the row sum
                         float bt[9], en[9];
 #pragma unroll
                         for (int d = 0; d < 9; d++) {
-                            bt[d] = __ldg(mg.rowcell + (size_t)d * np + i);
+                            bt[d] = d == 4 ? 0.f : __ldg(mg.rowcell + (size_t)d * np + i);
                             en[d] = __ldcg(e1 + key[h] + (d / 3 - 1) * NY + (d % 3 - 1));
                         }
                         float corr = 0.f;
 #pragma unroll
-                        for (int d = 0; d < 9; d++) corr = fmaf(bt[d], en[d], corr);
+                        for (int d = 0; d < 9; d++)
+                            if (d != 4) corr = fmaf(bt[d], en[d] - en[4], corr);
+                        corr = fmaf(cs[h], en[4], corr);
                         u = fmaf(mg.scale, en[4], mg.omega * yi[h]);
                         w = fmaf(mg.scale, corr, mg.omega * zi[h]);
                     }
@@ -1601,6 +1620,7 @@ __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv, const int3
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.n) return;
     const double d = A.diag[k];
+    A.rsum32[k] = f32(A.rsum[k]);
     // initial guess: the particle's solution of the last solve (rows without
     // an unknown stay 0, as the zero start leaves them)
     if (warm) kv.x[k] = d > 0.0 ? kv.x_prev[ids[k]] : 0.0;
@@ -1661,7 +1681,11 @@ SolveArgs make_args(const Consts& c, double tol, int64_t max_iter) {
     a.K = c.K;
     a.tol = tol;
     a.max_iter = max_iter;
-    a.inner_tol = 1e-6;  // FP32 floor of an inner solve's residual reduction
+    // An inner solve's residual reduction: with the operator in difference
+    // form one refinement reaches ~1e-5 of its start on the 1M-particle dam
+    // break (FP32 vectors); asking for more costs iterations that the next
+    // refinement's FP64 residual does not see.
+    a.inner_tol = 1e-5;
     a.max_refine = 40;
     a.warm = 0;
     return a;

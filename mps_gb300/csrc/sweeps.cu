@@ -519,6 +519,7 @@ __global__ void __launch_bounds__(kThreads) k_assemble(Consts c, StateBuf s, NbL
     int off = 0;
     if (k < c.n) {
         double diag = 0.0;
+        double rsum = 0.0;  // diag + the off-diagonals: the terms of neighbours without an unknown
         if (s.bc[k] == BC_INNER) {
             const int np = nb.n_pad, m = nb.cnt[k];
             const size_t sbase = (size_t)(k >> 5) * c.K * 32 + (k & 31);
@@ -534,11 +535,17 @@ __global__ void __launch_bounds__(kThreads) k_assemble(Consts c, StateBuf s, NbL
                     A.col[sbase + (size_t)off * 32] = j;
                     A.val[sbase + (size_t)off * 32] = -a;
                     off++;
+                } else {
+                    rsum = dadd(rsum, a);
                 }
             }
-            if (c.qc_on) diag = dadd(diag, c.qc_term);
+            if (c.qc_on) {
+                diag = dadd(diag, c.qc_term);
+                rsum = dadd(rsum, c.qc_term);
+            }
         }
         A.diag[k] = diag;
+        A.rsum[k] = rsum;
         A.offcnt[k] = off;
     }
     int w = __reduce_max_sync(0xffffffffu, off);
@@ -683,6 +690,7 @@ __global__ void k_cc_apply(Consts c, StateBuf s, const int* __restrict__ par,
     int8_t conn = (s.type[k] != T_GHOST && has_surface[r]) ? 1 : 0;
     s.dir[k] = conn;
     if (!conn && s.bc[k] == BC_INNER) {
+        A.rsum[k] = dadd(A.rsum[k], A.diag[k]);  // the row sum grows by the old diagonal
         A.diag[k] = dmul(A.diag[k], 2.0);
         atomicAdd(&ds->n_unconnected, 1);
     }
