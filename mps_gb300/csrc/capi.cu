@@ -322,19 +322,20 @@ void enqueue_step(mps_engine* e, bool do_export) {
 // counted once at its stored width (gathered vector entries count once, as
 // the row's own entry).  Per stored off-diagonal entry and pass: FP64 12 B
 // (column + value), compact FP32 5 B (value + index byte).  Per row and
-// iteration: FP64 CG 116 B (8 vectors); MIXED inner iteration 65 B with the
+// iteration: FP64 CG 116 B (8 vectors); MIXED inner iteration 69 B with the
 // Jacobi preconditioner; with the multigrid V-cycle, per cell of level 1
 // 72 B (segment bounds, the up pass's 9-point stencil and 8 vector words)
 // and of levels >= 2 132 B (the same plus the 4x4 restriction weights), and,
-// additive at level 0, 81 B per row (161 B with the smoothed transfer: the
-// 9 row-to-cell sums read twice and the neighbourhood's residuals; 141 B in
+// additive at level 0, 85 B per row (165 B with the smoothed transfer: the
+// 9 row-to-cell sums read twice and the neighbourhood's residuals; 145 B in
 // the overlapped arrangement of mode 1: the operator pass on y = D^-1 r
-// 25 B, the pass that forms u, w and the dot products 64 B with the 9
-// row-to-cell sums, the vector update 48 B, the level-1 sums 4 B),
-// multiplicative 143 B per row and two more level-0 operator passes.  MIXED adds per refinement the FP64
-// residual (12 B/entry + 36 B/row) and once the FP32 operator setup
-// (17 B/entry + 16 B/row written and read; 36 B/row more for the row-to-cell
-// sums of modes 1 and 3).
+// 29 B, the pass that forms u, w and the dot products 64 B with 8
+// row-to-cell sums and the row sum, the vector update 48 B, the level-1
+// sums 4 B), multiplicative 155 B per row and two more level-0 operator
+// passes (every operator pass reads the row's FP32 row sum).  MIXED adds per
+// refinement the FP64 residual (12 B/entry + 36 B/row) and once the FP32
+// operator setup (17 B/entry + 28 B/row written and read; 36 B/row more for
+// the row-to-cell sums of modes 1 and 3).
 double solve_bytes(const mps_engine* e, const DevStats& h) {
     const double nnz = (double)h.nnz_off, n = (double)e->n, it = (double)h.cg_iterations;
     if (e->precision == MPS_PRECISION_FP64) return it * (12.0 * nnz + 116.0 * n) + 36.0 * n;
@@ -342,14 +343,14 @@ double solve_bytes(const mps_engine* e, const DevStats& h) {
     const bool mg = g.enabled != 0;
     const bool additive = mg && g.additive;
     const double ent = e->c.planar ? 5.0 : 8.0;
-    const double row_add = g.smooth ? 161.0 : g.overlap ? 141.0 : 81.0;
-    double per_it = !mg ? (ent * nnz + 65.0 * n)
-                        : additive ? (ent * nnz + row_add * n) : (3.0 * ent * nnz + 143.0 * n);
+    const double row_add = g.smooth ? 165.0 : g.overlap ? 145.0 : 85.0;
+    double per_it = !mg ? (ent * nnz + 69.0 * n)
+                        : additive ? (ent * nnz + row_add * n) : (3.0 * ent * nnz + 155.0 * n);
     if (mg)
         for (int l = 1; l <= e->mg.nlev; l++)
             per_it += (l == 1 ? 72.0 : 132.0) * e->mg.lev[l].nx * e->mg.lev[l].ny;
     const double ref = (double)h.refinements + 1.0;
-    const double setup = 17.0 * nnz + 16.0 * n + (mg && (g.smooth || g.overlap) ? 36.0 * n : 0.0);
+    const double setup = 17.0 * nnz + 28.0 * n + (mg && (g.smooth || g.overlap) ? 36.0 * n : 0.0);
     return it * per_it + ref * (12.0 * nnz + 36.0 * n) + setup;
 }
 
