@@ -183,6 +183,9 @@ int alloc_state(mps_engine* e, StateBuf& s) {
     CU(e->alloc(&s.z, n));
     CU(e->alloc(&s.xyf, n));
     CU(e->alloc(&s.zf, n));
+    CU(e->alloc(&s.xylo, n));
+    CU(e->alloc(&s.vf, n));
+    CU(e->alloc(&s.pf, n));
     CU(e->alloc(&s.vx, n));
     CU(e->alloc(&s.vy, n));
     CU(e->alloc(&s.vz, n));
@@ -582,6 +585,9 @@ int mps_create(const mps_params* prm, int32_t n, const double* pos, const double
         c.ft_max = fbound(c.re_max);
         c.ft_v = fbound(c.re_v);
         c.ft_cd = fbound(c.cd);
+        const double tv = std::min(c.t_max, c.t_v);
+        c.fv_in = std::nextafter((float)(tv * (1.0 - std::ldexp(1.0, -16))), 0.0f);
+        c.fv_out = std::nextafter((float)(tv * (1.0 + std::ldexp(1.0, -16))), std::numeric_limits<float>::infinity());
     }
     ref_values(P.dim, c.l0, c.re_p, &c.n0_p, &c.lam_p);
     ref_values(P.dim, c.l0, c.re_v, &c.n0_v, &c.lam_v);

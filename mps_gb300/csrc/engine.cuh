@@ -53,6 +53,12 @@ struct Consts {
     // that radius in exact FP64 (margin: the FP32 rounding of coordinates of
     // magnitude up to the domain bound), so only the rest get the exact test
     float ft_max, ft_v, ft_cd;
+    // The mixed viscosity sweep decides "inside the radius" from the FP32
+    // squared distance of its coordinate pairs when that lies outside
+    // [fv_in, fv_out], a band of 2^-16 relative around the exact threshold
+    // min(t_max, t_v) that holds the pairs' error bound (2^-20) many times;
+    // inside the band it runs the exact FP64 test.
+    float fv_in, fv_out;
     double beta_n0s;    // beta * n0 (src/mps.cpp:271)
     double visc_a;      // nu * (2 dim) / (n0 lambda)           src/mps.cpp:182
     double mat_c;       // 2 D / (lambda n0)                     src/mps.cpp:343
@@ -71,6 +77,14 @@ struct StateBuf {
     // candidate in the neighbour sweeps' pre-filter), written by the rebuild gather
     float2* xyf;
     float* zf;
+    // The mixed step's FP32 work on planar scenes (written by the rebuild
+    // gather unless noted): the low parts x - xyf and y - xyf rounded to FP32
+    // (so that a coordinate difference is formed from FP32 pairs to within
+    // FP32 rounding of the difference itself), the FP32 velocities, and the
+    // pressure split the same way (hi, lo; written after the solve).
+    float2* xylo;
+    float2* vf;
+    float2* pf;
     double *p, *minp, *ndr, *nd_last;
     int32_t* id;
     int8_t *type, *bc, *dir;

@@ -95,9 +95,14 @@ __global__ void k_gather(int n, const int32_t* __restrict__ perm, const int32_t*
     const double x = in.x[o], y = in.y[o];
     out.x[k] = x;
     out.y[k] = y;
-    out.xyf[k] = make_float2(f32(x), f32(y));
-    out.vx[k] = in.vx[o];
-    out.vy[k] = in.vy[o];
+    const float xh = f32(x), yh = f32(y);
+    out.xyf[k] = make_float2(xh, yh);
+    // x - xh is exact in FP64 (xh is x rounded to 24 bits)
+    out.xylo[k] = make_float2(f32(x - (double)xh), f32(y - (double)yh));
+    const double vx = in.vx[o], vy = in.vy[o];
+    out.vx[k] = vx;
+    out.vy[k] = vy;
+    out.vf[k] = make_float2(f32(vx), f32(vy));
     if (!planar) {
         const double z = in.z[o];
         out.z[k] = z;

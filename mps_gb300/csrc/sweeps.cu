@@ -105,6 +105,34 @@ __global__ void __launch_bounds__(kThreads) k_explicit(Consts c, StateBuf in, St
             ax = dadd(c.g[0], dmul(tx, c.visc_a));
             ay = dadd(c.g[1], dmul(ty, c.visc_a));
             az = PLANAR ? 0.0 : dadd(c.g[2], dmul(tz, c.visc_a));
+        } else if (PLANAR) {
+            // FP32 weights and FP32 accumulation; the neighbour set is the
+            // exact FP64 one: the FP32 squared distance of the coordinate
+            // pairs decides outside the band [fv_in, fv_out] around the
+            // threshold (its error is far inside the band), the exact FP64
+            // test inside it
+            float tx = 0.f, ty = 0.f;
+            const float2 hk = in.xyf[k], lk = in.xylo[k], vk = in.vf[k];
+            for_each_near<PLANAR>(c, in, cs, key, k, c.ft_v, [&](int j) {
+                const float2 hj = in.xyf[j], lj = in.xylo[j];
+                const float dx = (hj.x - hk.x) + (lj.x - lk.x);
+                const float dy = (hj.y - hk.y) + (lj.y - lk.y);
+                const float d2f = dx * dx + dy * dy;
+                bool inside = d2f < c.fv_in;
+                if (!inside && !(d2f > c.fv_out)) {
+                    const double d2 = dist2<PLANAR>(in, k, j, x, y, z);
+                    inside = lt_cut(d2, c.t_max) && lt_cut(d2, c.t_v);
+                }
+                if (inside) {
+                    const float2 vj = in.vf[j];
+                    const float w = c.fre_v * rsqrtf(d2f) - 1.f;
+                    tx = fmaf(vj.x - vk.x, w, tx);
+                    ty = fmaf(vj.y - vk.y, w, ty);
+                }
+            });
+            ax = c.g[0] + (double)(tx * c.fvisc_a);
+            ay = c.g[1] + (double)(ty * c.fvisc_a);
+            az = 0.0;
         } else {
             // FP32 weights and FP32 accumulation; the neighbour set is the
             // exact FP64 one.
@@ -699,13 +727,16 @@ __global__ void k_cc_apply(Consts c, StateBuf s, const int* __restrict__ par,
 // ---------------------------------------------------------------------------
 // solvePoissonEquation's scatter + removeNegativePressure (src/mps.cpp:466-479)
 __global__ void k_pressure_out(int n, const double* __restrict__ x, double* __restrict__ p,
-                               const int32_t* __restrict__ id, double* __restrict__ x_prev,
-                               DevStats* ds) {
+                               float2* __restrict__ pf, const int32_t* __restrict__ id,
+                               double* __restrict__ x_prev, DevStats* ds) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     double v = x[k];
     if (!isfinite(v)) atomicOr(&ds->status, ST_NONFINITE);
-    p[k] = v < 0.0 ? 0.0 : v;
+    const double pv = v < 0.0 ? 0.0 : v;
+    p[k] = pv;
+    const float ph = f32(pv);
+    pf[k] = make_float2(ph, f32(pv - (double)ph));  // pv - ph is exact
     if (x_prev) x_prev[id[k]] = v;
 }
 
@@ -754,6 +785,29 @@ __global__ void __launch_bounds__(kThreads) k_gradient(Consts c, StateBuf s, NbL
         ax[k] = ddiv(dmul(-1.0, gx), c.rho);
         ay[k] = ddiv(dmul(-1.0, gy), c.rho);
         if (!PLANAR) az[k] = ddiv(dmul(-1.0, dmul(gz, c.grad_scale)), c.rho);
+    } else if (PLANAR) {
+        // FP32 throughout: the coordinate and pressure differences from the
+        // FP32 pairs (hi, lo), each within FP32 rounding of the exact
+        // difference (the FP64 subtractions they replace were most of this
+        // kernel's FP64 pipe time)
+        float gx = 0.f, gy = 0.f;
+        const float2 hk = s.xyf[k], lk = s.xylo[k];
+        const float pmh = f32(pmin), pml = f32(pmin - (double)pmh);
+        for (int q = 0; q < m; q++) {
+            int j = nb.slot[(size_t)q * np + k];
+            if (s.type[j] == T_DUMMY) continue;
+            double dist = nb.dist[(size_t)q * np + k];
+            if (!lt_cut(dist, c.re_p)) continue;
+            const float2 hj = s.xyf[j], lj = s.xylo[j], pj = s.pf[j];
+            const float fd = f32(dist);
+            const float dp = (pj.x - pmh) + (pj.y - pml);
+            const float coef = dp * (c.fre_p / fd - 1.f) / (fd * fd);
+            gx = fmaf((hj.x - hk.x) + (lj.x - lk.x), coef, gx);
+            gy = fmaf((hj.y - hk.y) + (lj.y - lk.y), coef, gy);
+        }
+        const float sc = -c.fgrad_scale / f32(c.rho);
+        ax[k] = (double)(gx * sc);
+        ay[k] = (double)(gy * sc);
     } else {
         float gx = 0.f, gy = 0.f, gz = 0.f;
         for (int q = 0; q < m; q++) {
@@ -765,7 +819,7 @@ __global__ void __launch_bounds__(kThreads) k_gradient(Consts c, StateBuf s, NbL
             float coef = f32(s.p[j] - pmin) * (c.fre_p / fd - 1.f) / (fd * fd);
             gx = fmaf(f32(s.x[j] - xi), coef, gx);
             gy = fmaf(f32(s.y[j] - yi), coef, gy);
-            if (!PLANAR) gz = fmaf(f32(s.z[j] - zi), coef, gz);
+            gz = fmaf(f32(s.z[j] - zi), coef, gz);
         }
         const float sc = -c.fgrad_scale / f32(c.rho);
         ax[k] = (double)(gx * sc);
@@ -948,7 +1002,7 @@ void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb, 
                           double* x_prev, double* ax, double* ay, double* az, int mixed,
                           DevStats* ds, cudaStream_t st) {
     int g = blocks_for(c.n);
-    k_pressure_out<<<g, kThreads, 0, st>>>(c.n, x, s.p, s.id, x_prev, ds);
+    k_pressure_out<<<g, kThreads, 0, st>>>(c.n, x, s.p, s.pf, s.id, x_prev, ds);
     ++g_launches;
     k_min_pressure<<<g, kThreads, 0, st>>>(c, s, nb);
     ++g_launches;
