@@ -338,7 +338,8 @@ void enqueue_step(mps_engine* e, bool do_export) {
 // passes (every operator pass reads the row's FP32 row sum).  MIXED adds per
 // refinement the FP64 residual (12 B/entry + 36 B/row) and once the FP32
 // operator setup (17 B/entry + 28 B/row written and read; 36 B/row more for
-// the row-to-cell sums of modes 1 and 3).
+// the row-to-cell sums of the multigrid modes, from which level 1's stencils
+// are summed).
 double solve_bytes(const mps_engine* e, const DevStats& h) {
     const double nnz = (double)h.nnz_off, n = (double)e->n, it = (double)h.cg_iterations;
     if (e->precision == MPS_PRECISION_FP64) return it * (12.0 * nnz + 116.0 * n) + 36.0 * n;
@@ -353,7 +354,7 @@ double solve_bytes(const mps_engine* e, const DevStats& h) {
         for (int l = 1; l <= e->mg.nlev; l++)
             per_it += (l == 1 ? 72.0 : 132.0) * e->mg.lev[l].nx * e->mg.lev[l].ny;
     const double ref = (double)h.refinements + 1.0;
-    const double setup = 17.0 * nnz + 28.0 * n + (mg && (g.smooth || g.overlap) ? 36.0 * n : 0.0);
+    const double setup = 17.0 * nnz + 28.0 * n + (mg ? 36.0 * n : 0.0);
     return it * per_it + ref * (12.0 * nnz + 36.0 * n) + setup;
 }
 

@@ -58,66 +58,21 @@ __global__ void k_mg_clear(Mg mg) {
     }
 }
 
-__global__ void k_mg_level1(Consts c, Ppe A, MatFree mf, MgLevel L, int32_t* nact, int2* act_rng) {
+// Level 1's 9-point stencil of cell I: the sum over the cell's rows of
+// their row-to-cell sums B (k_mg_rowcell), which is P1^T A P1 (rows that are
+// not unknowns have B = 0).  Nine coalesced loads per row instead of a walk
+// over the rows' entries.
+__global__ void k_mg_level1(Consts c, MgLevel L, const float* __restrict__ B, size_t np, const int32_t* cs,
+                            int32_t* nact, int2* act_rng) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= L.nx * L.ny) return;
-    const int cx = I / L.ny, cy = I - cx * L.ny;
     float st[9];
 #pragma unroll
     for (int d = 0; d < 9; d++) st[d] = 0.f;
-    const int b = mf.cs[I], e = mf.cs[I + 1];
-    int rs[3][4];
-    if (e > b) {
-        for (int r = 0; r < 3; r++) {
-            const int kk = (cx - 1 + r) * c.numY + cy - 1;
-            for (int q = 0; q < 4; q++) rs[r][q] = mf.cs[kk + q];
-        }
-    }
+    const int b = cs[I], e = cs[I + 1];
     for (int k = b; k < e; k++) {
-        const float dg = A.diag32[k];
-        if (!(dg > 0.f)) continue;  // not an unknown (not Inner)
-        st[4] += dg;
-        const int cnt = A.offcnt[k];
-        if (mf.enabled && !mf.sell_row[k]) {
-            // compact row: four groups of four entries per round of loads,
-            // entries added in order
-            const size_t q0 = qsell_index(k, 0, c.K) >> 2;
-            const float4* vp = reinterpret_cast<const float4*>(A.val32) + q0;
-            const uint32_t* ip = reinterpret_cast<const uint32_t*>(mf.idx8) + q0;
-            const int ng = (cnt + 3) >> 2;
-            for (int g0 = 0; g0 < ng; g0 += 4) {
-                float4 v[4];
-                uint32_t b4[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int gi = min(g0 + q, ng - 1);
-                    v[q] = __ldg(vp + gi * 32);
-                    b4[q] = __ldg(ip + gi * 32);
-                }
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const float vv[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
-#pragma unroll
-                    for (int t = 0; t < 4; t++) {
-                        if ((g0 + q) * 4 + t >= cnt) break;
-                        const int bt = (b4[q] >> (8 * t)) & 255;
-                        const int r = bt >> 6;
-                        const int j = rs[r][0] + (bt & 63);
-                        const int dy = (j >= rs[r][1]) + (j >= rs[r][2]) - 1;
-                        add_tap(st, r * 3 + (dy + 1), vv[t]);
-                    }
-                }
-            }
-        } else {
-            const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
-            for (int m = 0; m < cnt; m++) {
-                const float v = A.val32[qsell_index(k, m, c.K)];
-                const int j = A.col[base + (size_t)m * 32];
-                const int kj = mf.skey[j];
-                const int jx = kj / c.numY, jy = kj - jx * c.numY;
-                add_tap(st, (jx - cx + 1) * 3 + (jy - cy + 1), v);
-            }
-        }
+        for (int d = 0; d < 9; d++) st[d] += __ldg(B + (size_t)d * np + k);
     }
     const int n = L.nx * L.ny;
 #pragma unroll
@@ -278,13 +233,13 @@ void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg&
                      cudaStream_t st) {
     if (!mg.enabled) return;
     const int T = 256;
-    if (mg.smooth || mg.overlap) {
-        k_mg_rowcell<<<(c.n + T - 1) / T, T, 0, st>>>(c, A, mf, (size_t)mg.n_pad, mg.rowcell);
-        ++g_launches;
-    }
+    // the rows' 3x3-cell sums: the operator of modes 1 and 3, and level 1's stencil
+    k_mg_rowcell<<<(c.n + T - 1) / T, T, 0, st>>>(c, A, mf, (size_t)mg.n_pad, mg.rowcell);
+    ++g_launches;
     const MgLevel& L1 = mg.lev[1];
     k_mg_clear<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(mg);
-    k_mg_level1<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(c, A, mf, L1, mg.nact, mg.act1_rng);
+    k_mg_level1<<<(L1.nx * L1.ny + T - 1) / T, T, 0, st>>>(c, L1, mg.rowcell, (size_t)mg.n_pad, mf.cs, mg.nact,
+                                                             mg.act1_rng);
     g_launches += 2;
     for (int l = 1; l < mg.nlev; l++) {
         const MgLevel& C = mg.lev[l + 1];

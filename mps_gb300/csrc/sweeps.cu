@@ -740,32 +740,29 @@ __global__ void k_pressure_out(int n, const double* __restrict__ x, double* __re
     if (x_prev) x_prev[id[k]] = v;
 }
 
-// MPS::setMinimumPressure (src/mps.cpp:481-503)
-__global__ void __launch_bounds__(kThreads) k_min_pressure(Consts c, StateBuf s, NbList nb) {
+// MPS::setMinimumPressure (src/mps.cpp:481-503) for every particle that is
+// not Ignored, then MPS::calcPressureGradient (src/mps.cpp:505-533) for the
+// fluid ones, which use their own minimum: one kernel, two passes over the
+// particle's list (the second mostly from cache).
+template <bool PLANAR, bool MIXED>
+__global__ void __launch_bounds__(kThreads) k_gradient(Consts c, StateBuf s, NbList nb, double* ax,
+                                                       double* ay, double* az) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.n || s.bc[k] == BC_IGNORED) return;
-    double mn = s.p[k];
     const int np = nb.n_pad, m = nb.cnt[k];
+    double pmin = s.p[k];
     for (int q = 0; q < m; q++) {
         int j = nb.slot[(size_t)q * np + k];
         if (s.type[j] == T_DUMMY) continue;
         if (lt_cut(nb.dist[(size_t)q * np + k], c.re_p)) {
             double pj = s.p[j];
-            if (mn > pj) mn = pj;
+            if (pmin > pj) pmin = pj;
         }
     }
-    s.minp[k] = mn;
-}
-
-// MPS::calcPressureGradient (src/mps.cpp:505-533)
-template <bool PLANAR, bool MIXED>
-__global__ void __launch_bounds__(kThreads) k_gradient(Consts c, StateBuf s, NbList nb, double* ax,
-                                                       double* ay, double* az) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= c.n || s.type[k] != T_FLUID) return;
+    s.minp[k] = pmin;
+    // a fluid particle is never Ignored (only dummies and ghosts are)
+    if (s.type[k] != T_FLUID) return;
     const double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
-    const double pmin = s.minp[k];
-    const int np = nb.n_pad, m = nb.cnt[k];
     if (!MIXED) {
         double gx = 0.0, gy = 0.0, gz = 0.0;
         for (int q = 0; q < m; q++) {
@@ -1003,8 +1000,6 @@ void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb, 
                           DevStats* ds, cudaStream_t st) {
     int g = blocks_for(c.n);
     k_pressure_out<<<g, kThreads, 0, st>>>(c.n, x, s.p, s.pf, s.id, x_prev, ds);
-    ++g_launches;
-    k_min_pressure<<<g, kThreads, 0, st>>>(c, s, nb);
     ++g_launches;
     if (c.planar) {
         if (mixed) {
