@@ -268,14 +268,16 @@ void enqueue_pre_solve(mps_engine* e) {
     launch_bc_source(c, e->S(), e->nb, e->A, e->ds, st);
     launch_assemble(c, e->S(), e->nb, e->A, e->ds, st);
     launch_dirichlet(c, e->S(), e->nb, e->A, e->parent, e->has_surface, e->ds, st);
-    // solvePoissonEquation's symmetry test (src/mps.cpp:418-442)
-    launch_symmetry_check(c, e->S(), e->A, e->ds, st);
+    // solvePoissonEquation's symmetry test (src/mps.cpp:418-442); the mixed
+    // solver's setup reads the matrix anyway and forms the fingerprint there
+    if (!mixed) launch_symmetry_check(c, e->S(), e->A, e->ds, st);
 }
 
 // Mixed solver only: FP32 operator and multigrid hierarchy of this step.
 void enqueue_solver_setup(mps_engine* e) {
     if (e->precision != MPS_PRECISION_MIXED) return;
-    launch_mixed_setup(e->c, e->sc, e->A, e->mf, e->kv, e->S().id, e->warm_start != 0, e->st);
+    launch_mixed_setup(e->c, e->sc, e->A, e->mf, e->kv, e->S().id, e->warm_start != 0, e->ds, e->st);
+    launch_symmetry_locate(e->c, e->S(), e->A, e->ds, e->st);
     launch_mg_setup(e->c, e->A, e->mf, active_mg(e), e->st);
 }
 

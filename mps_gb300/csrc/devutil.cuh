@@ -160,6 +160,34 @@ __device__ __forceinline__ bool far32(const StateBuf& s, int j, float fx, float 
     return r > bound;
 }
 
+// Symmetry fingerprint of a matrix (the test of solvePoissonEquation,
+// src/mps.cpp:418-442): the term of stored off-diagonal entry (ri, ci) with
+// value v is sgn(ci - ri) H(min, max) bits(v) mod 2^64, H an odd 64-bit
+// hash of the unordered pair (the SplitMix64 finaliser of Steele, Lea and
+// Flood, 2014) and bits() the IEEE pattern (zeros canonical).  Integer sums
+// of these are exact and order-free: 0 for a bitwise symmetric matrix, and
+// not 0 for any other with probability 1 - 2^-64.
+__host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ unsigned long long entry_term(int ri, int ci, double v) {
+    const unsigned lo = (unsigned)min(ri, ci), hi = (unsigned)max(ri, ci);
+    const unsigned long long h = mix64(((unsigned long long)lo << 32) | hi) | 1ull;
+    const unsigned long long b = v == 0.0 ? 0ull : (unsigned long long)__double_as_longlong(v);
+    const unsigned long long t = h * b;
+    return ri < ci ? t : 0ull - t;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
 __device__ __forceinline__ void atomic_max_nonneg_double(unsigned long long* a, double v) {
     atomicMax(a, (unsigned long long)__double_as_longlong(v));
 }

@@ -222,6 +222,10 @@ void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, cons
 // when it is not zero; raises ST_ASYMMETRIC, which makes the solvers skip.
 void launch_symmetry_check(const Consts& c, const StateBuf& s, const Ppe& A, DevStats* ds,
                            cudaStream_t st);
+// The second half alone, after a kernel that accumulated the fingerprint
+// (the mixed setup does, over slots, while it reads the matrix).
+void launch_symmetry_locate(const Consts& c, const StateBuf& s, const Ppe& A, DevStats* ds,
+                            cudaStream_t st);
 // x_prev (may be null) receives the solution by particle id.
 void launch_pressure_post(const Consts& c, const StateBuf& s, const NbList& nb,
                           const double* x, double* x_prev, double* ax, double* ay, double* az,
@@ -355,8 +359,9 @@ void launch_mg_setup(const Consts& c, const Ppe& A, const MatFree& mf, const Mg&
                      cudaStream_t st);
 // FP32 copy of the assembled matrix in the compact layout of MatFree; with
 // warm set, also the solve's initial guess x (k.x_prev at the slots' ids on
-// rows with a diagonal, else 0).
+// rows with a diagonal, else 0); and the symmetry fingerprint of the matrix
+// (over slots) into ds->sym_fp, for launch_symmetry_locate.
 void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, MatFree& mf,
-                        const Krylov& k, const int32_t* ids, bool warm, cudaStream_t st);
+                        const Krylov& k, const int32_t* ids, bool warm, DevStats* ds, cudaStream_t st);
 
 }  // namespace mpsg

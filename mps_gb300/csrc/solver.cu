@@ -1616,48 +1616,55 @@ __global__ void __launch_bounds__(BS, MINB) k_cg_mixed_batched(const SceneSolve*
 // diagonal.  A row whose column lies 64 or more slots into its range keeps
 // the int32 columns (sell_row = 1).
 __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv, const int32_t* __restrict__ ids,
-                              int warm) {
+                              int warm, unsigned long long* __restrict__ sym_fp) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= c.n) return;
-    const double d = A.diag[k];
-    A.rsum32[k] = f32(A.rsum[k]);
-    // initial guess: the particle's solution of the last solve (rows without
-    // an unknown stay 0, as the zero start leaves them)
-    if (warm) kv.x[k] = d > 0.0 ? kv.x_prev[ids[k]] : 0.0;
-    A.diag32[k] = f32(d);
-    kv.inv_diag32[k] = d != 0.0 ? f32(ddiv(1.0, d)) : 1.f;
-    const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
-    const int w = A.slice_w[k >> 5];
-    const int wq = (w + 3) & ~3;
-    int8_t sell = 1;
-    if (mf.enabled) {
-        sell = 0;
-        const int32_t key = mf.skey[k];
-        int st[3] = {0, 0, 0};
-        if (key < c.nkeys) {
-            const int ix = key / c.numY, iy = key - ix * c.numY;
-            for (int r = 0; r < 3; r++) st[r] = mf.cs[(ix - 1 + r) * c.numY + iy - 1];
-        }
-        for (int r = 0; r < 3; r++) mf.rs[(size_t)r * mf.rs_stride + k] = st[r];
+    unsigned long long fp = 0;  // this row's terms of the symmetry fingerprint (over slots)
+    if (k < c.n) {
+        const double d = A.diag[k];
+        A.rsum32[k] = f32(A.rsum[k]);
+        // initial guess: the particle's solution of the last solve (rows without
+        // an unknown stay 0, as the zero start leaves them)
+        if (warm) kv.x[k] = d > 0.0 ? kv.x_prev[ids[k]] : 0.0;
+        A.diag32[k] = f32(d);
+        kv.inv_diag32[k] = d != 0.0 ? f32(ddiv(1.0, d)) : 1.f;
+        const size_t base = (size_t)(k >> 5) * c.K * 32 + (k & 31);
+        const int w = A.slice_w[k >> 5];
+        const int wq = (w + 3) & ~3;
         const int cnt = A.offcnt[k];
-        for (int m = 0; m < wq; m++) {
-            uint8_t b = 0;  // padding: range 0, offset 0, value 0
-            if (m < cnt) {
-                const int j = A.col[base + (size_t)m * 32];
-                int r = 2;
-                while (r > 0 && j < st[r]) r--;
-                const int off = j - st[r];
-                if (off >= 0 && off < 64)
-                    b = (uint8_t)((r << 6) | off);
-                else
-                    sell = 1;
+        int8_t sell = 1;
+        if (mf.enabled) {
+            sell = 0;
+            const int32_t key = mf.skey[k];
+            int st[3] = {0, 0, 0};
+            if (key < c.nkeys) {
+                const int ix = key / c.numY, iy = key - ix * c.numY;
+                for (int r = 0; r < 3; r++) st[r] = mf.cs[(ix - 1 + r) * c.numY + iy - 1];
             }
-            mf.idx8[qsell_index(k, m, c.K)] = b;
+            for (int r = 0; r < 3; r++) mf.rs[(size_t)r * mf.rs_stride + k] = st[r];
+            for (int m = 0; m < wq; m++) {
+                uint8_t b = 0;  // padding: range 0, offset 0, value 0
+                if (m < cnt) {
+                    const int j = A.col[base + (size_t)m * 32];
+                    int r = 2;
+                    while (r > 0 && j < st[r]) r--;
+                    const int off = j - st[r];
+                    if (off >= 0 && off < 64)
+                        b = (uint8_t)((r << 6) | off);
+                    else
+                        sell = 1;
+                }
+                mf.idx8[qsell_index(k, m, c.K)] = b;
+            }
+        }
+        mf.sell_row[k] = sell;
+        for (int m = 0; m < wq; m++) {
+            const double v = m < w ? A.val[base + (size_t)m * 32] : 0.0;
+            A.val32[qsell_index(k, m, c.K)] = m < w ? f32(v) : 0.f;
+            if (m < cnt) fp += entry_term(k, A.col[base + (size_t)m * 32], v);
         }
     }
-    mf.sell_row[k] = sell;
-    for (int m = 0; m < wq; m++)
-        A.val32[qsell_index(k, m, c.K)] = m < w ? f32(A.val[base + (size_t)m * 32]) : 0.f;
+    fp = warp_sum64(fp);
+    if ((threadIdx.x & 31) == 0 && fp) atomicAdd(sym_fp, fp);
 }
 
 // Co-resident blocks of a persistent kernel (0 if the configuration does not
@@ -1702,12 +1709,12 @@ void solver_setup(Krylov& k, int32_t /*n_pad*/, int device) {
 }
 
 void launch_mixed_setup(const Consts& c, const SortScratch& sc, const Ppe& A, MatFree& mf,
-                        const Krylov& k, const int32_t* ids, bool warm, cudaStream_t st) {
+                        const Krylov& k, const int32_t* ids, bool warm, DevStats* ds, cudaStream_t st) {
     mf.skey = sc.skey;
     mf.cs = sc.cell_start;
     mf.numY = c.numY;
     mf.nkeys = c.nkeys;
-    k_mixed_setup<<<(c.n + 255) / 256, 256, 0, st>>>(c, A, mf, k, ids, warm ? 1 : 0);
+    k_mixed_setup<<<(c.n + 255) / 256, 256, 0, st>>>(c, A, mf, k, ids, warm ? 1 : 0, &ds->sym_fp);
     ++g_launches;
 }
 

@@ -36,27 +36,6 @@ namespace {
 
 constexpr int kSymThreads = 256;
 
-__host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
-    // SplitMix64 finaliser (Steele, Lea and Flood, 2014)
-    z += 0x9e3779b97f4a7c15ull;
-    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-    return z ^ (z >> 31);
-}
-
-__device__ __forceinline__ unsigned long long entry_term(int ri, int ci, double v) {
-    const unsigned lo = (unsigned)min(ri, ci), hi = (unsigned)max(ri, ci);
-    const unsigned long long h = mix64(((unsigned long long)lo << 32) | hi) | 1ull;
-    const unsigned long long b = v == 0.0 ? 0ull : (unsigned long long)__double_as_longlong(v);
-    const unsigned long long t = h * b;
-    return ri < ci ? t : 0ull - t;
-}
-
-__device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
 
 // Rows of the engine's SELL-32 matrix (rows and columns are slots; ids map
 // them to particle ids), and of a plain CSR matrix (ids = rows).
@@ -152,9 +131,16 @@ void launch_symmetry_check(const Consts& c, const StateBuf& s, const Ppe& A, Dev
                            cudaStream_t st) {
     SellRows rows{A.offcnt, A.col, A.val, s.id, c.K, c.n};
     k_sym_fingerprint<<<grid_for(c.n), kSymThreads, 0, st>>>(rows, &ds->sym_fp);
+    ++g_launches;
+    launch_symmetry_locate(c, s, A, ds, st);
+}
+
+void launch_symmetry_locate(const Consts& c, const StateBuf& s, const Ppe& A, DevStats* ds,
+                            cudaStream_t st) {
+    SellRows rows{A.offcnt, A.col, A.val, s.id, c.K, c.n};
     k_sym_locate<<<grid_for(c.n), kSymThreads, 0, st>>>(rows, &ds->sym_fp, &ds->asym_big, &ds->asym_any,
                                                         &ds->status);
-    g_launches += 2;
+    ++g_launches;
 }
 
 // The message of a failed check: the reference's text for the first pair
