@@ -770,7 +770,7 @@ def run_ours(args, rank: int, world: int, dist):
                "d2h_bytes_per_step": int(hpos.nbytes + hvel.nbytes + hp.nbytes + hndr.nbytes
                                          + htype.nbytes + hbc.nbytes),
                "steps": args.e2e_steps,
-               "initial_guess": "zero (every step uploads its state; mps_upload restarts the guess)"}
+               "initial_guess": "the previous step's solution (kept across mps_upload)"}
     eng.close()
 
     others = {}

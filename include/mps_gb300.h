@@ -132,11 +132,13 @@ int mps_set_multigrid(mps_engine* e, int32_t mode, float omega, float scale);
 
 /* Initial guess of the MIXED solver.  previous = 1 (default): each solve
  * starts from the previous step's solution of the same particles (before
- * the negative-pressure clamp; 0 for particles that had no unknown, and for
- * the first step and the first after mps_upload); previous = 0: from zero,
- * as the reference's CG (Eigen's solve(), src/mps.cpp:452-460).  Either way
- * the solve stops at ||b - A x|| <= tol ||b||; only the iterations it takes
- * change.  The FP64 solver always starts from zero. */
+ * the negative-pressure clamp; 0 for particles that had no unknown and at
+ * the first step), kept across mps_upload; a guess whose residual exceeds
+ * ||b|| (a state replaced by the upload) is dropped for zero by the solve
+ * itself.  previous = 0: from zero, as the reference's CG (Eigen's solve(),
+ * src/mps.cpp:452-460).  Either way the solve stops at
+ * ||b - A x|| <= tol ||b||; only the iterations it takes change.  The FP64
+ * solver always starts from zero. */
 int mps_set_initial_guess(mps_engine* e, int32_t previous);
 
 /* Self-test of the device-side wait limits (no counterpart in the

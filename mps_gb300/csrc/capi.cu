@@ -932,8 +932,6 @@ int mps_upload(mps_engine* e, const double* pos, const double* vel, const int32_
     if (pos) k_vec3_from_host<<<G, T, 0, e->st>>>(n, s.id, ps, s.x, s.y, pl ? nullptr : s.z);
     if (vel) k_vec3_from_host<<<G, T, 0, e->st>>>(n, s.id, vs, s.vx, s.vy, pl ? nullptr : s.vz);
     if (type) k_type_from_host_order<<<G, T, 0, e->st>>>(n, s.id, ts, s.type);
-    // a new state: the next mixed solve starts from zero
-    CU(cudaMemsetAsync(e->kv.x_prev, 0, np * 8, e->st));
     CU(cudaStreamSynchronize(e->st));
     CU(cudaGetLastError());
     return MPS_OK;

@@ -1125,6 +1125,15 @@ __device__ __forceinline__ void solve_mixed(const Ppe& A, const MatFree& mf, con
         }
         if (!reduce_sync<1, BS>(gb, a0, t0, ds)) return;
         rn2 = t0[0];
+        if (a.warm && refine == 0 && rn2 > rhs2) {
+            // a guess worse than zero (a state replaced by mps_upload): start from zero
+            for (int i = gtid; i < a.n; i += gsz) {
+                kv.x[i] = 0.0;
+                kv.r[i] = A.src[i];
+            }
+            rn2 = rhs2;
+            if (!grid_sync(gb, ds)) return;
+        }
         if (rn2 < thr || refine >= a.max_refine || inner_total >= a.max_iter) break;
         refine++;
         // inner solve of A d = r / ||r|| (unit right-hand side), to the
@@ -1388,6 +1397,15 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
         }
         if (!reduce_sync<1, BS>(gb, a0, t0, ds)) return;
         rn2 = t0[0];
+        if (a.warm && refine == 0 && rn2 > rhs2) {
+            // a guess worse than zero (a state replaced by mps_upload): start from zero
+            for (int i = gtid; i < n; i += gsz) {
+                kv.x[i] = 0.0;
+                kv.r[i] = A.src[i];
+            }
+            rn2 = rhs2;
+            if (!grid_sync(gb, ds)) return;
+        }
         if (rn2 < thr || refine >= a.max_refine || inner_total >= a.max_iter) break;
         refine++;
         const float ithr = (float)fmax(a.inner_tol * a.inner_tol, 0.25 * thr / rn2);
