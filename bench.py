@@ -746,30 +746,40 @@ def run_ours(args, rank: int, world: int, dist):
     if prec == MIXED and not args.no_fp64:
         split = run_precision_split(prm, warm_state)
 
-    # end to end through the C ABI with host buffers, every step
+    # end to end through the C ABI with host buffers, every step, over the
+    # same physical steps as the device-resident window: a fresh engine from
+    # the initial state, the same warm-up, then each step uploads its state
+    # from pinned host memory and downloads the result
     e2e = None
     if not args.no_e2e:
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa
-        hpos, hvel, htype = pin(warm_state["pos"]), pin(warm_state["vel"]), pin(warm_state["type"])
+        ee = Engine(prm, pos, vel, types, precision=prec)
+        if prec == MIXED:
+            ee.set_initial_guess(args.initial_guess == "previous")
+        for _ in range(args.warmup):
+            ee.step()
+        st0 = ee.state()
+        hpos, hvel, htype = pin(st0["pos"]), pin(st0["vel"]), pin(st0["type"])
         hp, hndr, hbc = pin(np.zeros(n)), pin(np.zeros(n)), pin(np.zeros(n, np.int32))
-        eng.upload(hpos, hvel, htype)
-        eng.step()
+        k_e2e = args.e2e_steps if args.e2e_steps > 0 else args.steps
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            eng.upload(hpos, hvel, htype)
-            eng.step()
-            eng.download_into(pos=hpos, vel=hvel, pressure=hp, ndr=hndr, types=htype, bc=hbc)
+        for _ in range(k_e2e):
+            ee.upload(hpos, hvel, htype)
+            ee.step()
+            ee.download_into(pos=hpos, vel=hvel, pressure=hp, ndr=hndr, types=htype, bc=hbc)
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
         te = max_over_ranks(te, dist)
-        e2e = {"value": replica_throughput(nf, args.e2e_steps, te, world), "unit": UNIT,
+        ee.close()
+        e2e = {"value": replica_throughput(nf, k_e2e, te, world), "unit": UNIT,
                "h2d_bytes_per_step": int(hpos.nbytes + hvel.nbytes + htype.nbytes),
                "d2h_bytes_per_step": int(hpos.nbytes + hvel.nbytes + hp.nbytes + hndr.nbytes
                                          + htype.nbytes + hbc.nbytes),
-               "steps": args.e2e_steps,
+               "steps": k_e2e,
+               "window": "the same steps as the device-resident timing (same initial state and warm-up)",
                "initial_guess": "the previous step's solution (kept across mps_upload)"}
     eng.close()
 
@@ -850,7 +860,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--initial-guess", default="previous", choices=["previous", "zero"],
                     help="the mixed solver's start: the previous step's solution, or zero as the reference's CG")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0: the same K as the timed steps")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--trajectory-steps", type=int, default=500,
                     help="mixed vs FP64 accuracy window (0: skip)")
