@@ -69,9 +69,13 @@ def workload_config(name: str, prm: dict, nf: int, n: int) -> dict:
 
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region:
+    the sampler is started (and its first sample awaited) before the region,
+    the region's host wall-clock bounds are marked, and the summary keeps the
+    samples whose timestamps fall inside them (the one nearest to the middle
+    if the region is shorter than the sampling interval)."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -79,16 +83,23 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.path = os.path.join(tempfile.gettempdir(), f"mps_clocks_{os.getpid()}.csv")
+        self.window = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            t_end = time.time() + 3.0
+            while time.time() < t_end and os.path.getsize(self.path) == 0:
+                time.sleep(0.01)
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
+
+    def mark(self, t0: float, t1: float):
+        self.window = (t0, t1)
 
     def __exit__(self, *a):
         if self.proc:
@@ -99,26 +110,35 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        import datetime
+
         if not os.path.exists(self.path):
             return None
-        sm, mx, reasons = [], [], set()
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(f[2]), float(f[3]),
+                             {nm for nm, v in zip(names, f[6:10]) if v.lower() == "active"}))
             except ValueError:
                 continue
-            for nm, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        if not sm:
+        if not rows:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
-                "reasons": sorted(reasons), "samples": len(sm)}
+        inside = rows
+        if self.window:
+            t0, t1 = self.window
+            inside = [r for r in rows if t0 <= r[0] <= t1]
+            if not inside:  # shorter than the interval: the sample nearest the middle
+                mid = 0.5 * (t0 + t1)
+                inside = [min(rows, key=lambda r: abs(r[0] - mid))]
+        reasons = set().union(*(r[3] for r in inside))
+        return {"sm_mhz": statistics.median(r[1] for r in inside), "sm_max_mhz": max(r[2] for r in inside),
+                "reasons": sorted(reasons), "samples": len(inside),
+                "window_s": round(self.window[1] - self.window[0], 4) if self.window else None}
 
 
 # ---------------------------------------------------------------- roofline
@@ -688,7 +708,9 @@ def run_ours(args, rank: int, world: int, dist):
     for _ in range(args.warmup):
         eng.step()
     with ClockSampler(dev) as clk:
+        t_w0 = time.time()
         sec, stats = timed(eng, args.steps)
+        clk.mark(t_w0, time.time())
     clocks = clk.summary()
     sec = max_over_ranks(sec, dist)
     value = replica_throughput(nf, args.steps, sec, world)
