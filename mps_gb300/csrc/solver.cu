@@ -262,16 +262,32 @@ __device__ __forceinline__ void sum_partials_f2(const GridBar& gb, const F2* par
     __shared__ float s_tot[M];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (warp == 0) {
+        // each lane sums blocks lane, lane + 32, ... in that order; the loads
+        // of five of them for every m are issued before any is used
+        F2 a[M];
 #pragma unroll
-        for (int m = 0; m < M; m++) {
-            F2 a = {0.f, 0.f};
-            for (int b = lane; b < gb.size; b += 32) {
-                const float2 q = __ldcg(reinterpret_cast<const float2*>(part + b * 8 + m));
-                a = f2_add(a, F2{q.x, q.y});
+        for (int m = 0; m < M; m++) a[m] = F2{0.f, 0.f};
+        for (int b0 = lane; b0 < gb.size; b0 += 32 * 5) {
+            float2 q[M][5];
+#pragma unroll
+            for (int u = 0; u < 5; u++) {
+                const int b = b0 + 32 * u;
+#pragma unroll
+                for (int m = 0; m < M; m++)
+                    q[m][u] = b < gb.size ? __ldcg(reinterpret_cast<const float2*>(part + b * 8 + m))
+                                          : make_float2(0.f, 0.f);
             }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) a = f2_add(a, f2_shfl_down(a, o));
-            if (lane == 0) s_tot[m] = a.hi + a.lo;
+            for (int u = 0; u < 5; u++)
+#pragma unroll
+                for (int m = 0; m < M; m++)
+                    if (b0 + 32 * u < gb.size) a[m] = f2_add(a[m], F2{q[m][u].x, q[m][u].y});
+        }
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a[m] = f2_add(a[m], f2_shfl_down(a[m], o));
+            if (lane == 0) s_tot[m] = a[m].hi + a[m].lo;
         }
     }
     __syncthreads();
