@@ -68,7 +68,9 @@ void drop_graph(mps_batch* b) {
     b->gexec = nullptr;
 }
 
-int configure(mps_batch* b, int block, double alpha) {
+// warm = false: every scene's solve starts from zero (the autotuner's
+// candidates solve the same systems one after another and must start alike).
+int configure(mps_batch* b, int block, double alpha, bool warm = true) {
     std::vector<BatchScene> sc;
     const size_t per = (size_t)2 * b->max_grid * 8;
     for (size_t s = 0; s < b->eng.size(); s++) {
@@ -81,7 +83,8 @@ int configure(mps_batch* b, int block, double alpha) {
         mf.cs = e->sc.cell_start;
         mf.numY = e->c.numY;
         mf.nkeys = e->c.nkeys;
-        sc.push_back(BatchScene{e->c, e->A, mf, engine_active_mg(e), kv, e->ds, b->tol, mi});
+        sc.push_back(BatchScene{e->c, e->A, mf, engine_active_mg(e), kv, e->ds, b->tol, mi,
+                                warm ? e->warm_start : 0});
     }
     const int rc = batch_solve_setup(sc, block, alpha, b->device, b->bs);
     if (rc == 1) return bfail(MPS_ERR_ARG, "batch: more scenes than co-resident solver blocks");
@@ -132,7 +135,7 @@ int tuned_step(mps_batch* b) {
     double ba = 1.0;
     for (int blk : kBlocks)
         for (double al : kAlphas) {
-            int rc = configure(b, blk, al);
+            int rc = configure(b, blk, al, false);
             if (rc) return rc;
             float ms = 0.f;
             for (int rep = 0; rep < 2; rep++) {  // the second run is timed

@@ -334,6 +334,7 @@ struct BatchScene {
     DevStats* ds;
     double tol;
     int64_t max_iter;
+    int32_t warm;  // the scene's x holds its initial guess (mps_set_initial_guess)
 };
 struct BatchSolve {
     int32_t n_scenes = 0;

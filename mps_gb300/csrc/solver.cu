@@ -1867,7 +1867,9 @@ int batch_solve_setup(const std::vector<BatchScene>& scenes, int block, double a
     std::vector<int2> bmap;
     for (int s = 0; s < ns; s++) {
         const BatchScene& q = scenes[s];
-        hs[s] = SceneSolve{q.A, q.mf, q.mg, q.kv, make_args(q.c, q.tol, q.max_iter), q.ds};
+        SolveArgs a = make_args(q.c, q.tol, q.max_iter);
+        a.warm = q.warm ? 1 : 0;
+        hs[s] = SceneSolve{q.A, q.mf, q.mg, q.kv, a, q.ds};
         for (int r = 0; r < gs[s]; r++) bmap.push_back(make_int2(s, r));
     }
     if (cudaMalloc(&b.scenes, sizeof(SceneSolve) * ns) != cudaSuccess ||
