@@ -759,17 +759,34 @@ __device__ void mg_block_cycle(const Mg& mg, int lo) {
         group_bar<NT>();
     }
     {
-        // coarsest level: e = A_c^-1 r, one warp per row (lanes split the row)
+        // coarsest level: e = A_c^-1 r, one warp per row (lanes split the
+        // row); a warp's rows (up to kDenseRows of them) in one pass, so that
+        // all their loads are in flight together
+        constexpr int kDenseRows = 6;
         const MgLevel L = lev_view(mg, mg.nlev, bsw);
         float* out = mg.nlev == lo ? L.t : L.e;
         const int n = L.nx * L.ny;
-        const int lane = tid & 31;
-        for (int i = tid >> 5; i < n; i += nt >> 5) {
-            float acc = 0.f;
-            for (int j = lane; j < n; j += 32) acc = fmaf(__ldg(mg.dense + i * n + j), ldv(L.r, j), acc);
+        const int lane = tid & 31, nw = nt >> 5;
+        for (int i0 = tid >> 5; i0 < n; i0 += kDenseRows * nw) {
+            float acc[kDenseRows];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) out[i] = ldc(L.invd, i) > 0.f ? acc : 0.f;
+            for (int q = 0; q < kDenseRows; q++) acc[q] = 0.f;
+            for (int j = lane; j < n; j += 32) {
+                const float rj = ldv(L.r, j);
+#pragma unroll
+                for (int q = 0; q < kDenseRows; q++) {
+                    const int i = i0 + q * nw;
+                    if (i < n) acc[q] = fmaf(__ldg(mg.dense + i * n + j), rj, acc[q]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kDenseRows; q++) {
+                const int i = i0 + q * nw;
+                float a = acc[q];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+                if (lane == 0 && i < n) out[i] = ldc(L.invd, i) > 0.f ? a : 0.f;
+            }
         }
         group_bar<NT>();
     }
