@@ -1683,36 +1683,46 @@ __global__ void k_mixed_setup(Consts c, Ppe A, MatFree mf, Krylov kv, const int3
         const int wq = (w + 3) & ~3;
         const int cnt = A.offcnt[k];
         int8_t sell = 1;
+        int st[3] = {0, 0, 0};
         if (mf.enabled) {
             sell = 0;
             const int32_t key = mf.skey[k];
-            int st[3] = {0, 0, 0};
             if (key < c.nkeys) {
                 const int ix = key / c.numY, iy = key - ix * c.numY;
                 for (int r = 0; r < 3; r++) st[r] = mf.cs[(ix - 1 + r) * c.numY + iy - 1];
             }
             for (int r = 0; r < 3; r++) mf.rs[(size_t)r * mf.rs_stride + k] = st[r];
-            for (int m = 0; m < wq; m++) {
-                uint8_t b = 0;  // padding: range 0, offset 0, value 0
+        }
+        // four entries per pass: one 16-byte value word and one 4-byte word
+        // of index bytes (padding: range 0, offset 0, value 0)
+        for (int m0 = 0; m0 < wq; m0 += 4) {
+            float v4[4];
+            uint32_t b4 = 0;
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int m = m0 + t;
+                const size_t e = base + (size_t)m * 32;
+                const double v = m < w ? A.val[e] : 0.0;
+                v4[t] = m < w ? f32(v) : 0.f;
                 if (m < cnt) {
-                    const int j = A.col[base + (size_t)m * 32];
-                    int r = 2;
-                    while (r > 0 && j < st[r]) r--;
-                    const int off = j - st[r];
-                    if (off >= 0 && off < 64)
-                        b = (uint8_t)((r << 6) | off);
-                    else
-                        sell = 1;
+                    const int j = A.col[e];
+                    fp += entry_term(k, j, v);
+                    if (mf.enabled) {
+                        int r = 2;
+                        while (r > 0 && j < st[r]) r--;
+                        const int off = j - st[r];
+                        if (off >= 0 && off < 64)
+                            b4 |= (uint32_t)((r << 6) | off) << (8 * t);
+                        else
+                            sell = 1;
+                    }
                 }
-                mf.idx8[qsell_index(k, m, c.K)] = b;
             }
+            const size_t q = qsell_index(k, m0, c.K);  // a multiple of 4
+            reinterpret_cast<float4*>(A.val32)[q >> 2] = make_float4(v4[0], v4[1], v4[2], v4[3]);
+            if (mf.enabled) reinterpret_cast<uint32_t*>(mf.idx8)[q >> 2] = b4;
         }
         mf.sell_row[k] = sell;
-        for (int m = 0; m < wq; m++) {
-            const double v = m < w ? A.val[base + (size_t)m * 32] : 0.0;
-            A.val32[qsell_index(k, m, c.K)] = m < w ? f32(v) : 0.f;
-            if (m < cnt) fp += entry_term(k, A.col[base + (size_t)m * 32], v);
-        }
     }
     fp = warp_sum64(fp);
     if ((threadIdx.x & 31) == 0 && fp) atomicAdd(sym_fp, fp);
