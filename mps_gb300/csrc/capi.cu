@@ -263,9 +263,8 @@ void enqueue_pre_solve(mps_engine* e) {
     if (taping) tape_phase(e, TAPE_COLLISION);
     launch_rebuild(c, e->S(), e->buf[e->cur ^ 1], e->sc, e->ds, st);
     e->swap();
-    launch_build_list(c, e->S(), e->sc, e->nb, e->ds, st);
+    launch_build_list_bc_source(c, e->S(), e->sc, e->nb, e->A, e->ds, st);
     if (taping) tape_phase(e, TAPE_LIST2);
-    launch_bc_source(c, e->S(), e->nb, e->A, e->ds, st);
     launch_assemble(c, e->S(), e->nb, e->A, e->ds, st);
     launch_dirichlet(c, e->S(), e->nb, e->A, e->parent, e->has_surface, e->ds, st);
     // solvePoissonEquation's symmetry test (src/mps.cpp:418-442); the mixed

@@ -210,8 +210,10 @@ void launch_collision(const Consts& c, const StateBuf& s, const SortScratch& sc,
                       int32_t pair_cap, int32_t* scan_tmp, DevStats* ds, cudaStream_t st);
 void launch_build_list(const Consts& c, const StateBuf& s, const SortScratch& sc,
                        const NbList& nb, DevStats* ds, cudaStream_t st);
-void launch_bc_source(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
-                      DevStats* ds, cudaStream_t st);
+// The pressure part's build: the list, and with it setBoundaryCondition and
+// setSourceTerm (src/mps.cpp:262-320; the higher-order source after it).
+void launch_build_list_bc_source(const Consts& c, const StateBuf& s, const SortScratch& sc,
+                                 const NbList& nb, const Ppe& A, DevStats* ds, cudaStream_t st);
 void launch_assemble(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
                      DevStats* ds, cudaStream_t st);
 void launch_dirichlet(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
@@ -292,9 +294,9 @@ struct Mg {
     int32_t* nact;  // per level: the length of lev[l].act (device, written by the setup)
     int2* act1_rng; // per entry of lev[1].act: the cell's first slot and slot count
     // per slot, for the overlapped solve's fused level-1 sums: if the slot is
-    // the last of a level-1 cell with unknowns, (cell | min(slots, 255) << 24,
-    // bits of the cell's 1/diagonal), else (-1, 0) (n_pad)
-    int2* cell_end;
+    // the last of a level-1 cell with unknowns, cell | min(slots, 255) << 24,
+    // else -1 (n_pad)
+    int32_t* cell_end;
 };
 
 // --------------------------------------------------------------- solver.cu

@@ -1389,11 +1389,11 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
         // the last slots of the level-1 cells with unknowns (fixed for the solve)
         if (fuse1) {
             const int key = __ldg(mf.skey + i);
-            int2 ce = make_int2(-1, 0);
+            int32_t ce = -1;
             if (key < n1 && (i == n - 1 || key != __ldg(mf.skey + i + 1))) {
                 const float iv = __ldg(mg.lev[1].invd + key);
                 const int len = i + 1 - __ldg(mf.cs + key);
-                if (iv > 0.f) ce = make_int2(key | (min(len, 255) << 24), __float_as_int(iv));
+                if (iv > 0.f) ce = key | (min(len, 255) << 24);
             }
             mg.cell_end[i] = ce;
         }
@@ -1566,7 +1566,7 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
                 float* ring = s_ring[warp];
                 for (int base = rlo; base < rhi; base += 64) {
                     float u[2], p[2], sv[2], w[2], x[2], r[2], id[2];
-                    int2 ce[2];
+                    int32_t ce[2];
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
                         const int i = min(base + 32 * h + lane, rhi - 1);
@@ -1577,7 +1577,7 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
                         x[h] = kv.x32[i];
                         r[h] = __ldcg(kv.r32 + i);
                         id[h] = kv.inv_diag32[i];
-                        ce[h] = fuse1 ? __ldg(mg.cell_end + i) : make_int2(-1, 0);
+                        ce[h] = fuse1 ? __ldg(mg.cell_end + i) : -1;
                     }
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
@@ -1598,9 +1598,10 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
                         const int i = base + 32 * h + lane;
-                        if (i < rhi && ce[h].x >= 0) {
-                            const int key = ce[h].x & 0xFFFFFF;
-                            int len = (int)((unsigned)ce[h].x >> 24);
+                        if (i < rhi && ce[h] >= 0) {
+                            const int key = ce[h] & 0xFFFFFF;
+                            const float iv = __ldg(mg.lev[1].invd + key);
+                            int len = (int)((unsigned)ce[h] >> 24);
                             if (len == 255) len = i + 1 - __ldg(mf.cs + key);
                             const int j0 = i + 1 - len;
                             float acc = 0.f;
@@ -1609,7 +1610,7 @@ __device__ __forceinline__ void solve_mixed_overlap(const Ppe& A, const MatFree&
                             for (int j = j0; j <= i; j++)
                                 acc += j >= keep ? ring[(j - rlo) & (kRing - 1)] : __ldcg(kv.r32 + j);
                             r1[key] = acc;
-                            e1n[key] = mg.omega * __int_as_float(ce[h].y) * acc;
+                            e1n[key] = mg.omega * iv * acc;
                         }
                     }
                     __syncwarp();

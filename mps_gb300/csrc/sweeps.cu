@@ -419,16 +419,21 @@ __global__ void __launch_bounds__(kThreads) k_coll_wave(Consts c, StateBuf s, co
 // MPS::setNeighbors (src/mps.cpp:585-619): the neighbour list of the build
 // that the pressure part uses, stored column-major (slot, FP64 distance,
 // FP64 weight at re_p), plus the number density at re_p (kept per particle
-// as the value a stale-list read returns once it becomes a ghost).
-template <bool PLANAR>
+// as the value a stale-list read returns once it becomes a ghost).  With BC
+// (the pressure part's build) the same pass also runs setBoundaryCondition
+// and the classic setSourceTerm (src/mps.cpp:262-320): the surface number
+// density summed over the list entries within re_s, in list order (the
+// order in which the reference's getNumberDensity reads the stored list).
+template <bool PLANAR, bool BC>
 __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
                                                          const int32_t* __restrict__ skey,
                                                          const int32_t* __restrict__ cs, NbList nb,
-                                                         DevStats* ds) {
+                                                         Ppe A, DevStats* ds) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = k < c.n && s.type[k] != T_GHOST;
     const int np = nb.n_pad;
     int m = 0;
+    double nd = 0.0, nsurf = 0.0;  // number densities at re_p and (BC) re_s
     if (valid) {
         const double xi = s.x[k], yi = s.y[k], zi = PLANAR ? 0.0 : s.z[k];
         const float2 fk = s.xyf[k];
@@ -443,7 +448,6 @@ __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
             if (ns < c.K) nb.slot[(size_t)ns * np + k] = j;
             ns++;
         });
-        double nd = 0.0;
         if (ns <= c.K) {
             // exact test, compacting in place (order kept): src/mps.cpp:585-619
             for (int q = 0; q < ns; q++) {
@@ -453,6 +457,7 @@ __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
                 const double dist = dsqrt(d2);
                 const double w = weight(dist, c.re_p);
                 if (lt_cut(dist, c.re_p)) nd = dadd(nd, w);  // src/mps.cpp:573-583
+                if (BC && lt_cut(dist, c.re_s)) nsurf = dadd(nsurf, weight(dist, c.re_s));
                 const size_t e = (size_t)m * np + k;
                 nb.slot[e] = j;
                 nb.dist[e] = dist;
@@ -469,6 +474,7 @@ __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
                 const double w = weight(dist, c.re_p);
                 if (lt_cut(dist, c.re_p)) nd = dadd(nd, w);
                 if (m < c.K) {
+                    if (BC && lt_cut(dist, c.re_s)) nsurf = dadd(nsurf, weight(dist, c.re_s));
                     const size_t e = (size_t)m * np + k;
                     nb.slot[e] = j;
                     nb.dist[e] = dist;
@@ -481,39 +487,26 @@ __global__ void __launch_bounds__(kThreads) k_build_list(Consts c, StateBuf s,
     }
     if (k < c.n) nb.cnt[k] = m < c.K ? m : c.K;
     if (m > c.K) raise_status(ds, ST_CAPACITY);
+    if (BC) {
+        int8_t bc = BC_IGNORED;
+        if (k < c.n) {
+            const int8_t t = s.type[k];
+            if (t != T_GHOST && t != T_DUMMY) bc = nsurf < c.beta_n0s ? BC_SURFACE : BC_INNER;
+            s.bc[k] = bc;
+            double b = 0.0;
+            if (bc == BC_INNER && !c.ho_on) b = ddiv(dmul(c.src_g1, dsub(nd, c.n0_p)), c.n0_p);
+            A.src[k] = b;
+        }
+        const unsigned in_mask = __ballot_sync(0xffffffffu, k < c.n && bc == BC_INNER);
+        const unsigned sf_mask = __ballot_sync(0xffffffffu, k < c.n && bc == BC_SURFACE);
+        if ((threadIdx.x & 31) == 0) {
+            if (in_mask) atomicAdd(&ds->n_inner, __popc(in_mask));
+            if (sf_mask) atomicAdd(&ds->n_surface, __popc(sf_mask));
+        }
+    }
     // one atomic per warp for the largest neighbour count
     const int wmax = __reduce_max_sync(0xffffffffu, m);
     if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(&ds->max_neighbors, wmax);
-}
-
-// setBoundaryCondition + setSourceTerm (classic form), src/mps.cpp:262-320.
-__global__ void __launch_bounds__(kThreads) k_bc_source(Consts c, StateBuf s, NbList nb, Ppe A,
-                                                        DevStats* ds) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= c.n) return;
-    int8_t t = s.type[k];
-    int8_t bc;
-    if (t == T_GHOST || t == T_DUMMY) {
-        bc = BC_IGNORED;
-    } else {
-        const int np = nb.n_pad, m = nb.cnt[k];
-        double ns = 0.0;
-        for (int q = 0; q < m; q++) {
-            double dist = nb.dist[(size_t)q * np + k];
-            if (lt_cut(dist, c.re_s)) ns = dadd(ns, weight(dist, c.re_s));
-        }
-        bc = ns < c.beta_n0s ? BC_SURFACE : BC_INNER;
-    }
-    s.bc[k] = bc;
-    double b = 0.0;
-    if (bc == BC_INNER && !c.ho_on) b = ddiv(dmul(c.src_g1, dsub(s.nd_last[k], c.n0_p)), c.n0_p);
-    A.src[k] = b;
-    unsigned in_mask = __ballot_sync(__activemask(), bc == BC_INNER);
-    unsigned sf_mask = __ballot_sync(__activemask(), bc == BC_SURFACE);
-    if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) {
-        if (in_mask) atomicAdd(&ds->n_inner, __popc(in_mask));
-        if (sf_mask) atomicAdd(&ds->n_surface, __popc(sf_mask));
-    }
 }
 
 // Higher-order source term (src/mps.cpp:288-306), needs every neighbour's BC.
@@ -943,20 +936,26 @@ void launch_collision(const Consts& c, const StateBuf& s, const SortScratch& sc,
 void launch_build_list(const Consts& c, const StateBuf& s, const SortScratch& sc,
                        const NbList& nb, DevStats* ds, cudaStream_t st) {
     int g = blocks_for(c.n);
+    const Ppe none{};
     if (c.planar) {
-        k_build_list<true><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, ds);
+        k_build_list<true, false><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, none, ds);
         ++g_launches;
     } else {
-        k_build_list<false><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, ds);
+        k_build_list<false, false><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, none, ds);
         ++g_launches;
     }
 }
 
-void launch_bc_source(const Consts& c, const StateBuf& s, const NbList& nb, const Ppe& A,
-                      DevStats* ds, cudaStream_t st) {
+void launch_build_list_bc_source(const Consts& c, const StateBuf& s, const SortScratch& sc,
+                                 const NbList& nb, const Ppe& A, DevStats* ds, cudaStream_t st) {
     int g = blocks_for(c.n);
-    k_bc_source<<<g, kThreads, 0, st>>>(c, s, nb, A, ds);
-    ++g_launches;
+    if (c.planar) {
+        k_build_list<true, true><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, A, ds);
+        ++g_launches;
+    } else {
+        k_build_list<false, true><<<g, kThreads, 0, st>>>(c, s, sc.skey, sc.cell_start, nb, A, ds);
+        ++g_launches;
+    }
     if (c.ho_on) {
         if (c.planar) {
             k_source_ho<true><<<g, kThreads, 0, st>>>(c, s, nb, A);
