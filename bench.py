@@ -191,7 +191,7 @@ t0 = time.perf_counter()
 for _ in range(%(warmup)d):
     o.step()
 tw = time.perf_counter() - t0
-out = {"nf": nf, "n": int(len(t)), "warmup": %(warmup)d, "warmup_s": tw, "legs": []}
+out = {"wl": %(wl)r, "nf": nf, "n": int(len(t)), "warmup": %(warmup)d, "warmup_s": tw, "legs": []}
 for tol, solves, name in %(legs)r:
     if tol is None:
         o.set_cg(solves=solves)
@@ -231,7 +231,7 @@ def finish_cpu_1m(proc, threads: int, timeout: float = 3600) -> dict:
                              "cg_solves": leg["solves"], "cg_relative_error": leg["cg_error"]}
     ref = d["legs"][0]
     return {"value": d["nf"] / ref["seconds"], "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": (f"dambreak_1m itself ({d['nf']} fluid / {d['n']} particles) on the CPU oracle: "
+            "sample": (f"{d['wl']} itself ({d['nf']} fluid / {d['n']} particles) on the CPU oracle: "
                        f"{d['warmup']} warm-up steps with the CG capped at {CPU_WARMUP_CG} iterations "
                        f"({d['warmup_s']:.1f} s, untimed), then one full step per leg: "
                        + "; ".join(f"{x['name']}: {x['seconds']:.1f} s, {x['cg_iterations']} CG iterations "
