@@ -10,7 +10,9 @@ takes over a minute per step there, so these checks stand in for it.
   bitwise symmetric with rows only for Inner particles (src/mps.cpp:322-360);
 * from one developed state, one mixed step and one FP64 step give the same
   surface flags, pressures within the mixed solver's tolerance and positions
-  within 1e-9 m.
+  within 1e-9 m;
+* five steps as CUDA graph replays and as eager launches end in bit-identical
+  states (the solver's reductions have a fixed order).
 """
 import numpy as np
 import pytest
@@ -80,3 +82,24 @@ def test_full_size_lists_matrix_and_mixed_step():
     assert np.array_equal(mx["type"], fp["type"])
     assert rel_l2(mx["pressure"], fp["pressure"]) < 1e-6
     assert np.max(np.abs(mx["pos"] - fp["pos"])) < 1e-9
+
+
+def test_full_size_graph_replays_equal_eager_steps():
+    """Determinism at full size: the same five steps as CUDA graph replays and
+    as eager launches end in bit-identical states."""
+    m = engine_or_skip()
+    prm, pos, vel, t = _dambreak_1m()
+    out = []
+    for graphs in (True, False):
+        e = m.Engine(prm, pos, vel, t, precision=m.MIXED)
+        e.set_graphs(graphs)
+        st = [e.step() for _ in range(5)]
+        assert all(x["status"] == 0 for x in st)
+        if graphs:
+            assert st[-1]["graph_replayed"]
+        out.append((e.state(), [x["cg_iterations"] for x in st]))
+        e.close()
+    (a, ia), (b, ib) = out
+    assert ia == ib
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
